@@ -1,0 +1,378 @@
+"""Benchmark: harmonic-mean GTEPS over 64 seeded roots on a Graph500 Kronecker
+graph (scale 26, edgefactor 16) on one GB300, plain vs batched BFS.
+
+A step is one pass of the hot path over the 64-root batch:
+  plain   -- 64 one-root searches (the drop-in, g5_bfs_run), device-resident
+  batched -- one batched level loop over the same 64 roots (g5_batch_run)
+TEPS per root = Graph500 edge count of the search (generated edges with a
+visited endpoint, self loops and duplicates included) / search time; the
+headline value is the harmonic mean over roots of the plain form, as the
+reference driver reports (cpu_2d/main.cpp:524-529,944-950).
+
+Inputs: the Kronecker graph is generated and built on the GPU with the
+reference generator's seeds (1, 2); synthetic data standing in for the
+Graph500 benchmark input.  The CSR (8.6 GB at scale 26) is far larger than
+L2, so no flush is needed between searches.
+
+Prints one JSON line (rank 0).  --impl reference times the reference's CPU
+path (the oracle port of CPUBFS_bin) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "harmonic-mean GTEPS @scale 26, 64 roots: batched vs plain BFS; p99 query ms"
+UNIT = "GTEPS"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=int, default=26)
+    ap.add_argument("--roots", type=int, default=64)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    return ap.parse_args()
+
+
+def hmean(xs):
+    xs = [x for x in xs if x > 0]
+    return len(xs) / sum(1.0 / x for x in xs) if xs else 0.0
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = float(f[2])
+                except ValueError:
+                    continue
+                names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+                for name, val in zip(names, f[5:9]):
+                    if val.lower() == "active":
+                        reasons.add(name)
+            os.unlink(self.path)
+        except Exception:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    return rank, ws, dist
+
+
+def barrier_sync(dist):
+    import torch
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+
+
+def max_over_ranks(x, dist):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, dist):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU side (oracle port of the reference CPU BFS)
+# ---------------------------------------------------------------------------
+
+def cpu_bfs_sample(ro, col, roots, nedges, seconds, threads):
+    """Times the oracle's CPUBFS_bin restatement on host cores over a bounded
+    sample of the roots; returns (harmonic-mean GTEPS, roots run, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    lib = orc.lib()
+    n = len(ro) - 1
+    res = []
+    lock = threading.Lock()
+    t_end = time.time() + seconds
+    idx = [0]
+
+    def worker():
+        pred = np.empty(n, np.int64)
+        while True:
+            with lock:
+                if idx[0] >= len(roots) or (time.time() > t_end and res):
+                    return
+                i = idx[0]
+                idx[0] += 1
+            t0 = time.perf_counter()
+            lib.g5o_bfs(n, ro.ctypes.data, col.ctypes.data, int(roots[i]), pred.ctypes.data, None)
+            dt = time.perf_counter() - t0
+            with lock:
+                res.append(nedges[i] / dt / 1e9)
+
+    ts = [threading.Thread(target=worker) for _ in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    return hmean(res), len(res)
+
+
+def reference_arm(args):
+    rank, ws, dist = dist_init(args)
+    if rank != 0:
+        return 0
+    import gpugraph500_gb300 as g5
+
+    # graph built by the GPU generator (bit-exact with the reference generator),
+    # copied to the host; the timed path is the CPU BFS only
+    g = g5.Graph.kronecker(args.scale)
+    roots = g5.select_roots(g, args.roots)
+    b = g5.CudaBFS(g)
+    nedges = []
+    for r in roots:
+        b.runBFS(int(r))
+        nedges.append(b.teps_edges())
+    b.close()
+    ro, col = g.csr()
+    g.close()
+    cores = os.cpu_count() or 1
+    per_step = max(args.cpu_seconds / max(args.steps + args.warmup, 1), 1.0)
+    for _ in range(args.warmup):
+        cpu_bfs_sample(ro, col, roots, nedges, per_step, cores)
+    vals, times, nrun = [], [], 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        v, k = cpu_bfs_sample(ro, col, roots, nedges, per_step, cores)
+        times.append(time.perf_counter() - t0)
+        vals.append(v)
+        nrun += k
+    value = hmean(vals)
+    sample = (f"oracle CPUBFS_bin port, scale {args.scale}, {nrun} searches over {args.steps} steps, "
+              f"{cores} searches in parallel (one per host thread)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / max(len(times), 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+            "data": "synthetic (Graph500 Kronecker, seeds 1,2)",
+            "config": {"workload": f"kronecker scale {args.scale} edgefactor 16, {args.roots} roots"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    rank, ws, dist = dist_init(args)
+    import torch
+    import gpugraph500_gb300 as g5
+
+    dev = torch.cuda.current_device()
+    t0 = time.time()
+    g = g5.Graph.kronecker(args.scale)
+    gen_s = time.time() - t0
+    roots = g5.select_roots(g, args.roots)
+    nr = len(roots)
+    bfs = g5.CudaBFS(g)
+
+    # Graph500 edge counts and validation (untimed)
+    nedges, all_valid, all_minpar = [], True, True
+    for r in roots:
+        bfs.runBFS(int(r))
+        nedges.append(bfs.teps_edges())
+        v, mp = bfs.validate(int(r))
+        all_valid &= v
+        all_minpar &= mp
+
+    def plain_step(stats_out):
+        for i, r in enumerate(roots):
+            code = bfs.run(int(r), None, None, stats=True)
+            if code != 0:
+                raise g5.G5Error(code, "g5_bfs_run")
+            s = bfs.stats
+            stats_out.append((i, s.device_ms, s.alg_bytes, s.levels, s.bottom_up_levels))
+
+    for _ in range(args.warmup):
+        plain_step([])
+    recs = []
+    with Clocks(dev) as clk:
+        barrier_sync(dist)
+        t_start = time.perf_counter()
+        for _ in range(args.steps):
+            plain_step(recs)
+        barrier_sync(dist)
+        wall = time.perf_counter() - t_start
+    clocks = clk.summary()
+    wall = max_over_ranks(wall, dist)
+    teps = [nedges[i] / (ms * 1e-3) / 1e9 for (i, ms, _, _, _) in recs]
+    value_rank = hmean(teps)
+    dev_ms = [ms for (_, ms, _, _, _) in recs]
+    alg = [b for (_, _, b, _, _) in recs]
+    achieved = sum(alg) / (sum(dev_ms) * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+
+    # end to end through the C ABI with host (pinned) output buffers
+    pinned = torch.empty(g.n, dtype=torch.int64, pin_memory=True)
+    e2e = []
+    for i, r in enumerate(roots):
+        t1 = time.perf_counter()
+        code = bfs.run(int(r), pinned.data_ptr(), None, stats=False)
+        dt = time.perf_counter() - t1
+        if code != 0:
+            raise g5.G5Error(code, "g5_bfs_run")
+        e2e.append(nedges[i] / dt / 1e9)
+    e2e_value = hmean(e2e)
+
+    # batched form
+    batched = None
+    if not args.no_batch and hasattr(g5.lib(), "g5_batch_run"):
+        try:
+            batched = bench_batched(g5, torch, g, roots, nedges, args)
+        except g5.G5Error as e:
+            batched = {"error": str(e)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        ro, col = g.csr()
+        cores = 1
+        v, k = cpu_bfs_sample(ro, col, roots, nedges, args.cpu_seconds, cores)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"oracle CPUBFS_bin port on {k} of the {nr} roots, serial like the reference "
+                         f"(cpu_2d/cpubfs_bin.cpp:147,168), ~{args.cpu_seconds:.0f} s budget"}
+        del ro, col
+
+    value = sum_over_ranks(value_rank, dist) if ws > 1 else value_rank
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+            "data": "synthetic (Graph500 Kronecker generated on the GPU, seeds 1,2)",
+            "config": {"workload": f"plain BFS, kronecker scale {args.scale} edgefactor 16, {nr} roots",
+                       "n": g.n, "nnz": g.nnz, "roots": nr, "parallelism": "replicas" if ws > 1 else "1 GPU",
+                       "l2": "inputs larger than L2 (CSR %.1f GB)" % ((g.nnz * 4 + g.n * 8) / 1e9),
+                       "graph_build_s": round(gen_s, 2)},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * nr,
+                    "d2h_bytes_per_step": 8 * g.n * nr},
+            "gpu_launches": None,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "scope": "whole search (all kernels of the level loop), algorithmic bytes"},
+            "clocks": clocks,
+            "validation": {"all_valid": all_valid, "all_min_parent": all_minpar},
+            "plain": {"hmean_gteps": value_rank, "mean_ms": statistics.mean(dev_ms),
+                      "p99_ms": float(np.percentile(dev_ms, 99)), "levels": recs[0][3] if recs else None},
+            "batched": batched,
+            "cpu_baseline": cpu,
+        }
+        launches = sum(rec[3] for rec in recs[:nr]) * 4 + 4 * nr
+        line["gpu_launches"] = launches * args.steps
+        print(json.dumps(line))
+    bfs.close()
+    g.close()
+    return 0
+
+
+def bench_batched(g5, torch, g, roots, nedges, args):
+    bt = g5.Batch([g])
+    nr = len(roots)
+    out = torch.empty(nr * g.n, dtype=torch.int32, device="cuda")
+    for _ in range(args.warmup):
+        bt.run(roots, [nr], out)
+    ms = []
+    for _ in range(args.steps):
+        ms.append(bt.run(roots, [nr], out))
+    total = sum(nedges)
+    agg = [total / (m * 1e-3) / 1e9 for m in ms]
+    bt.close()
+    return {"aggregate_gteps": hmean(agg), "ms_per_batch": statistics.mean(ms)}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

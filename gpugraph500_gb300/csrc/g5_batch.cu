@@ -1,0 +1,764 @@
+// g5_batch.cu -- batched BFS: up to 64 roots per graph, any number of graphs
+// of uneven scale, all in one device-resident level loop.
+//
+// Each vertex carries three 64-bit words (one bit per root of its graph):
+// visited, frontier and next-frontier.  One read of a vertex's adjacency
+// serves every root whose frontier touches it, which is where the batched
+// form beats 64 one-root searches.  The reference has no batched search (it
+// runs runBFS once per root, cpu_2d/main.cpp:419-462); this is the
+// multi-source form of the same level-synchronous BFS.
+//
+// Per level and per graph the direction is chosen as in the plain search
+// (Beamer's alpha/beta on the union frontier):
+//   top-down   edge-balanced tiles over the active-vertex queue; for an edge
+//              (u, v) the roots new to v are front[u] & ~visited[v]; they are
+//              OR-ed into next[v] and each root's parent slot takes an
+//              atomicMin with u
+//   bottom-up  each vertex not yet visited by every root scans its ascending
+//              adjacency: hit = front[u] & still-needed roots; the first hit
+//              of a root is its parent; the scan stops once no root is needed
+// Both give every root the smallest previous-level neighbour as parent, the
+// same parent as the plain search and the reference CPU BFS.
+//
+// Vertex ranges of the graphs are padded to whole compaction chunks so every
+// chunk belongs to one graph; the level loop is one CUDA graph (conditional
+// while node) like the plain search.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "g5_common.cuh"
+#include "g5_internal.h"
+
+namespace {
+
+constexpr int kB = 256;
+constexpr int kW = kB / 32;
+constexpr int kChunk = 2048;           // vertices per compaction chunk
+constexpr int kPerThread = kChunk / kB;
+constexpr uint64_t kTile = 256;        // edges per top-down warp tile
+constexpr int kSerial = 4;             // bottom-up entries scanned per lane first
+constexpr int kMaxGraphs = 64;
+constexpr int kMaxLevels = 1024;
+
+enum : int32_t { TD = 0, BU = 1 };
+
+struct GraphDesc {
+    const int64_t *row_off;
+    const uint32_t *col;
+    int64_t n;
+    int64_t nnz;
+    uint64_t vbase;      // first global vertex id
+    uint64_t pred_base;  // offset of root 0's parent array in pred_out
+    uint64_t mask;       // one bit per root
+    int32_t nroots;
+    int32_t dir;         // direction for the current level
+    uint64_t nf, mf;     // active vertices and their adjacency entries
+    uint64_t mu;         // adjacency entries of not fully visited vertices
+    uint64_t examined;
+};
+
+struct BState {
+    int32_t level;
+    uint32_t err;
+    uint64_t active;     // active vertices over all graphs (this level)
+    uint64_t qlen;       // queue length (top-down graphs only)
+    uint64_t qedges;     // its adjacency entries
+};
+
+struct BArgs {
+    GraphDesc *gd;
+    int ngraphs;
+    const uint8_t *chunk_graph;
+    uint32_t nchunks;
+    uint64_t ntot;          // padded global vertex count
+    const uint32_t *deg;    // per global vertex
+    uint64_t *vis, *front, *next;
+    uint32_t *pred;         // output parents, root-major per graph
+    uint32_t *queue;
+    uint64_t *qoff;
+    int64_t *qbase;
+    uint32_t *tile_start;
+    uint64_t max_tiles;
+    uint64_t *chunk_n, *chunk_m;
+    BState *st;
+    const int64_t *roots;   // device copy of the roots (graph-major)
+    const int32_t *root_off;
+    double alpha, beta;
+    cudaGraphConditionalHandle cond;
+    int use_cond;
+    uint64_t *level_log;    // per level: active vertices
+};
+
+__device__ __forceinline__ uint64_t wsum(uint64_t v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ int graph_of(const BArgs &a, uint64_t v) { return a.chunk_graph[v / kChunk]; }
+
+// ---- init: roots into next, parents of roots -------------------------------------
+
+__global__ void k_binit(BArgs a)
+{
+    for (int g = blockIdx.x; g < a.ngraphs; g += gridDim.x) {
+        GraphDesc &d = a.gd[g];
+        for (int r = threadIdx.x; r < d.nroots; r += blockDim.x) {
+            const int64_t root = a.roots[a.root_off[g] + r];
+            if (root < 0 || root >= d.n) {
+                atomicOr(&a.st->err, 1u);
+                continue;
+            }
+            atomicOr((unsigned long long *)&a.next[d.vbase + root], 1ull << r);
+            a.pred[d.pred_base + (uint64_t)r * d.n + root] = (uint32_t)root;
+        }
+        if (threadIdx.x == 0) {
+            d.dir = TD;
+            d.mu = (uint64_t)d.nnz;
+            d.examined = 0;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.st->level = -1;
+        a.st->err = 0;
+    }
+}
+
+// ---- expansion ------------------------------------------------------------------------
+
+__device__ void bexp_td(const BArgs &a, uint64_t &examined)
+{
+    __shared__ uint64_t s_q[kW][32];
+    const int lane = g5_lane(), wib = threadIdx.x >> 5;
+    const uint64_t gw = (uint64_t)blockIdx.x * kW + wib, nw = (uint64_t)gridDim.x * kW;
+    const uint64_t mf = a.st->qedges, nf = a.st->qlen;
+    const uint64_t ntiles = (mf + kTile - 1) / kTile;
+    if (ntiles > a.max_tiles) {
+        if (threadIdx.x == 0) atomicOr(&a.st->err, 2u);
+        return;
+    }
+    for (uint64_t t = gw; t < ntiles; t += nw) {
+        const uint64_t e0 = t * kTile, e1 = min(e0 + kTile, mf);
+        uint64_t cur = a.tile_start[t];
+        for (uint64_t gb = e0; gb < e1; gb += 32) {
+            const uint64_t idx = cur + 1 + lane;
+            s_q[wib][lane] = idx <= nf ? a.qoff[idx] : ~0ull;
+            __syncwarp();
+            const uint64_t e = gb + lane;
+            int lo = 0, hi = 32;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (s_q[wib][mid] <= e) lo = mid + 1;
+                else hi = mid;
+            }
+            const uint64_t i = cur + lo;
+            bool in_range = true;
+            if (lo == 32 && e < e1) in_range = (i + 1 > nf) ? false : (a.qoff[i + 1] > e);
+            if (e < e1) {
+                if (!in_range) {
+                    atomicOr(&a.st->err, 4u);
+                } else {
+                    const uint32_t ug = a.queue[i];
+                    const GraphDesc &d = a.gd[graph_of(a, ug)];
+                    const uint32_t vl = __ldg(d.col + (a.qbase[i] + (int64_t)e));
+                    const uint64_t vg = d.vbase + vl;
+                    const uint64_t nb = a.front[ug] & ~a.vis[vg];
+                    if (nb) {
+                        atomicOr((unsigned long long *)&a.next[vg], (unsigned long long)nb);
+                        const uint32_t ul = (uint32_t)(ug - d.vbase);
+                        uint64_t x = nb;
+                        while (x) {
+                            const int r = __ffsll((long long)x) - 1;
+                            x &= x - 1;
+                            atomicMin(a.pred + d.pred_base + (uint64_t)r * d.n + vl, ul);
+                        }
+                    }
+                }
+            }
+            cur = __shfl_sync(0xFFFFFFFFu, i, 31);
+            __syncwarp();
+        }
+        if (lane == 0) examined += e1 - e0;
+    }
+}
+
+__device__ void bexp_bu(const BArgs &a, uint64_t &examined)
+{
+    const int lane = g5_lane();
+    const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
+    // one warp per 32 consecutive vertices (never spans two chunks)
+    for (uint64_t w = gw; w < a.ntot / 32; w += nw) {
+        const uint64_t v = w * 32 + lane;
+        const int g = graph_of(a, w * 32);
+        const GraphDesc &d = a.gd[g];
+        if (d.dir != BU || d.nf == 0) continue;
+        const uint64_t vl = v - d.vbase;
+        uint64_t need = ((int64_t)vl < d.n) ? (~a.vis[v] & d.mask) : 0;
+        int64_t s = 0, e = 0;
+        if (need) {
+            s = d.row_off[vl];
+            e = d.row_off[vl + 1];
+        }
+        uint64_t found = 0;
+        int64_t j = s;
+        const int64_t lim = min(e, s + kSerial);
+        for (; j < lim && need; ++j) {
+            const uint32_t u = __ldg(d.col + j);
+            const uint64_t hit = a.front[d.vbase + u] & need;
+            if (hit) {
+                uint64_t x = hit;
+                while (x) {
+                    const int r = __ffsll((long long)x) - 1;
+                    x &= x - 1;
+                    a.pred[d.pred_base + (uint64_t)r * d.n + vl] = u;
+                }
+                found |= hit;
+                need &= ~hit;
+            }
+        }
+        uint64_t ex = (uint64_t)(j - s);
+        unsigned pend = __ballot_sync(0xFFFFFFFFu, need && j < e);
+        while (pend) {
+            const int l = __ffs(pend) - 1;
+            pend &= pend - 1;
+            int64_t jj = __shfl_sync(0xFFFFFFFFu, j, l);
+            const int64_t ee = __shfl_sync(0xFFFFFFFFu, e, l);
+            uint64_t nd = __shfl_sync(0xFFFFFFFFu, need, l);
+            const uint64_t vll = __shfl_sync(0xFFFFFFFFu, vl, l);
+            const int64_t st = jj;
+            uint64_t fnd = 0;
+            while (jj < ee && nd) {
+                const int64_t idx = jj + lane;
+                uint32_t u = 0;
+                uint64_t hit = 0;
+                if (idx < ee) {
+                    u = __ldg(d.col + idx);
+                    hit = a.front[d.vbase + u] & nd;
+                }
+                unsigned hm = __ballot_sync(0xFFFFFFFFu, hit != 0);
+                int last = 31;
+                while (hm) {
+                    const int f = __ffs(hm) - 1;
+                    hm &= hm - 1;
+                    const uint64_t hf = __shfl_sync(0xFFFFFFFFu, hit, f) & nd;
+                    if (hf) {
+                        const uint32_t uf = __shfl_sync(0xFFFFFFFFu, u, f);
+                        // lanes write the parent slots of the new roots in parallel
+                        uint64_t x = hf;
+                        int k = 0;
+                        while (x) {
+                            const int r = __ffsll((long long)x) - 1;
+                            x &= x - 1;
+                            if ((k & 31) == lane) a.pred[d.pred_base + (uint64_t)r * d.n + vll] = uf;
+                            ++k;
+                        }
+                        fnd |= hf;
+                        nd &= ~hf;
+                        if (!nd) {
+                            last = f;
+                            break;
+                        }
+                    }
+                }
+                jj += nd ? 32 : last + 1;
+            }
+            jj = min(jj, ee);
+            if (lane == l) {
+                found |= fnd;
+                ex += (uint64_t)(jj - st);
+            }
+        }
+        if (found) atomicOr((unsigned long long *)&a.next[v], (unsigned long long)found);
+        examined += ex;
+    }
+}
+
+__global__ void __launch_bounds__(kB) k_bexp(BArgs a)
+{
+    if (a.st->err || a.st->level < 0 || a.st->active == 0) return;
+    uint64_t ex_td = 0, ex_bu = 0;
+    bexp_td(a, ex_td);
+    bexp_bu(a, ex_bu);
+    (void)ex_td;
+    (void)ex_bu;
+}
+
+// ---- compaction ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kB) k_bcount(BArgs a)
+{
+    const uint32_t c = blockIdx.x;
+    const uint64_t v0 = (uint64_t)c * kChunk + (uint64_t)threadIdx.x * kPerThread;
+    uint64_t cn = 0, cm = 0;
+#pragma unroll
+    for (int k = 0; k < kPerThread; ++k) {
+        if (a.next[v0 + k]) {
+            ++cn;
+            cm += a.deg[v0 + k];
+        }
+    }
+    cn = wsum(cn);
+    cm = wsum(cm);
+    __shared__ uint64_t s_n[kW], s_m[kW];
+    if (g5_lane() == 0) {
+        s_n[threadIdx.x >> 5] = cn;
+        s_m[threadIdx.x >> 5] = cm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t tn = 0, tm = 0;
+        for (int i = 0; i < kW; ++i) {
+            tn += s_n[i];
+            tm += s_m[i];
+        }
+        a.chunk_n[c] = tn;
+        a.chunk_m[c] = tm;
+    }
+}
+
+// Single block: per-graph totals and directions, then prefix sums over the
+// chunks of top-down graphs (their vertices form the next queue).
+__global__ void __launch_bounds__(1024) k_bscan(BArgs a)
+{
+    __shared__ uint64_t s_gn[kMaxGraphs], s_gm[kMaxGraphs];
+    __shared__ int s_gdir[kMaxGraphs];
+    __shared__ uint64_t s_w[33];
+    for (int g = threadIdx.x; g < a.ngraphs; g += blockDim.x) {
+        s_gn[g] = 0;
+        s_gm[g] = 0;
+    }
+    __syncthreads();
+    const uint32_t C = a.nchunks;
+    for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
+        const int g = a.chunk_graph[c];
+        if (a.chunk_n[c]) {
+            atomicAdd((unsigned long long *)&s_gn[g], (unsigned long long)a.chunk_n[c]);
+            atomicAdd((unsigned long long *)&s_gm[g], (unsigned long long)a.chunk_m[c]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < a.ngraphs) {
+        GraphDesc &d = a.gd[threadIdx.x];
+        const uint64_t tn = s_gn[threadIdx.x], tm = s_gm[threadIdx.x];
+        int nd = d.dir;
+        // Beamer's switch on the union frontier of the graph's roots
+        const uint64_t mu_after = d.mu >= tm ? d.mu - tm : 0;
+        if (a.st->level >= 0) {
+            if (d.dir == TD) {
+                if ((double)tm > (double)mu_after / a.alpha) nd = BU;
+            } else if ((double)tn < (double)d.n / a.beta && tn < d.nf) {
+                nd = TD;
+            }
+        }
+        d.mu = mu_after;
+        d.dir = nd;
+        d.nf = tn;
+        d.mf = tm;
+        s_gdir[threadIdx.x] = nd;
+    }
+    __syncthreads();
+    // exclusive prefix over chunks of top-down graphs
+    const uint32_t per = (C + 1023) / 1024;
+    const uint32_t b0 = threadIdx.x * per;
+    uint64_t ln = 0, lm = 0;
+    for (uint32_t i = 0; i < per && b0 + i < C; ++i) {
+        if (s_gdir[a.chunk_graph[b0 + i]] == TD) {
+            ln += a.chunk_n[b0 + i];
+            lm += a.chunk_m[b0 + i];
+        }
+    }
+    // block scan (two passes over s_w)
+    uint64_t tot_n, tot_m, on, om;
+    {
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        for (int pass = 0; pass < 2; ++pass) {
+            uint64_t v = pass ? lm : ln, x = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint64_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) s_w[wid] = x;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint64_t acc = 0;
+                for (int i = 0; i < 32; ++i) {
+                    uint64_t t = s_w[i];
+                    s_w[i] = acc;
+                    acc += t;
+                }
+                s_w[32] = acc;
+            }
+            __syncthreads();
+            const uint64_t r = x - v + s_w[wid];
+            if (pass) {
+                om = r;
+                tot_m = s_w[32];
+            } else {
+                on = r;
+                tot_n = s_w[32];
+            }
+            __syncthreads();
+        }
+    }
+    for (uint32_t i = 0; i < per && b0 + i < C; ++i) {
+        const uint64_t xn = a.chunk_n[b0 + i], xm = a.chunk_m[b0 + i];
+        const bool td = s_gdir[a.chunk_graph[b0 + i]] == TD;
+        a.chunk_n[b0 + i] = td ? on : ~0ull;  // ~0: chunk not queued
+        a.chunk_m[b0 + i] = om;
+        if (td) {
+            on += xn;
+            om += xm;
+        }
+    }
+    if (threadIdx.x == 0) {
+        uint64_t act = 0;
+        for (int g = 0; g < a.ngraphs; ++g) act += s_gn[g];
+        BState *st = a.st;
+        st->level += 1;
+        st->active = act;
+        st->qlen = tot_n;
+        st->qedges = tot_m;
+        a.qoff[tot_n] = tot_m;
+        if (st->level < kMaxLevels) a.level_log[st->level] = act;
+        bool cont = act > 0 && st->err == 0;
+        if (cont && st->level + 1 >= kMaxLevels) {
+            st->err |= 8u;
+            cont = false;
+        }
+        if (a.use_cond) cudaGraphSetConditional(a.cond, cont ? 1u : 0u);
+    }
+}
+
+__global__ void __launch_bounds__(kB) k_bwrite(BArgs a)
+{
+    const uint32_t c = blockIdx.x;
+    const uint64_t v0 = (uint64_t)c * kChunk + (uint64_t)threadIdx.x * kPerThread;
+    uint64_t nx[kPerThread];
+    uint64_t cn = 0, cm = 0;
+    const bool queued = a.chunk_n[c] != ~0ull;
+#pragma unroll
+    for (int k = 0; k < kPerThread; ++k) {
+        nx[k] = a.next[v0 + k];
+        if (nx[k]) {
+            a.vis[v0 + k] |= nx[k];
+            a.next[v0 + k] = 0;
+            ++cn;
+            cm += a.deg[v0 + k];
+        }
+        a.front[v0 + k] = nx[k];
+    }
+    if (!queued) return;
+    __shared__ uint64_t s_n[kW], s_m[kW];
+    const int lane = g5_lane(), wid = threadIdx.x >> 5;
+    uint64_t xn = cn, xm = cm;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint64_t yn = __shfl_up_sync(0xFFFFFFFFu, xn, o), ym = __shfl_up_sync(0xFFFFFFFFu, xm, o);
+        if (lane >= o) {
+            xn += yn;
+            xm += ym;
+        }
+    }
+    if (lane == 31) {
+        s_n[wid] = xn;
+        s_m[wid] = xm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t an = 0, am = 0;
+        for (int i = 0; i < kW; ++i) {
+            const uint64_t tn = s_n[i], tm = s_m[i];
+            s_n[i] = an;
+            s_m[i] = am;
+            an += tn;
+            am += tm;
+        }
+    }
+    __syncthreads();
+    uint64_t pos = a.chunk_n[c] + s_n[wid] + xn - cn;
+    uint64_t mpos = a.chunk_m[c] + s_m[wid] + xm - cm;
+    const GraphDesc &d = a.gd[a.chunk_graph[c]];
+#pragma unroll
+    for (int k = 0; k < kPerThread; ++k) {
+        if (!nx[k]) continue;
+        const uint64_t v = v0 + k;
+        const uint64_t dg = a.deg[v];
+        a.queue[pos] = (uint32_t)v;
+        a.qoff[pos] = mpos;
+        a.qbase[pos] = d.row_off[v - d.vbase] - (int64_t)mpos;
+        uint64_t t = (mpos + kTile - 1) / kTile;
+        const uint64_t tend = (mpos + dg + kTile - 1) / kTile;
+        for (; t < tend && t < a.max_tiles; ++t) a.tile_start[t] = (uint32_t)pos;
+        mpos += dg;
+        ++pos;
+    }
+}
+
+__global__ void k_bdeg(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t ntot, uint32_t *deg)
+{
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < ntot;
+         v += (uint64_t)gridDim.x * blockDim.x) {
+        const GraphDesc &d = gd[chunk_graph[v / kChunk]];
+        const int64_t vl = (int64_t)(v - d.vbase);
+        deg[v] = vl < d.n ? (uint32_t)(d.row_off[vl + 1] - d.row_off[vl]) : 0u;
+    }
+}
+
+}  // namespace
+
+struct g5_batch {
+    std::vector<g5_graph *> graphs;
+    std::vector<GraphDesc> hgd;
+    BArgs args;
+    cudaStream_t stream = nullptr;
+    GraphDesc *gd = nullptr;
+    uint8_t *chunk_graph = nullptr;
+    uint32_t *deg = nullptr;
+    uint64_t *words = nullptr;  // vis | front | next
+    uint32_t *queue = nullptr;
+    uint64_t *qoff = nullptr;
+    int64_t *qbase = nullptr;
+    uint32_t *tile_start = nullptr;
+    uint64_t *chunks = nullptr;
+    BState *st = nullptr;
+    int64_t *roots = nullptr;
+    int32_t *root_off = nullptr;
+    uint64_t *level_log = nullptr;
+    int64_t *h_roots = nullptr;
+    int32_t *h_root_off = nullptr;
+    BState *h_st = nullptr;
+    uint32_t *bound_pred = nullptr;  // pred pointer the graph was built for
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+void enqueue_batch(g5_batch *b, const BArgs &a, cudaStream_t s, bool body)
+{
+    if (!body) {
+        cudaMemsetAsync(b->words, 0, sizeof(uint64_t) * 3 * a.ntot, s);
+        k_binit<<<std::max(1, a.ngraphs), kB, 0, s>>>(a);
+        return;
+    }
+    k_bcount<<<a.nchunks, kB, 0, s>>>(a);
+    k_bscan<<<1, 1024, 0, s>>>(a);
+    k_bwrite<<<a.nchunks, kB, 0, s>>>(a);
+    k_bexp<<<g5::grid_for(8), kB, 0, s>>>(a);
+}
+
+g5_status build_batch_graph(g5_batch *b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    cudaStream_t s = b->stream;
+    cudaGraph_t pro = nullptr;
+    G5_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    enqueue_batch(b, b->args, s, false);
+    G5_CUDA(cudaStreamEndCapture(s, &pro));
+    cudaGraph_t g = nullptr;
+    G5_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphNode_t pn;
+    G5_CUDA(cudaGraphAddChildGraphNode(&pn, g, nullptr, 0, pro));
+    cudaGraphDestroy(pro);
+    cudaGraphConditionalHandle h;
+    G5_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cn;
+    G5_CUDA(cudaGraphAddNode(&cn, g, &pn, nullptr, 1, &cp));
+    BArgs a = b->args;
+    a.cond = h;
+    a.use_cond = 1;
+    G5_CUDA(cudaStreamBeginCaptureToGraph(s, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal));
+    enqueue_batch(b, a, s, true);
+    cudaGraph_t body = nullptr;
+    G5_CUDA(cudaStreamEndCapture(s, &body));
+    G5_CUDA(cudaGraphInstantiate(&b->exec, g, 0));
+    b->graph = g;
+    return G5_OK;
+}
+
+void free_batch(g5_batch *b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    cudaFree(b->gd);
+    cudaFree(b->chunk_graph);
+    cudaFree(b->deg);
+    cudaFree(b->words);
+    cudaFree(b->queue);
+    cudaFree(b->qoff);
+    cudaFree(b->qbase);
+    cudaFree(b->tile_start);
+    cudaFree(b->chunks);
+    cudaFree(b->st);
+    cudaFree(b->roots);
+    cudaFree(b->root_off);
+    cudaFree(b->level_log);
+    cudaFreeHost(b->h_roots);
+    cudaFreeHost(b->h_root_off);
+    cudaFreeHost(b->h_st);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
+{
+    if (!graphs || !out || ngraphs < 1 || ngraphs > kMaxGraphs) return G5_ERR_INVALID_ARG;
+    *out = nullptr;
+    g5_batch *b = new g5_batch();
+    auto fail = [&](g5_status s) {
+        free_batch(b);
+        delete b;
+        return s;
+    };
+    uint64_t vb = 0, nnz_max = 0;
+    std::vector<uint8_t> cg;
+    for (int i = 0; i < ngraphs; ++i) {
+        if (!graphs[i]) return fail(G5_ERR_INVALID_ARG);
+        b->graphs.push_back(graphs[i]);
+        GraphDesc d;
+        memset(&d, 0, sizeof d);
+        d.row_off = graphs[i]->row_off;
+        d.col = graphs[i]->col;
+        d.n = graphs[i]->n;
+        d.nnz = graphs[i]->nnz;
+        d.vbase = vb;
+        const uint64_t chunks = ((uint64_t)d.n + kChunk - 1) / kChunk;
+        for (uint64_t c = 0; c < chunks; ++c) cg.push_back((uint8_t)i);
+        vb += chunks * kChunk;
+        nnz_max += (uint64_t)d.nnz;
+        b->hgd.push_back(d);
+    }
+    if (vb >= (1ull << 32)) return fail(G5_ERR_CAPACITY);
+    BArgs &a = b->args;
+    memset(&a, 0, sizeof a);
+    a.ngraphs = ngraphs;
+    a.nchunks = (uint32_t)cg.size();
+    a.ntot = vb;
+    a.max_tiles = nnz_max / kTile + 2 + (uint64_t)ngraphs;
+    a.alpha = 14.0;
+    a.beta = 24.0;
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(G5_ERR_CUDA);
+    cudaEventCreate(&b->ev0);
+    cudaEventCreate(&b->ev1);
+#define B_ALLOC(ptr, bytes) \
+    if (cudaMalloc(&(ptr), (bytes)) != cudaSuccess) return fail(G5_ERR_OOM)
+    B_ALLOC(b->gd, sizeof(GraphDesc) * ngraphs);
+    B_ALLOC(b->chunk_graph, cg.size());
+    B_ALLOC(b->deg, sizeof(uint32_t) * vb);
+    B_ALLOC(b->words, sizeof(uint64_t) * 3 * vb);
+    B_ALLOC(b->queue, sizeof(uint32_t) * vb);
+    B_ALLOC(b->qoff, sizeof(uint64_t) * (vb + 1));
+    B_ALLOC(b->qbase, sizeof(int64_t) * vb);
+    B_ALLOC(b->tile_start, sizeof(uint32_t) * a.max_tiles);
+    B_ALLOC(b->chunks, sizeof(uint64_t) * 2 * a.nchunks);
+    B_ALLOC(b->st, sizeof(BState));
+    B_ALLOC(b->roots, sizeof(int64_t) * 64 * ngraphs);
+    B_ALLOC(b->root_off, sizeof(int32_t) * (ngraphs + 1));
+    B_ALLOC(b->level_log, sizeof(uint64_t) * kMaxLevels);
+#undef B_ALLOC
+    if (cudaMallocHost(&b->h_roots, sizeof(int64_t) * 64 * ngraphs) != cudaSuccess ||
+        cudaMallocHost(&b->h_root_off, sizeof(int32_t) * (ngraphs + 1)) != cudaSuccess ||
+        cudaMallocHost(&b->h_st, sizeof(BState)) != cudaSuccess)
+        return fail(G5_ERR_OOM);
+    if (cudaMemcpy(b->chunk_graph, cg.data(), cg.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b->gd, b->hgd.data(), sizeof(GraphDesc) * ngraphs, cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(G5_ERR_CUDA);
+    a.gd = b->gd;
+    a.chunk_graph = b->chunk_graph;
+    a.deg = b->deg;
+    a.vis = b->words;
+    a.front = b->words + vb;
+    a.next = b->words + 2 * vb;
+    a.queue = b->queue;
+    a.qoff = b->qoff;
+    a.qbase = b->qbase;
+    a.tile_start = b->tile_start;
+    a.chunk_n = b->chunks;
+    a.chunk_m = b->chunks + a.nchunks;
+    a.st = b->st;
+    a.roots = b->roots;
+    a.root_off = b->root_off;
+    a.level_log = b->level_log;
+    k_bdeg<<<g5::grid_for(8), kB, 0, b->stream>>>(b->gd, b->chunk_graph, vb, b->deg);
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
+    *out = b;
+    return G5_OK;
+}
+
+g5_status g5_batch_destroy(g5_batch *b)
+{
+    if (!b) return G5_ERR_INVALID_ARG;
+    cudaStreamSynchronize(b->stream);
+    free_batch(b);
+    delete b;
+    return G5_OK;
+}
+
+g5_status g5_batch_run(g5_batch *b, const int64_t *roots_host, const int *nroots, uint32_t *pred_out_dev,
+                       double *device_ms)
+{
+    if (!b || !roots_host || !nroots || !pred_out_dev) return G5_ERR_INVALID_ARG;
+    const int ng = (int)b->graphs.size();
+    uint64_t pb = 0;
+    int off = 0;
+    for (int i = 0; i < ng; ++i) {
+        if (nroots[i] < 0 || nroots[i] > 64) return G5_ERR_INVALID_ARG;
+        GraphDesc &d = b->hgd[i];
+        d.nroots = nroots[i];
+        d.mask = nroots[i] == 64 ? ~0ull : ((1ull << nroots[i]) - 1);
+        d.pred_base = pb;
+        pb += (uint64_t)nroots[i] * (uint64_t)d.n;
+        b->h_root_off[i] = off;
+        for (int r = 0; r < nroots[i]; ++r) {
+            const int64_t v = roots_host[off + r];
+            if (v < 0 || v >= d.n) return G5_ERR_INVALID_ARG;
+            b->h_roots[off + r] = v;
+        }
+        off += nroots[i];
+    }
+    b->h_root_off[ng] = off;
+    cudaStream_t s = b->stream;
+    b->args.pred = pred_out_dev;
+    if (!b->exec || b->bound_pred != pred_out_dev) {
+        G5_TRY(build_batch_graph(b));
+        b->bound_pred = pred_out_dev;
+    }
+    G5_CUDA(cudaMemcpyAsync(b->gd, b->hgd.data(), sizeof(GraphDesc) * ng, cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaMemcpyAsync(b->roots, b->h_roots, sizeof(int64_t) * (off ? off : 1), cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaMemcpyAsync(b->root_off, b->h_root_off, sizeof(int32_t) * (ng + 1), cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaEventRecord(b->ev0, s));
+    if (pb) G5_CUDA(cudaMemsetAsync(pred_out_dev, 0xFF, sizeof(uint32_t) * pb, s));
+    G5_CUDA(cudaGraphLaunch(b->exec, s));
+    G5_CUDA(cudaEventRecord(b->ev1, s));
+    G5_CUDA(cudaMemcpyAsync(b->h_st, b->st, sizeof(BState), cudaMemcpyDeviceToHost, s));
+    G5_CUDA(cudaStreamSynchronize(s));
+    if (device_ms) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+        *device_ms = ms;
+    }
+    if (b->h_st->err & 8u) return G5_ERR_TIMEOUT;
+    if (b->h_st->err) return G5_ERR_CAPACITY;
+    return G5_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,1035 @@
+// g5_bfs.cu -- plain (one root per search) direction-optimising BFS.
+//
+// Replaces the reference's CUDA_BFS backend (cpu_2d/cuda/cuda_bfs.cu) and
+// the b40c enactor it drives (b40c/graph/bfs/enactor_multi_gpu_2d.cuh:741-1101)
+// for a 1x1 process grid.  Per level, all on the device:
+//
+//   expand   top-down (queue, edge-balanced tiles, atomicMin parent) or
+//            bottom-up (bitmap sweep, first hit in the sorted adjacency)
+//   count    popcount + degree sum of the next-frontier bitmap per chunk
+//   scan     chunk prefix sums, Beamer direction switch, loop condition
+//   write    visited |= next, next -> front, sorted queue + edge offsets
+//   codec    optional s4-bp128 encode + decode of the sorted queue; the
+//            decoded queue feeds the next top-down level
+//
+// The level loop is one CUDA graph with a conditional while node, so a
+// search costs one graph launch and one small read-back at the end (the
+// reference copies the visited mask and the queue across PCIe every level,
+// cuda_bfs.cu:252-269,397-450,524-529).
+//
+// Parent choice: a vertex discovered at level L+1 gets the smallest adjacent
+// vertex of level L.  Top-down reaches it with a 64-bit atomicMin, bottom-up
+// with the first frontier hit of the ascending adjacency.  This is the parent
+// CPUBFS_bin's ascending first-writer sweep picks (cpu_2d/cpubfs_bin.cpp:
+// 143-180), so parents equal the reference CPU path's, not only valid ones.
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "g5_codec_dev.cuh"
+#include "g5_common.cuh"
+#include "g5_internal.h"
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kWarps = kBlock / 32;
+constexpr int kChunkWords = 2048;  // bitmap words per compaction chunk
+constexpr int kWordsPerThread = kChunkWords / kBlock;
+constexpr uint64_t kTile = 256;    // frontier edges per top-down warp tile
+constexpr int kBuSerial = 6;       // bottom-up entries scanned per lane first
+
+enum : int32_t { DIR_TD = 0, DIR_BU = 1 };
+
+struct LevelRec {
+    int32_t dir;        // direction used to expand this level's frontier
+    int32_t pad;
+    uint64_t nf;        // frontier vertices
+    uint64_t mf;        // their adjacency entries
+    uint64_t examined;  // adjacency entries read while expanding
+};
+
+struct BfsState {
+    int32_t level;      // index L of the frontier currently held
+    int32_t dir;        // direction for expanding F_L
+    uint64_t nf, mf;    // |F_L| and its adjacency entries
+    uint64_t mu;        // adjacency entries of still-unvisited vertices
+    uint64_t nvisited;
+    uint64_t examined;  // accumulator of the running expansion
+    uint32_t err;
+    int32_t want_queue; // 1 if F_L is also held as a sorted queue
+    int32_t bu_levels;
+    int32_t pad;
+    uint64_t codec_acc[2]; // encoded words, values through the codec
+};
+
+struct BfsArgs {
+    const int64_t *row_off;
+    const uint32_t *col;
+    const uint32_t *deg;
+    int64_t n;
+    int64_t nnz;
+    uint64_t nwords;
+    uint32_t nchunks;
+    uint32_t *visited;
+    uint32_t *front;
+    uint32_t *next;
+    int64_t *pred;
+    int32_t *level;       // may be null
+    uint32_t *queue;      // sorted next-frontier queue
+    const uint32_t *qsrc; // queue the top-down expansion reads (decoded if codec)
+    uint64_t *qoff;       // edge offset of each queue entry (+ sentinel)
+    int64_t *qbase;       // row_off[u] - qoff[i]
+    uint32_t *tile_start; // first queue index of each top-down tile
+    uint64_t max_tiles;
+    uint64_t *chunk_n;
+    uint64_t *chunk_m;
+    BfsState *st;
+    LevelRec *log;
+    int max_levels;
+    const int64_t *root_dev;
+    double alpha, beta;
+    int codec;
+    const uint64_t *codec_scal; // CS_* scalars of the codec work
+    cudaGraphConditionalHandle cond;
+    int use_cond;
+};
+
+__device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+// ---- init -----------------------------------------------------------------
+
+__global__ void k_init(BfsArgs a)
+{
+    __shared__ int64_t s_root, s_deg, s_base;
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        int64_t r = *a.root_dev;
+        s_ok = (r >= 0 && r < a.n);
+        s_root = s_ok ? r : 0;
+        s_base = s_ok ? a.row_off[r] : 0;
+        s_deg = s_ok ? a.row_off[r + 1] - s_base : 0;
+        BfsState *st = a.st;
+        st->level = 0;
+        st->dir = DIR_TD;
+        st->nf = s_ok ? 1 : 0;
+        st->mf = (uint64_t)s_deg;
+        st->mu = (uint64_t)(a.nnz - s_deg);
+        st->nvisited = s_ok ? 1 : 0;
+        st->examined = 0;
+        st->err = s_ok ? 0u : G5_DEVERR_CAPACITY;
+        st->want_queue = 1;
+        st->bu_levels = 0;
+        st->codec_acc[0] = st->codec_acc[1] = 0;
+        a.log[0].dir = DIR_TD;
+        a.log[0].nf = st->nf;
+        a.log[0].mf = st->mf;
+        a.log[0].examined = 0;
+        if (s_ok) {
+            const int64_t r = s_root;
+            a.pred[r] = r;
+            a.visited[r >> 5] |= 1u << (r & 31);
+            a.front[r >> 5] |= 1u << (r & 31);
+            if (a.level) a.level[r] = 0;
+            a.queue[0] = (uint32_t)r;
+            if (a.qsrc != a.queue) const_cast<uint32_t *>(a.qsrc)[0] = (uint32_t)r;
+            a.qoff[0] = 0;
+            a.qoff[1] = (uint64_t)s_deg;
+            a.qbase[0] = s_base;
+        }
+        // vertices past n in the last word count as visited
+        const int tail = (int)(a.n & 31);
+        if (tail) a.visited[a.nwords - 1] |= ~((1u << tail) - 1u);
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    const uint64_t tiles = ((uint64_t)s_deg + kTile - 1) / kTile;
+    for (uint64_t t = threadIdx.x; t < tiles; t += blockDim.x) a.tile_start[t] = 0;
+}
+
+// ---- expansion ----------------------------------------------------------------
+
+__device__ void expand_td(const BfsArgs &a, uint64_t &examined)
+{
+    __shared__ uint64_t s_q[kWarps][32];
+    const int lane = g5_lane();
+    const int wib = threadIdx.x >> 5;
+    const uint64_t gw = (uint64_t)blockIdx.x * kWarps + wib;
+    const uint64_t nw = (uint64_t)gridDim.x * kWarps;
+    const uint64_t mf = a.st->mf, nf = a.st->nf;
+    const uint64_t ntiles = (mf + kTile - 1) / kTile;
+    if (ntiles > a.max_tiles) {
+        if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(&a.st->err, G5_DEVERR_CAPACITY);
+        return;
+    }
+    for (uint64_t t = gw; t < ntiles; t += nw) {
+        const uint64_t e0 = t * kTile;
+        const uint64_t e1 = min(e0 + kTile, mf);
+        uint64_t cur = a.tile_start[t];
+        for (uint64_t gb = e0; gb < e1; gb += 32) {
+            const uint64_t idx = cur + 1 + lane;
+            s_q[wib][lane] = idx <= nf ? a.qoff[idx] : ~0ull;
+            __syncwarp();
+            const uint64_t e = gb + lane;
+            int lo = 0, hi = 32;
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (s_q[wib][mid] <= e) lo = mid + 1;
+                else hi = mid;
+            }
+            const uint64_t i = cur + lo;
+            // i(e) <= cur + 32 when every queued vertex has an edge (cur is
+            // the vertex of the previous group's last edge); lo == 32 is then
+            // exact, and the next boundary confirms it
+            bool in_range = true;
+            if (lo == 32 && e < e1) in_range = (i + 1 > nf) ? false : (a.qoff[i + 1] > e);
+            if (e < e1) {
+                if (!in_range) {
+                    // a queued vertex without edges: only a non-symmetric CSR
+                    atomicOr(&a.st->err, G5_DEVERR_CAPACITY);
+                } else {
+                    const uint32_t u = a.qsrc[i];
+                    const uint32_t v = __ldg(a.col + (a.qbase[i] + (int64_t)e));
+                    const uint32_t vw = a.visited[v >> 5];
+                    if (!((vw >> (v & 31)) & 1u)) {
+                        unsigned long long old =
+                            atomicMin((unsigned long long *)(a.pred + v), (unsigned long long)u);
+                        if (old == ~0ull) atomicOr(a.next + (v >> 5), 1u << (v & 31));
+                    }
+                }
+            }
+            cur = __shfl_sync(0xFFFFFFFFu, i, 31);
+            __syncwarp();
+        }
+        if (lane == 0) examined += e1 - e0;
+    }
+}
+
+__device__ void expand_bu(const BfsArgs &a, uint64_t &examined)
+{
+    const int lane = g5_lane();
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t *__restrict__ front = a.front;
+    const uint32_t *__restrict__ col = a.col;
+    for (uint64_t w = gw; w < a.nwords; w += nw) {
+        const uint32_t vis = a.visited[w];
+        if (vis == 0xFFFFFFFFu) continue;
+        const uint64_t v = w * 32 + lane;
+        const bool mine = !((vis >> lane) & 1u);
+        int64_t s = 0, e = 0;
+        if (mine) {
+            s = a.row_off[v];
+            e = a.row_off[v + 1];
+        }
+        bool found = false;
+        uint32_t par = 0;
+        int64_t j = s;
+        const int64_t lim = min(e, s + kBuSerial);
+        for (; j < lim; ++j) {
+            const uint32_t u = __ldg(col + j);
+            if ((__ldg(front + (u >> 5)) >> (u & 31)) & 1u) {
+                found = true;
+                par = u;
+                break;
+            }
+        }
+        uint64_t ex = mine ? (uint64_t)(j - s) + (found ? 1 : 0) : 0;
+        unsigned pend = __ballot_sync(0xFFFFFFFFu, mine && !found && j < e);
+        while (pend) {
+            const int l = __ffs(pend) - 1;
+            pend &= pend - 1;
+            int64_t jj = __shfl_sync(0xFFFFFFFFu, j, l);
+            const int64_t ee = __shfl_sync(0xFFFFFFFFu, e, l);
+            const int64_t st = jj;
+            bool got = false;
+            uint32_t gpar = 0;
+            while (jj < ee) {
+                const int64_t idx = jj + lane;
+                uint32_t u = 0;
+                bool hit = false;
+                if (idx < ee) {
+                    u = __ldg(col + idx);
+                    hit = (__ldg(front + (u >> 5)) >> (u & 31)) & 1u;
+                }
+                const unsigned m = __ballot_sync(0xFFFFFFFFu, hit);
+                if (m) {
+                    const int f = __ffs(m) - 1;
+                    gpar = __shfl_sync(0xFFFFFFFFu, u, f);
+                    got = true;
+                    jj += f + 1;
+                    break;
+                }
+                jj += 32;
+            }
+            jj = min(jj, ee);
+            if (lane == l) {
+                found = got;
+                par = gpar;
+                ex += (uint64_t)(jj - st);
+            }
+        }
+        const unsigned fm = __ballot_sync(0xFFFFFFFFu, found);
+        if (found) a.pred[v] = (int64_t)par;
+        if (lane == 0 && fm) a.next[w] = fm;
+        examined += ex;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_expand(BfsArgs a)
+{
+    uint64_t examined = 0;
+    if (a.st->err) return;
+    if (a.st->dir == DIR_TD) expand_td(a, examined);
+    else expand_bu(a, examined);
+    examined = warp_sum_u64(examined);
+    __shared__ uint64_t s_ex[kWarps];
+    if (g5_lane() == 0) s_ex[threadIdx.x >> 5] = examined;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t t = 0;
+        for (int i = 0; i < kWarps; ++i) t += s_ex[i];
+        if (t) atomicAdd((unsigned long long *)&a.st->examined, (unsigned long long)t);
+    }
+}
+
+// ---- compaction: count, scan, write ----------------------------------------------
+
+__device__ __forceinline__ void thread_words(const BfsArgs &a, uint64_t w0, uint32_t *wd)
+{
+#pragma unroll
+    for (int k = 0; k < kWordsPerThread; ++k) wd[k] = (w0 + k < a.nwords) ? a.next[w0 + k] : 0u;
+}
+
+__device__ __forceinline__ void count_words(const BfsArgs &a, uint64_t w0, const uint32_t *wd,
+                                            uint64_t &cn, uint64_t &cm)
+{
+    cn = 0;
+    cm = 0;
+#pragma unroll
+    for (int k = 0; k < kWordsPerThread; ++k) {
+        uint32_t x = wd[k];
+        cn += __popc(x);
+        while (x) {
+            const int b = __ffs(x) - 1;
+            x &= x - 1;
+            cm += __ldg(a.deg + (w0 + k) * 32 + b);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_count(BfsArgs a)
+{
+    const uint32_t c = blockIdx.x;
+    const uint64_t w0 = (uint64_t)c * kChunkWords + (uint64_t)threadIdx.x * kWordsPerThread;
+    uint32_t wd[kWordsPerThread];
+    thread_words(a, w0, wd);
+    uint64_t cn, cm;
+    count_words(a, w0, wd, cn, cm);
+    cn = warp_sum_u64(cn);
+    cm = warp_sum_u64(cm);
+    __shared__ uint64_t s_n[kWarps], s_m[kWarps];
+    if (g5_lane() == 0) {
+        s_n[threadIdx.x >> 5] = cn;
+        s_m[threadIdx.x >> 5] = cm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t tn = 0, tm = 0;
+        for (int i = 0; i < kWarps; ++i) {
+            tn += s_n[i];
+            tm += s_m[i];
+        }
+        a.chunk_n[c] = tn;
+        a.chunk_m[c] = tm;
+    }
+}
+
+// Block-wide exclusive scan of one u64 per thread (1024 threads).
+__device__ uint64_t block_excl_scan_1024(uint64_t v, uint64_t *s_warp, uint64_t &total)
+{
+    const int lane = g5_lane(), wid = threadIdx.x >> 5;
+    uint64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint64_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        uint64_t y = s_warp[lane];
+        uint64_t z = y;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint64_t t = __shfl_up_sync(0xFFFFFFFFu, z, o);
+            if (lane >= o) z += t;
+        }
+        s_warp[lane] = z - y;
+        if (lane == 31) s_warp[32] = z;
+    }
+    __syncthreads();
+    const uint64_t r = x - v + s_warp[wid];
+    total = s_warp[32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(1024) k_scan(BfsArgs a)
+{
+    __shared__ uint64_t s_w[33];
+    const uint32_t C = a.nchunks;
+    const uint32_t per = (C + 1023) / 1024;
+    const uint32_t b0 = threadIdx.x * per;
+    uint64_t ln = 0, lm = 0;
+    for (uint32_t i = 0; i < per && b0 + i < C; ++i) {
+        ln += a.chunk_n[b0 + i];
+        lm += a.chunk_m[b0 + i];
+    }
+    uint64_t tn, tm;
+    uint64_t on = block_excl_scan_1024(ln, s_w, tn);
+    uint64_t om = block_excl_scan_1024(lm, s_w, tm);
+    for (uint32_t i = 0; i < per && b0 + i < C; ++i) {
+        const uint64_t xn = a.chunk_n[b0 + i], xm = a.chunk_m[b0 + i];
+        a.chunk_n[b0 + i] = on;
+        a.chunk_m[b0 + i] = om;
+        on += xn;
+        om += xm;
+    }
+    if (threadIdx.x == 0) {
+        BfsState *st = a.st;
+        const int32_t L = st->level;
+        a.log[L].examined = st->examined;
+        const uint64_t mu_after = st->mu >= tm ? st->mu - tm : 0;
+        int32_t nd = st->dir;
+        if (st->dir == DIR_TD) {
+            if ((double)tm > (double)mu_after / a.alpha) nd = DIR_BU;
+        } else {
+            if ((double)tn < (double)a.n / a.beta && tn < st->nf) nd = DIR_TD;
+        }
+        const bool want_q = (nd == DIR_TD) || a.codec != 0;
+        st->level = L + 1;
+        st->dir = nd;
+        st->nf = tn;
+        st->mf = tm;
+        st->mu = mu_after;
+        st->nvisited += tn;
+        st->examined = 0;
+        st->want_queue = want_q ? 1 : 0;
+        if (tn && nd == DIR_BU) st->bu_levels += 1;
+        if (want_q) a.qoff[tn] = tm;
+        if (L + 1 < a.max_levels) {
+            a.log[L + 1].dir = nd;
+            a.log[L + 1].nf = tn;
+            a.log[L + 1].mf = tm;
+            a.log[L + 1].examined = 0;
+        }
+        bool cont = tn > 0 && st->err == 0;
+        if (cont && L + 2 >= a.max_levels) {
+            st->err |= G5_DEVERR_LEVELS;
+            cont = false;
+        }
+        if (a.codec_scal && a.codec_scal[g5::CS_ERR]) cont = false;
+        if (a.use_cond) cudaGraphSetConditional(a.cond, cont ? 1u : 0u);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
+{
+    const uint32_t c = blockIdx.x;
+    const uint64_t w0 = (uint64_t)c * kChunkWords + (uint64_t)threadIdx.x * kWordsPerThread;
+    uint32_t wd[kWordsPerThread];
+    thread_words(a, w0, wd);
+    const int32_t L = a.st->level;  // index of the new frontier
+    const bool want_q = a.st->want_queue != 0;
+    // bitmaps
+#pragma unroll
+    for (int k = 0; k < kWordsPerThread; ++k) {
+        const uint64_t w = w0 + k;
+        if (w < a.nwords) {
+            if (wd[k]) {
+                a.visited[w] |= wd[k];
+                a.next[w] = 0;
+            }
+            a.front[w] = wd[k];
+        }
+    }
+    if (!want_q && !a.level) return;
+    uint64_t cn, cm;
+    count_words(a, w0, wd, cn, cm);
+    // block scan of (cn, cm)
+    __shared__ uint64_t s_n[kWarps + 1], s_m[kWarps + 1];
+    const int lane = g5_lane(), wid = threadIdx.x >> 5;
+    uint64_t xn = cn, xm = cm;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint64_t yn = __shfl_up_sync(0xFFFFFFFFu, xn, o);
+        uint64_t ym = __shfl_up_sync(0xFFFFFFFFu, xm, o);
+        if (lane >= o) {
+            xn += yn;
+            xm += ym;
+        }
+    }
+    if (lane == 31) {
+        s_n[wid] = xn;
+        s_m[wid] = xm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t an = 0, am = 0;
+        for (int i = 0; i < kWarps; ++i) {
+            uint64_t tn = s_n[i], tm = s_m[i];
+            s_n[i] = an;
+            s_m[i] = am;
+            an += tn;
+            am += tm;
+        }
+    }
+    __syncthreads();
+    uint64_t pos = a.chunk_n[c] + s_n[wid] + xn - cn;
+    uint64_t mpos = a.chunk_m[c] + s_m[wid] + xm - cm;
+#pragma unroll
+    for (int k = 0; k < kWordsPerThread; ++k) {
+        uint32_t x = wd[k];
+        while (x) {
+            const int b = __ffs(x) - 1;
+            x &= x - 1;
+            const uint64_t v = (w0 + k) * 32 + b;
+            if (a.level) a.level[v] = L;
+            if (want_q) {
+                const uint64_t d = __ldg(a.deg + v);
+                a.queue[pos] = (uint32_t)v;
+                a.qoff[pos] = mpos;
+                a.qbase[pos] = a.row_off[v] - (int64_t)mpos;
+                uint64_t t = (mpos + kTile - 1) / kTile;
+                const uint64_t tend = (mpos + d + kTile - 1) / kTile;
+                for (; t < tend && t < a.max_tiles; ++t) a.tile_start[t] = (uint32_t)pos;
+                mpos += d;
+            }
+            ++pos;
+        }
+    }
+}
+
+// ---- TEPS edge count and validation -----------------------------------------------
+
+__global__ void k_teps(const int64_t *__restrict__ pred, const uint32_t *__restrict__ end_deg, int64_t n,
+                       unsigned long long *out)
+{
+    uint64_t s = 0;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+         v += (int64_t)gridDim.x * blockDim.x)
+        if (pred[v] != -1) s += end_deg[v];
+    s = warp_sum_u64(s);
+    if (g5_lane() == 0 && s) atomicAdd(out, (unsigned long long)s);
+}
+
+enum : unsigned {
+    VAL_RANGE = 1u, VAL_ROOT = 2u, VAL_SELF = 4u, VAL_CYCLE = 8u, VAL_TREE_EDGE = 16u,
+    VAL_LEVEL = 32u, VAL_COVER = 64u, VAL_MINPAR = 128u
+};
+
+__global__ void k_val_init(const int64_t *__restrict__ pred, int64_t n, int64_t root,
+                           int64_t *__restrict__ anc, int32_t *__restrict__ dist, unsigned *flags)
+{
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+         v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = pred[v];
+        if (p < -1 || p >= n) {
+            atomicOr(flags, VAL_RANGE);
+            anc[v] = -1;
+            dist[v] = -1;
+            continue;
+        }
+        if (v == root) {
+            if (p != root) atomicOr(flags, VAL_ROOT);
+            anc[v] = root;
+            dist[v] = 0;
+        } else if (p == -1) {
+            anc[v] = -1;
+            dist[v] = -1;
+        } else {
+            if (p == v) atomicOr(flags, VAL_SELF);
+            anc[v] = p;
+            dist[v] = 1;
+        }
+    }
+}
+
+// One pointer-jumping round: dist += dist[anc], anc = anc[anc].
+__global__ void k_val_jump(const int64_t *__restrict__ anc_in, const int32_t *__restrict__ dist_in,
+                           int64_t *__restrict__ anc_out, int32_t *__restrict__ dist_out, int64_t n,
+                           int64_t root, unsigned *changed)
+{
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+         v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = anc_in[v];
+        int32_t d = dist_in[v];
+        int64_t np = p;
+        if (p >= 0 && p != root) {
+            const int64_t pp = anc_in[p];
+            const int32_t pd = dist_in[p];
+            if (pp < 0 || pd < 0) {
+                np = -2;  // chain leaves the tree: pred points at an unvisited vertex
+                d = -1;
+            } else {
+                np = pp;
+                d = d + pd;
+                if (d > (int32_t)(1 << 30)) d = (int32_t)(1 << 30);
+                *changed = 1u;
+            }
+        }
+        anc_out[v] = np;
+        dist_out[v] = d;
+    }
+}
+
+__global__ void k_val_edges(const int64_t *__restrict__ row_off, const uint32_t *__restrict__ col,
+                            const int64_t *__restrict__ pred, const int64_t *__restrict__ anc,
+                            const int32_t *__restrict__ dist, int64_t n, int64_t root, unsigned *flags)
+{
+    const int lane = g5_lane();
+    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t v = gw; v < n; v += nw) {
+        const int64_t p = pred[v];
+        if (p == -1) continue;
+        if (anc[v] != root || dist[v] < 0) {
+            if (lane == 0) atomicOr(flags, VAL_CYCLE);
+            continue;
+        }
+        const int32_t d = dist[v];
+        const int64_t s = row_off[v], e = row_off[v + 1];
+        bool tree = (v == root);
+        int64_t first_prev = -1;  // smallest neighbour one level up
+        unsigned bad = 0;
+        for (int64_t j0 = s; j0 < e; j0 += 32) {
+            const int64_t j = j0 + lane;
+            bool is_par = false, is_prev = false;
+            uint32_t u = 0;
+            if (j < e) {
+                u = col[j];
+                const int64_t pu = pred[u];
+                const int32_t du = (pu == -1 || anc[u] != root) ? -1 : dist[u];
+                if (du < 0) bad |= VAL_COVER;
+                else if (du > d + 1 || du < d - 1) bad |= VAL_LEVEL;
+                is_par = ((int64_t)u == p);
+                is_prev = (du == d - 1);
+            }
+            if (__any_sync(0xFFFFFFFFu, is_par)) tree = true;
+            const unsigned pm = __ballot_sync(0xFFFFFFFFu, is_prev);
+            if (pm && first_prev < 0) first_prev = __shfl_sync(0xFFFFFFFFu, (int64_t)u, __ffs(pm) - 1);
+        }
+        if (v != root) {
+            if (!tree) bad |= VAL_TREE_EDGE;
+            if (first_prev != p) bad |= VAL_MINPAR;
+            if (dist[v] != 0 && first_prev < 0) bad |= VAL_LEVEL;
+        }
+        if (bad) atomicOr(flags, bad);
+    }
+}
+
+}  // namespace
+
+// ---- workspace --------------------------------------------------------------------
+
+struct g5_bfs {
+    g5_graph *g = nullptr;
+    g5_bfs_config cfg;
+    cudaStream_t stream = nullptr;
+    BfsArgs args;
+    uint32_t *deg = nullptr;
+    uint32_t *bitmaps = nullptr;  // visited | front | next
+    int64_t *pred = nullptr;
+    int32_t *level = nullptr;
+    uint32_t *queue = nullptr;
+    uint32_t *dqueue = nullptr;
+    uint64_t *qoff = nullptr;
+    int64_t *qbase = nullptr;
+    uint32_t *tile_start = nullptr;
+    uint64_t *chunks = nullptr;
+    BfsState *st = nullptr;
+    LevelRec *log = nullptr;
+    int64_t *root_dev = nullptr;
+    uint32_t *codec_stream = nullptr;
+    g5::CodecWork cw;
+    // host mirrors
+    int64_t *h_root = nullptr;  // pinned
+    BfsState *h_st = nullptr;   // pinned
+    LevelRec *h_log = nullptr;  // pinned
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool ran = false;
+    int64_t last_root = -1;
+};
+
+namespace {
+
+void enqueue_prologue(g5_bfs *b, cudaStream_t s)
+{
+    const BfsArgs &a = b->args;
+    cudaMemsetAsync(b->bitmaps, 0, sizeof(uint32_t) * 3 * a.nwords, s);
+    cudaMemsetAsync(b->pred, 0xFF, sizeof(int64_t) * (size_t)a.n, s);
+    if (b->level) cudaMemsetAsync(b->level, 0xFF, sizeof(int32_t) * (size_t)a.n, s);
+    k_init<<<1, kBlock, 0, s>>>(a);
+}
+
+void enqueue_level(g5_bfs *b, const BfsArgs &a, cudaStream_t s)
+{
+    k_expand<<<g5::grid_for(8), kBlock, 0, s>>>(a);
+    k_count<<<a.nchunks, kBlock, 0, s>>>(a);
+    k_scan<<<1, 1024, 0, s>>>(a);
+    k_write<<<a.nchunks, kBlock, 0, s>>>(a);
+    if (a.codec) {
+        g5::codec_encode_launch(b->cw, b->queue, &b->st->nf, b->codec_stream, a.codec,
+                                b->cfg.codec_threshold, s);
+        g5::decode_launch_acc(b->cw, b->codec_stream, b->cw.scal + g5::CS_WORDS, b->dqueue, (size_t)a.n,
+                              a.codec, b->cfg.codec_threshold, &b->st->nf, b->queue, b->st->codec_acc, s);
+    }
+}
+
+g5_status build_graph(g5_bfs *b)
+{
+    cudaStream_t s = b->stream;
+    // prologue captured as a child graph
+    cudaGraph_t pro = nullptr;
+    G5_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    enqueue_prologue(b, s);
+    G5_CUDA(cudaStreamEndCapture(s, &pro));
+    cudaGraph_t g = nullptr;
+    G5_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphNode_t pro_node;
+    G5_CUDA(cudaGraphAddChildGraphNode(&pro_node, g, nullptr, 0, pro));
+    cudaGraphDestroy(pro);
+    cudaGraphConditionalHandle h;
+    G5_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    G5_CUDA(cudaGraphAddNode(&cnode, g, &pro_node, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    BfsArgs a = b->args;
+    a.cond = h;
+    a.use_cond = 1;
+    G5_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    enqueue_level(b, a, s);
+    cudaGraph_t body_out = nullptr;
+    G5_CUDA(cudaStreamEndCapture(s, &body_out));
+    G5_CUDA(cudaGraphInstantiate(&b->exec, g, 0));
+    b->graph = g;
+    return G5_OK;
+}
+
+g5_status alloc_ws(g5_bfs *b)
+{
+    g5_graph *g = b->g;
+    const int64_t n = g->n;
+    BfsArgs &a = b->args;
+    memset(&a, 0, sizeof a);
+    a.n = n;
+    a.nnz = g->nnz;
+    a.nwords = (uint64_t)((n + 31) / 32);
+    a.nchunks = (uint32_t)((a.nwords + kChunkWords - 1) / kChunkWords);
+    a.max_tiles = (uint64_t)g->nnz / kTile + 2;
+    a.max_levels = b->cfg.max_levels;
+    G5_CUDA(cudaMalloc(&b->deg, sizeof(uint32_t) * (size_t)n));
+    G5_CUDA(cudaMalloc(&b->bitmaps, sizeof(uint32_t) * 3 * a.nwords));
+    G5_CUDA(cudaMalloc(&b->pred, sizeof(int64_t) * (size_t)n));
+    if (b->cfg.want_levels) G5_CUDA(cudaMalloc(&b->level, sizeof(int32_t) * (size_t)n));
+    G5_CUDA(cudaMalloc(&b->queue, sizeof(uint32_t) * (size_t)n + 16));
+    G5_CUDA(cudaMalloc(&b->qoff, sizeof(uint64_t) * (size_t)(n + 1)));
+    G5_CUDA(cudaMalloc(&b->qbase, sizeof(int64_t) * (size_t)n));
+    G5_CUDA(cudaMalloc(&b->tile_start, sizeof(uint32_t) * a.max_tiles));
+    G5_CUDA(cudaMalloc(&b->chunks, sizeof(uint64_t) * 2 * a.nchunks));
+    G5_CUDA(cudaMalloc(&b->st, sizeof(BfsState)));
+    G5_CUDA(cudaMalloc(&b->log, sizeof(LevelRec) * (size_t)b->cfg.max_levels));
+    G5_CUDA(cudaMalloc(&b->root_dev, sizeof(int64_t)));
+    G5_CUDA(cudaMallocHost(&b->h_root, sizeof(int64_t)));
+    G5_CUDA(cudaMallocHost(&b->h_st, sizeof(BfsState)));
+    G5_CUDA(cudaMallocHost(&b->h_log, sizeof(LevelRec) * (size_t)b->cfg.max_levels));
+    if (b->cfg.codec) {
+        G5_CUDA(cudaMalloc(&b->dqueue, sizeof(uint32_t) * (size_t)n + 16));
+        G5_CUDA(cudaMalloc(&b->codec_stream, sizeof(uint32_t) * g5::codec_bound((size_t)n)));
+        G5_TRY(g5::codec_work_alloc(b->cw, (size_t)n));
+    }
+    a.row_off = g->row_off;
+    a.col = g->col;
+    a.deg = b->deg;
+    a.visited = b->bitmaps;
+    a.front = b->bitmaps + a.nwords;
+    a.next = b->bitmaps + 2 * a.nwords;
+    a.pred = b->pred;
+    a.level = b->level;
+    a.queue = b->queue;
+    a.qsrc = b->cfg.codec ? b->dqueue : b->queue;
+    a.qoff = b->qoff;
+    a.qbase = b->qbase;
+    a.tile_start = b->tile_start;
+    a.chunk_n = b->chunks;
+    a.chunk_m = b->chunks + a.nchunks;
+    a.st = b->st;
+    a.log = b->log;
+    a.root_dev = b->root_dev;
+    a.alpha = b->cfg.alpha;
+    a.beta = b->cfg.beta;
+    a.codec = b->cfg.codec;
+    a.codec_scal = b->cfg.codec ? b->cw.scal : nullptr;
+    a.use_cond = 0;
+    return G5_OK;
+}
+
+__global__ void k_degrees(const int64_t *__restrict__ ro, int64_t n, uint32_t *__restrict__ d)
+{
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+         v += (int64_t)gridDim.x * blockDim.x)
+        d[v] = (uint32_t)(ro[v + 1] - ro[v]);
+}
+
+void free_ws(g5_bfs *b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    cudaFree(b->deg);
+    cudaFree(b->bitmaps);
+    cudaFree(b->pred);
+    cudaFree(b->level);
+    cudaFree(b->queue);
+    cudaFree(b->dqueue);
+    cudaFree(b->qoff);
+    cudaFree(b->qbase);
+    cudaFree(b->tile_start);
+    cudaFree(b->chunks);
+    cudaFree(b->st);
+    cudaFree(b->log);
+    cudaFree(b->root_dev);
+    cudaFree(b->codec_stream);
+    cudaFreeHost(b->h_root);
+    cudaFreeHost(b->h_st);
+    cudaFreeHost(b->h_log);
+    if (b->cfg.codec) g5::codec_work_free(b->cw);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+// Algorithmic HBM bytes of one search from the level log (per level:
+// top-down 4|F| + 16|F| + 4 E_td + N/8 + 4|F'| + 9|F'|; bottom-up
+// 8(N+1) + 4 E_bu + 3N/8 + 9|F'|).
+int64_t alg_bytes(const LevelRec *log, int nlev, int64_t n)
+{
+    double B = 0;
+    for (int L = 0; L < nlev; ++L) {
+        const double nf = (double)log[L].nf;
+        const double nf1 = (L + 1 < nlev) ? (double)log[L + 1].nf : 0.0;
+        if (log[L].dir == DIR_TD)
+            B += 20.0 * nf + 4.0 * (double)log[L].examined + (double)n / 8.0 + 13.0 * nf1;
+        else
+            B += 8.0 * (double)(n + 1) + 4.0 * (double)log[L].examined + 3.0 * (double)n / 8.0 + 9.0 * nf1;
+    }
+    return (int64_t)B;
+}
+
+}  // namespace
+
+extern "C" {
+
+void g5_bfs_config_default(g5_bfs_config *cfg)
+{
+    if (!cfg) return;
+    cfg->alpha = 14.0;
+    cfg->beta = 24.0;
+    cfg->codec = G5_CODEC_NONE;
+    cfg->codec_threshold = 64;
+    cfg->use_graph = 1;
+    cfg->max_levels = 4096;
+    cfg->want_levels = 0;
+}
+
+g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
+{
+    if (!g || !out) return G5_ERR_INVALID_ARG;
+    *out = nullptr;
+    g5_bfs *b = new g5_bfs();
+    b->g = g;
+    if (cfg) b->cfg = *cfg;
+    else g5_bfs_config_default(&b->cfg);
+    if (b->cfg.max_levels < 2) b->cfg.max_levels = 2;
+    if (b->cfg.codec < 0 || b->cfg.codec > 2 || b->cfg.alpha <= 0 || b->cfg.beta <= 0) {
+        delete b;
+        return G5_ERR_INVALID_ARG;
+    }
+    g5_status st = G5_OK;
+    auto fail = [&](g5_status s) {
+        free_ws(b);
+        delete b;
+        return s;
+    };
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(G5_ERR_CUDA);
+    cudaEventCreate(&b->ev0);
+    cudaEventCreate(&b->ev1);
+    if ((st = alloc_ws(b)) != G5_OK) return fail(st);
+    k_degrees<<<g5::grid_for(8), kBlock, 0, b->stream>>>(g->row_off, g->n, b->deg);
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
+    if (b->cfg.use_graph && (st = build_graph(b)) != G5_OK) return fail(st);
+    *out = b;
+    return G5_OK;
+}
+
+g5_status g5_bfs_destroy(g5_bfs *b)
+{
+    if (!b) return G5_ERR_INVALID_ARG;
+    cudaStreamSynchronize(b->stream);
+    free_ws(b);
+    delete b;
+    return G5_OK;
+}
+
+g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_out, g5_bfs_stats *stats)
+{
+    if (!b || root < 0 || root >= b->g->n) return G5_ERR_INVALID_ARG;
+    if (level_out && !b->level) return G5_ERR_INVALID_ARG;
+    cudaStream_t s = b->stream;
+    *b->h_root = root;
+    G5_CUDA(cudaMemcpyAsync(b->root_dev, b->h_root, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaEventRecord(b->ev0, s));
+    if (b->exec) {
+        G5_CUDA(cudaGraphLaunch(b->exec, s));
+    } else {
+        enqueue_prologue(b, s);
+        for (int L = 0; L < b->cfg.max_levels; ++L) {
+            enqueue_level(b, b->args, s);
+            G5_CUDA(cudaMemcpyAsync(b->h_st, b->st, sizeof(BfsState), cudaMemcpyDeviceToHost, s));
+            G5_CUDA(cudaStreamSynchronize(s));
+            if (b->h_st->nf == 0 || b->h_st->err) break;
+            if (b->h_st->level + 2 >= b->cfg.max_levels) break;
+        }
+    }
+    G5_CUDA(cudaEventRecord(b->ev1, s));
+    G5_CUDA(cudaMemcpyAsync(b->h_st, b->st, sizeof(BfsState), cudaMemcpyDeviceToHost, s));
+    if (pred_out)
+        G5_CUDA(cudaMemcpyAsync(pred_out, b->pred, sizeof(int64_t) * (size_t)b->g->n, cudaMemcpyDefault, s));
+    if (level_out)
+        G5_CUDA(cudaMemcpyAsync(level_out, b->level, sizeof(int32_t) * (size_t)b->g->n, cudaMemcpyDefault, s));
+    uint64_t cscal[g5::CS_COUNT] = {0};
+    if (b->cfg.codec)
+        G5_CUDA(cudaMemcpyAsync(cscal, b->cw.scal, sizeof cscal, cudaMemcpyDeviceToHost, s));
+    G5_CUDA(cudaStreamSynchronize(s));
+    b->ran = true;
+    b->last_root = root;
+    const BfsState &hs = *b->h_st;
+    if (hs.err & G5_DEVERR_LEVELS) return G5_ERR_TIMEOUT;
+    if (hs.err) return G5_ERR_CAPACITY;
+    if (b->cfg.codec && (cscal[g5::CS_ERR] & G5_DEVERR_MISMATCH)) return G5_ERR_MISMATCH;
+    if (b->cfg.codec && cscal[g5::CS_ERR]) return G5_ERR_CORRUPT_STREAM;
+    if (stats) {
+        const int nlev = hs.level + 1;
+        G5_CUDA(cudaMemcpy(b->h_log, b->log, sizeof(LevelRec) * (size_t)nlev, cudaMemcpyDeviceToHost));
+        memset(stats, 0, sizeof *stats);
+        stats->levels = nlev;
+        stats->visited = (int64_t)hs.nvisited;
+        for (int L = 0; L < nlev; ++L) {
+            const LevelRec &r = b->h_log[L];
+            if (r.dir == DIR_TD) stats->edges_td += (int64_t)r.examined;
+            else {
+                stats->edges_bu += (int64_t)r.examined;
+                stats->bottom_up_levels += 1;
+            }
+            stats->queue_total += (int64_t)r.nf;
+        }
+        stats->codec_words = (int64_t)hs.codec_acc[0];
+        stats->codec_values = (int64_t)hs.codec_acc[1];
+        stats->alg_bytes = alg_bytes(b->h_log, nlev, b->g->n);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+        stats->device_ms = ms;
+    }
+    return G5_OK;
+}
+
+g5_status g5_bfs_device_pred(g5_bfs *b, const int64_t **pred)
+{
+    if (!b || !pred) return G5_ERR_INVALID_ARG;
+    *pred = b->pred;
+    return G5_OK;
+}
+
+g5_status g5_bfs_teps_edges(g5_bfs *b, int64_t *nedge)
+{
+    if (!b || !nedge || !b->ran || !b->g->end_deg) return G5_ERR_INVALID_ARG;
+    unsigned long long *d = nullptr;
+    G5_CUDA(cudaMalloc(&d, sizeof *d));
+    cudaMemsetAsync(d, 0, sizeof *d, b->stream);
+    k_teps<<<g5::grid_for(8), kBlock, 0, b->stream>>>(b->pred, b->g->end_deg, b->g->n, d);
+    unsigned long long h = 0;
+    cudaMemcpyAsync(&h, d, sizeof h, cudaMemcpyDeviceToHost, b->stream);
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    cudaFree(d);
+    G5_CUDA(e);
+    *nedge = (int64_t)(h / 2);
+    return G5_OK;
+}
+
+g5_status g5_bfs_validate(g5_bfs *b, int64_t root, int *valid, int *min_parent_out)
+{
+    if (!b || !valid || root < 0 || root >= b->g->n || !b->ran) return G5_ERR_INVALID_ARG;
+    const int64_t n = b->g->n;
+    cudaStream_t s = b->stream;
+    int64_t *anc[2] = {nullptr, nullptr};
+    int32_t *dist[2] = {nullptr, nullptr};
+    unsigned *flags = nullptr;
+    g5_status rc = G5_OK;
+    auto cleanup = [&]() {
+        cudaFree(anc[0]);
+        cudaFree(anc[1]);
+        cudaFree(dist[0]);
+        cudaFree(dist[1]);
+        cudaFree(flags);
+    };
+    if (cudaMalloc(&anc[0], sizeof(int64_t) * n) != cudaSuccess ||
+        cudaMalloc(&anc[1], sizeof(int64_t) * n) != cudaSuccess ||
+        cudaMalloc(&dist[0], sizeof(int32_t) * n) != cudaSuccess ||
+        cudaMalloc(&dist[1], sizeof(int32_t) * n) != cudaSuccess ||
+        cudaMalloc(&flags, sizeof(unsigned) * 2) != cudaSuccess) {
+        cleanup();
+        return G5_ERR_OOM;
+    }
+    cudaMemsetAsync(flags, 0, sizeof(unsigned) * 2, s);
+    k_val_init<<<g5::grid_for(8), kBlock, 0, s>>>(b->pred, n, root, anc[0], dist[0], flags);
+    int cur = 0;
+    for (int r = 0; r < 64; ++r) {
+        cudaMemsetAsync(flags + 1, 0, sizeof(unsigned), s);
+        k_val_jump<<<g5::grid_for(8), kBlock, 0, s>>>(anc[cur], dist[cur], anc[1 - cur], dist[1 - cur], n, root,
+                                                       flags + 1);
+        cur = 1 - cur;
+        unsigned ch = 0;
+        cudaMemcpyAsync(&ch, flags + 1, sizeof ch, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) {
+            rc = G5_ERR_CUDA;
+            break;
+        }
+        if (!ch) break;
+    }
+    if (rc == G5_OK) {
+        k_val_edges<<<g5::grid_for(8), kBlock, 0, s>>>(b->g->row_off, b->g->col, b->pred, anc[cur], dist[cur], n,
+                                                        root, flags);
+        unsigned f = 0;
+        cudaMemcpyAsync(&f, flags, sizeof f, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) rc = G5_ERR_CUDA;
+        *valid = (f & ~VAL_MINPAR) == 0;
+        if (min_parent_out) *min_parent_out = (f & VAL_MINPAR) == 0;
+    }
+    cleanup();
+    return rc;
+}
+
+}  // extern "C"

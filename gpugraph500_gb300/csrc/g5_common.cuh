@@ -1,0 +1,66 @@
+// g5_common.cuh -- shared definitions of the libg5bfs CUDA sources.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+
+#include "g5bfs.h"
+
+#define G5_NUM_SMS_DEFAULT 152
+
+namespace g5 {
+
+// Maps a CUDA error to a status code (allocation failures are OOM).
+inline g5_status cuda_status(cudaError_t e)
+{
+    if (e == cudaSuccess) return G5_OK;
+    if (e == cudaErrorMemoryAllocation) return G5_ERR_OOM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return G5_ERR_NO_DEVICE;
+    return G5_ERR_CUDA;
+}
+
+// Returns from the enclosing function with a status if a CUDA call fails.
+#define G5_CUDA(call)                                                            \
+    do {                                                                         \
+        cudaError_t g5_e_ = (call);                                              \
+        if (g5_e_ != cudaSuccess) {                                              \
+            if (getenv("G5_VERBOSE"))                                            \
+                fprintf(stderr, "g5: %s failed at %s:%d: %s\n", #call, __FILE__, \
+                        __LINE__, cudaGetErrorString(g5_e_));                    \
+            return ::g5::cuda_status(g5_e_);                                     \
+        }                                                                        \
+    } while (0)
+
+#define G5_TRY(call)                       \
+    do {                                   \
+        g5_status g5_s_ = (call);          \
+        if (g5_s_ != G5_OK) return g5_s_;  \
+    } while (0)
+
+// Number of SMs of the current device (cached per process).
+int num_sms();
+
+// True if p is a device or managed pointer.
+bool is_device_ptr(const void *p);
+
+// Grid of `per_sm` blocks per SM.
+inline int grid_for(int per_sm) { return num_sms() * per_sm; }
+
+}  // namespace g5
+
+// Device-side error flags (bit set in a status word).
+enum : uint32_t {
+    G5_DEVERR_CAPACITY = 1u,
+    G5_DEVERR_CORRUPT = 2u,
+    G5_DEVERR_MISMATCH = 4u,
+    G5_DEVERR_LEVELS = 8u,
+};
+
+__device__ __forceinline__ int g5_lane() { return threadIdx.x & 31; }
+__device__ __forceinline__ unsigned g5_lanemask_lt()
+{
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}

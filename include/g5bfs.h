@@ -1,0 +1,251 @@
+/*
+ * g5bfs.h -- C ABI of the GB300-native gpugraph500 BFS hot path.
+ *
+ * One library, libg5bfs.so, with hand-written sm_103a kernels behind plain
+ * C entry points: no C++ or torch types cross this boundary, only pointers,
+ * sizes and status codes.  Each entry point names the reference interface it
+ * replaces (paths relative to the gpugraph500 project root).
+ *
+ * Pointers documented as "device" must be CUDA device (or managed) memory.
+ * Pointers documented as "host or device" are classified with
+ * cudaPointerGetAttributes; host memory is copied inside the call.
+ * Nothing here aborts the process: every failure is a g5_status.
+ */
+#ifndef G5BFS_H
+#define G5BFS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The reference reports CUDA failures with B40CPerror + MPI_Abort
+ * (cpu_2d/cuda/cuda_bfs.cu:567-574,605-611,652-658) and codec misuse with
+ * assert (cpu_2d/compression/cpusimd.hh:49-57,84-90); these codes replace
+ * both. */
+typedef enum g5_status {
+    G5_OK = 0,
+    G5_ERR_OOM = 1,            /* device or pinned allocation failed       */
+    G5_ERR_CAPACITY = 2,       /* a buffer or limit is too small           */
+    G5_ERR_INVALID_ARG = 3,    /* bad pointer, size, root or mode          */
+    G5_ERR_TIMEOUT = 4,        /* a bounded device wait or level cap ran out */
+    G5_ERR_CORRUPT_STREAM = 5, /* codec stream fails validation            */
+    G5_ERR_CUDA = 6,           /* any other CUDA runtime error             */
+    G5_ERR_NO_DEVICE = 7,      /* no CUDA device visible                   */
+    G5_ERR_MISMATCH = 8        /* an in-loop round-trip check failed       */
+} g5_status;
+
+/* Human-readable name of a status code (static storage). */
+const char *g5_status_str(g5_status s);
+
+/* Library/ABI version, 0xMMmmpp. */
+uint32_t g5_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Graphs: a symmetric CSR resident in HBM                                   */
+/* ------------------------------------------------------------------------ */
+
+typedef struct g5_graph g5_graph;
+
+/* Uploads a host CSR (int64 row offsets, n+1 entries; uint32 sorted column
+ * ids, nnz entries) to the current device.  Replaces
+ * CsrProblem::FromHostProblem (b40c/graph/bfs/csr_problem_2d.cuh:314-394),
+ * which the reference calls from CUDA_BFS's constructor
+ * (cpu_2d/cuda/cuda_bfs.cu:15-60).  Column ids must be < n and each row
+ * sorted ascending without duplicates (the shape setupMatrix2 builds,
+ * cpu_2d/distmatrix2d.hh:1033-1164); rows that are not sorted still give
+ * valid BFS trees, but not the reference's parent choice. */
+g5_status g5_graph_create(const int64_t *row_off, const uint32_t *col, int64_t n,
+                          int64_t nnz, g5_graph **out);
+
+/* Generates the Graph500 Kronecker graph of the given scale on the GPU and
+ * builds its symmetric CSR there (self loops and duplicates dropped), the
+ * work of make_graph (cpu_2d/main.cpp:221, cpu_2d/generator/make_graph.c:34-69)
+ * plus DistMatrix2d::setupMatrix2 (cpu_2d/distmatrix2d.hh:745-1166) at 1x1.
+ * n = 2^scale.  Also keeps, per vertex, the number of generated edge
+ * endpoints (duplicates and self loops included) so that the Graph500 TEPS
+ * edge count of a search (cpu_2d/validate/validate.h:440-443,485) can be
+ * computed on the device. */
+g5_status g5_graph_generate_kronecker(int scale, int edgefactor, uint64_t seed1,
+                                      uint64_t seed2, g5_graph **out);
+
+/* Copies the raw generated edge list [start, end) (int64 pairs) of a
+ * Kronecker graph to host memory, generating it again on the device in
+ * slices (cpu_2d/generator/graph_generator.c:157-187). */
+g5_status g5_kronecker_edges(int scale, uint64_t seed1, uint64_t seed2,
+                             int64_t start, int64_t end, int64_t *edges_host);
+
+g5_status g5_graph_info(const g5_graph *g, int64_t *n, int64_t *nnz);
+
+/* Copies the CSR back (either pointer may be NULL). */
+g5_status g5_graph_copy_csr(const g5_graph *g, int64_t *row_off_host, uint32_t *col_host);
+
+/* Device pointers of the resident CSR (for callers that run their own
+ * kernels on it).  Valid until g5_graph_destroy. */
+g5_status g5_graph_device_csr(const g5_graph *g, const int64_t **row_off,
+                              const uint32_t **col);
+
+g5_status g5_graph_destroy(g5_graph *g);
+
+/* Root selection of the reference driver (cpu_2d/main.cpp:351-392):
+ * default-seeded std::knuth_b, uniform_int_distribution<int64_t>(0, n-1),
+ * skipping repeats and CSR-degree-0 vertices, at most nroots*maxgen draws
+ * (the driver uses maxgen = 32). *found = roots written. */
+g5_status g5_select_roots(const g5_graph *g, int nroots, int64_t maxgen,
+                          int64_t *roots_host, int *found);
+
+/* ------------------------------------------------------------------------ */
+/* Plain BFS: one root per search (the drop-in for CUDA_BFS)                 */
+/* ------------------------------------------------------------------------ */
+
+typedef struct g5_bfs g5_bfs;
+
+enum {
+    G5_CODEC_NONE = 0, /* no codec pass                                        */
+    G5_CODEC_D4 = 1,   /* s4-bp128-d4: CompositeCodec<SIMDBinaryPacking<
+                          SIMDIntegratedBlockPacker<CoarseDelta4SIMD>>,
+                          VariableByte<true>> (codecfactory.h:103-105)        */
+    G5_CODEC_DM = 2    /* s4-bp128-dm: same with Max4DeltaSIMD (:106-108); the
+                          stream the reference's CpuSimd plugin actually emits,
+                          see g5_plugin_compress                             */
+};
+
+typedef struct g5_bfs_config {
+    double alpha;        /* top-down -> bottom-up when m_f > m_u / alpha (Beamer) */
+    double beta;         /* bottom-up -> top-down when n_f < n / beta           */
+    int codec;           /* G5_CODEC_*: round-trip every level's sorted queue   */
+    uint32_t codec_threshold; /* raw below or at this length (cpusimd.hh:27,44) */
+    int use_graph;       /* 1: level loop as one CUDA graph (conditional while
+                            node); 0: host-driven loop, one sync per level       */
+    int max_levels;      /* safety cap on levels (G5_ERR_TIMEOUT past it)       */
+    int want_levels;     /* keep a per-vertex level array                        */
+} g5_bfs_config;
+
+/* Fills the defaults: alpha 14, beta 24, no codec, threshold 64, CUDA graph,
+ * 4096 levels, no level array. */
+void g5_bfs_config_default(g5_bfs_config *cfg);
+
+/* Per-search workspace on one graph; not thread safe (one per host thread),
+ * like a CUDA_BFS instance (cpu_2d/cuda/cuda_bfs.h:39-84). */
+g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out);
+g5_status g5_bfs_destroy(g5_bfs *b);
+
+typedef struct g5_bfs_stats {
+    int32_t levels;           /* BFS depth + 1 (levels run)                      */
+    int32_t bottom_up_levels; /* levels expanded bottom-up                        */
+    int64_t visited;          /* vertices reached                                 */
+    int64_t edges_td;         /* adjacency entries read top-down                  */
+    int64_t edges_bu;         /* adjacency entries examined bottom-up             */
+    int64_t queue_total;      /* sum of frontier queue lengths                    */
+    int64_t codec_words;      /* sum of encoded words over levels                 */
+    int64_t codec_values;     /* sum of values that went through the codec        */
+    int64_t alg_bytes;        /* algorithmic HBM bytes of the search              */
+    double device_ms;         /* device time of the search (CUDA events)          */
+} g5_bfs_stats;
+
+/* One BFS from root: GlobalBFS::runBFS (cpu_2d/globalbfs.hh:548-1263) at 1x1
+ * with CUDA_BFS's hooks (cpu_2d/cuda/cuda_bfs.cu:230-659) followed by
+ * getBackPredecessor/getPredecessor (cuda_bfs.cu:328-378).  pred_out (host or
+ * device, n entries, may be NULL) receives the parent array in the
+ * reference's convention: -1 unvisited, root -> root, otherwise the smallest
+ * vertex of the previous level adjacent to the vertex (the parent
+ * CPUBFS_bin's ascending first-writer sweep picks, cpu_2d/cpubfs_bin.cpp:
+ * 143-180).  level_out (host or device, may be NULL; needs want_levels)
+ * receives levels, -1 unvisited.  stats may be NULL. */
+g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_out,
+                     g5_bfs_stats *stats);
+
+/* Device pointer to the workspace's int64 parent array of the last search. */
+g5_status g5_bfs_device_pred(g5_bfs *b, const int64_t **pred);
+
+/* Graph500 TEPS edge count of the last search, computed on the device: the
+ * number of generated input edges (self loops and duplicates included) with a
+ * visited endpoint (validate.h:440-443,485).  Needs a generated graph. */
+g5_status g5_bfs_teps_edges(g5_bfs *b, int64_t *nedge);
+
+/* Graph500 validation of the last search on the device: parent range, root
+ * is its own parent, no other self parent, every tree edge exists in the CSR,
+ * level(parent) = level(child) - 1, every edge spans at most one level, and
+ * every vertex adjacent to a visited vertex is visited (validate.h:248-491).
+ * *valid = 1 if all hold.  If min_parent_out is not NULL it is set to 1 when
+ * each parent is also the smallest previous-level neighbour (the reference
+ * CPU BFS's choice). */
+g5_status g5_bfs_validate(g5_bfs *b, int64_t root, int *valid, int *min_parent_out);
+
+/* ------------------------------------------------------------------------ */
+/* Batched BFS: up to 64 roots per graph with bit-sliced frontier words      */
+/* ------------------------------------------------------------------------ */
+
+typedef struct g5_batch g5_batch;
+
+/* Workspace for batched searches over a set of graphs (one per slot). */
+g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out);
+g5_status g5_batch_destroy(g5_batch *bt);
+
+/* Runs nroots[i] (<= 64) roots on graph i, all graphs in one level loop.
+ * roots holds the roots of graph 0, then graph 1, ...  Parents are written
+ * as uint32 (0xFFFFFFFF unvisited, root -> root) to pred_out (device) in
+ * root-major order: graph 0 root 0 (n0 entries), root 1, ... then graph 1.
+ * Same parent choice as g5_bfs_run. */
+g5_status g5_batch_run(g5_batch *bt, const int64_t *roots_host, const int *nroots,
+                       uint32_t *pred_out_dev, double *device_ms);
+
+/* ------------------------------------------------------------------------ */
+/* s4-bp128 frontier codec on the device                                     */
+/* ------------------------------------------------------------------------ */
+
+typedef struct g5_codec g5_codec;
+
+/* Upper bound on encoded words for n values. */
+size_t g5_codec_bound(size_t n);
+
+/* Workspace for values up to max_n per call. */
+g5_status g5_codec_create(size_t max_n, g5_codec **out);
+g5_status g5_codec_destroy(g5_codec *c);
+
+/* IntegerCODEC::encodeArray of the named composite codec
+ * (compression/cpusimd/include/compositecodec.h:31-51) on device buffers:
+ * in_dev n uint32 values, out_dev >= g5_codec_bound(n) words (16-byte
+ * aligned).  *out_words (host) = words written.  mode = G5_CODEC_D4 or
+ * G5_CODEC_DM.  stream may be NULL (default stream). */
+g5_status g5_codec_encode(g5_codec *c, const uint32_t *in_dev, size_t n, uint32_t *out_dev,
+                          size_t *out_words, int mode, void *stream);
+
+/* IntegerCODEC::decodeArray (compositecodec.h:52-71): decodes a stream of
+ * `words` words into out_dev (capacity out_cap values); *out_n = values.
+ * Streams that fail validation give G5_ERR_CORRUPT_STREAM. */
+g5_status g5_codec_decode(g5_codec *c, const uint32_t *in_dev, size_t words, uint32_t *out_dev,
+                          size_t out_cap, size_t *out_n, int mode, void *stream);
+
+/* The CpuSimd plugin (cpu_2d/compression/cpusimd.hh:70-118): int64 host
+ * queue -> *compressed (malloc'd by this call, caller frees, as the reference
+ * caller does at cpu_2d/globalbfs.hh:903), raw uint32 when size <= threshold.
+ * mode selects the stream; the reference plugin, whatever name it is given,
+ * encodes with s4-bp128-dm because its codec member is a reference bound at
+ * construction (cpusimd.hh:26,52-53), so G5_CODEC_DM matches it byte for byte. */
+g5_status g5_plugin_compress(const int64_t *fq_host, size_t size, uint32_t **compressed,
+                             size_t *compressedsize, uint32_t threshold, int mode);
+
+/* cpusimd.hh:120-157: *uncompressedsize is the original length in and the
+ * decoded length out; *uncompressed is malloc'd (int64). */
+g5_status g5_plugin_decompress(const uint32_t *compressed_host, size_t compressedsize,
+                               int64_t **uncompressed, size_t *uncompressedsize,
+                               uint32_t threshold, int mode);
+
+/* ------------------------------------------------------------------------ */
+/* Frontier-bitmap OR                                                        */
+/* ------------------------------------------------------------------------ */
+
+/* dst[i] |= srcs[0][i] | ... | srcs[k-1][i] over `words` uint64 words, all
+ * device pointers (srcs itself is a host array of k <= 64 device pointers):
+ * the reduce callback of vreduce (cpu_2d/vreduce.hpp:112,257-259,359-361)
+ * bound to CPUBFS_bin::reduce_fq_out (cpu_2d/cpubfs_bin.cpp:55-65). */
+g5_status g5_bitmap_or(uint64_t *dst, const uint64_t *const *srcs, int k, size_t words,
+                       void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,148 @@
+"""Plain BFS on the GPU against the oracle (parents bit-exact, levels exact)."""
+import numpy as np
+import pytest
+
+import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+g5 = pytest.importorskip("gpugraph500_gb300")
+
+
+def csr_from_edges(n, edges):
+    return orc.build_csr(n, np.asarray(edges, np.int64).reshape(-1, 2))
+
+
+def run_all_roots(ro, col, roots, **kw):
+    g = g5.Graph.from_csr(ro, col)
+    for use_graph in (True, False):
+        b = g5.CudaBFS(g, want_levels=True, use_graph=use_graph, **kw)
+        for r in roots:
+            b.runBFS(int(r))
+            want_pred, want_level = orc.bfs(ro, col, int(r))
+            assert np.array_equal(b.getPredecessor(), want_pred), (r, use_graph)
+            assert np.array_equal(b.getLevels(), want_level), (r, use_graph)
+            valid, minpar = b.validate()
+            assert valid and minpar
+        b.close()
+    g.close()
+
+
+def test_hand_graphs():
+    # path 0-1-2-...-9, star around 10, two components, self loops, duplicates
+    edges = [(i, i + 1) for i in range(9)]
+    edges += [(10, 11 + i) for i in range(12)]
+    edges += [(30, 31), (31, 32), (32, 30), (33, 33), (30, 31), (31, 30)]
+    edges += [(40, 41), (40, 41), (41, 41)]
+    n = 64
+    ro, col = csr_from_edges(n, edges)
+    run_all_roots(ro, col, [0, 5, 9, 10, 11, 30, 33, 40])
+
+
+def test_long_path_many_levels():
+    n = 3000
+    edges = [(i, i + 1) for i in range(n - 1)]
+    ro, col = csr_from_edges(n, edges)
+    run_all_roots(ro, col, [0, 1500])
+
+
+def test_odd_sizes():
+    rng = np.random.default_rng(3)
+    for n in (33, 95, 1000, 4097):
+        e = rng.integers(0, n, size=(4 * n, 2))
+        ro, col = csr_from_edges(n, e)
+        run_all_roots(ro, col, [0, n - 1, n // 2])
+
+
+@pytest.mark.parametrize("scale", [8, 11, 14])
+def test_kronecker_parents_match_oracle(scale):
+    e = orc.kronecker(scale)
+    ro, col = orc.build_csr(1 << scale, e)
+    roots = orc.select_roots(ro, 16)
+    run_all_roots(ro, col, roots)
+
+
+def test_direction_extremes():
+    """Pure top-down (alpha huge) and early bottom-up (alpha tiny) agree."""
+    e = orc.kronecker(12)
+    ro, col = orc.build_csr(1 << 12, e)
+    roots = orc.select_roots(ro, 4)
+    for alpha, beta in ((1e12, 1e12), (1e-6, 1e-6), (1.0, 2.0)):
+        run_all_roots(ro, col, roots, alpha=alpha, beta=beta)
+
+
+def test_gpu_generator_and_csr_match_oracle():
+    for scale in (6, 10, 13):
+        g = g5.Graph.kronecker(scale)
+        e = orc.kronecker(scale)
+        assert np.array_equal(g5.kronecker_edges(scale), e)
+        ro, col = orc.build_csr(1 << scale, e)
+        gro, gcol = g.csr()
+        assert np.array_equal(gro, ro) and np.array_equal(gcol, col)
+        assert np.array_equal(g5.select_roots(g, 64), orc.select_roots(ro, 64))
+        g.close()
+
+
+def test_generator_slices():
+    e = orc.kronecker(12, start=1000, end=5000)
+    assert np.array_equal(g5.kronecker_edges(12, start=1000, end=5000), e)
+
+
+def test_teps_edges_and_validation_match_oracle():
+    scale = 12
+    g = g5.Graph.kronecker(scale)
+    e = orc.kronecker(scale)
+    ro, col = orc.build_csr(1 << scale, e)
+    b = g5.CudaBFS(g)
+    for r in orc.select_roots(ro, 8):
+        b.runBFS(int(r))
+        ok, ne, _ = orc.validate(1 << scale, e, int(r), b.getPredecessor())
+        assert ok
+        assert b.teps_edges() == ne
+        assert b.validate() == (True, True)
+    b.close()
+    g.close()
+
+
+def test_codec_in_loop_round_trips():
+    e = orc.kronecker(13)
+    ro, col = orc.build_csr(1 << 13, e)
+    roots = orc.select_roots(ro, 6)
+    for codec in (g5.CODEC_D4, g5.CODEC_DM):
+        run_all_roots(ro, col, roots, codec=codec)
+    g = g5.Graph.from_csr(ro, col)
+    b = g5.CudaBFS(g, codec=g5.CODEC_D4)
+    b.runBFS(int(roots[0]))
+    s = b.stats
+    assert s.codec_values == s.queue_total - 1  # every level's queue except the root
+    assert 0 < s.codec_words < s.codec_values
+
+
+def test_invalid_root_and_config():
+    ro, col = csr_from_edges(8, [(0, 1)])
+    g = g5.Graph.from_csr(ro, col)
+    b = g5.CudaBFS(g)
+    assert b.run(-1) == g5.G5_ERR_INVALID_ARG
+    assert b.run(8) == g5.G5_ERR_INVALID_ARG
+    with pytest.raises(g5.G5Error):
+        g5.CudaBFS(g, codec=7)
+    b.runBFS(5)  # isolated root: only itself
+    p = b.getPredecessor()
+    assert p[5] == 5 and (np.delete(p, 5) == -1).all()
+
+
+def test_level_cap_reports_timeout():
+    n = 200
+    ro, col = csr_from_edges(n, [(i, i + 1) for i in range(n - 1)])
+    g = g5.Graph.from_csr(ro, col)
+    for use_graph in (True, False):
+        b = g5.CudaBFS(g, max_levels=50, use_graph=use_graph)
+        assert b.run(0) == g5.G5_ERR_TIMEOUT
+        b.close()
+
+
+def test_bad_csr_rejected():
+    ro = np.array([0, 1, 2], np.int64)
+    col = np.array([1, 5], np.uint32)  # id out of range
+    with pytest.raises(g5.G5Error):
+        g5.Graph.from_csr(ro, col)
