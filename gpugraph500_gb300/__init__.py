@@ -91,6 +91,7 @@ SIGNATURES = {
     "g5_codec_destroy": (_I, [_P]),
     "g5_codec_encode": (_I, [_P, _P, _SZ, _P, C.POINTER(_SZ), _I, _P]),
     "g5_codec_decode": (_I, [_P, _P, _SZ, _P, _SZ, C.POINTER(_SZ), _I, _P]),
+    "g5_codec_encode_noalloc": (_I, [_P, _SZ, _P, C.POINTER(_SZ), _I, _P]),
     "g5_plugin_compress": (_I, [_P, _SZ, C.POINTER(_P), C.POINTER(_SZ), _U32, _I]),
     "g5_plugin_decompress": (_I, [_P, _SZ, C.POINTER(_P), C.POINTER(_SZ), _U32, _I]),
     "g5_bitmap_or": (_I, [_P, _P, _I, _SZ, _P]),

@@ -27,8 +27,10 @@
 // the chain is resolved with binary lifting over all 16-byte positions
 // (group starts are always 16-byte aligned), then one warp unpacks each
 // miniblock and a prefix sum over miniblocks restores absolute values.
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "g5_codec_dev.cuh"
 #include "g5_common.cuh"
@@ -855,3 +857,81 @@ g5_status g5_codec_decode(g5_codec *c, const uint32_t *in_dev, size_t words, uin
 }
 
 }  // extern "C"
+
+// ---- encode without allocation ---------------------------------------------------------
+//
+// For callers that must not touch the CUDA allocator at all: a serving loop
+// that may not block on (or fragment) device memory between requests, or a
+// host process whose device memory is owned by another allocator (a
+// framework's caching pool) with no headroom for cudaMalloc.  The encoder's
+// scratch (bit widths, payload offsets, scan partials, length scalars) lives
+// in the file-scope array below instead of a g5_codec workspace.  Every GPU
+// that loads the library holds these bytes until the process exits.
+
+namespace {
+
+constexpr size_t kNoAllocMaxValues = (size_t)1 << 20;          // values per call
+constexpr size_t kNoAllocMb = kNoAllocMaxValues / 128 + 1;       // miniblocks
+constexpr size_t kNoAllocParts = 4096;                           // scan partials
+constexpr size_t kNoAllocBytes = 128 + 8 + kNoAllocMb * 4 + kNoAllocMb + kNoAllocParts * 4 + 256;
+
+// In host code this name is only a host-side stand-in for the device array;
+// kernels receive the device address fetched with cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g5_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[256] = {nullptr};  // per device ordinal
+
+}  // namespace
+
+extern "C" g5_status g5_codec_encode_noalloc(const uint32_t *in_dev, size_t n, uint32_t *out_dev,
+                                             size_t *out_words, int mode, void *stream)
+{
+    if ((n && !in_dev) || !out_dev || !out_words) return G5_ERR_INVALID_ARG;
+    if (mode != G5_CODEC_D4 && mode != G5_CODEC_DM) return G5_ERR_INVALID_ARG;
+    if (((uintptr_t)in_dev | (uintptr_t)out_dev) & 15) return G5_ERR_INVALID_ARG;
+    if (n > kNoAllocMaxValues) {
+        if (getenv("G5_VERBOSE"))
+            fprintf(stderr, "g5_codec_encode_noalloc: %zu values exceed the limit of %zu\n", n, kNoAllocMaxValues);
+        return G5_ERR_CAPACITY;
+    }
+    int dev = 0;
+    G5_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return G5_ERR_INVALID_ARG;
+    void *base = nullptr;
+    {
+        // set-up, once per device, with that device current
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void *p = nullptr;
+            G5_CUDA(cudaGetSymbolAddress(&p, g5_noalloc_scratch));
+            g_noalloc_addr[dev] = p;
+        }
+        base = g_noalloc_addr[dev];
+    }
+    unsigned char *b = static_cast<unsigned char *>(base);
+    g5::CodecWork w;
+    w.max_n = kNoAllocMaxValues;
+    w.max_mb = kNoAllocMb;
+    w.grid = std::min(g5::num_sms() * 4, (int)kNoAllocParts - 1);
+    w.scal = reinterpret_cast<uint64_t *>(b);                        // 16 scalars
+    uint64_t *n_dev = reinterpret_cast<uint64_t *>(b + 128);
+    w.mb_len = reinterpret_cast<uint32_t *>(b + 136);
+    w.mb_bits = reinterpret_cast<uint8_t *>(b + 136 + kNoAllocMb * 4);
+    const size_t off_part = (136 + 5 * kNoAllocMb + 7) & ~(size_t)7;
+    static_assert(((136 + 5 * kNoAllocMb + 7) & ~(size_t)7) + kNoAllocParts * 4 <= kNoAllocBytes,
+                  "scratch layout exceeds the static array");
+    w.part = reinterpret_cast<uint64_t *>(b + off_part);
+    cudaStream_t s = (cudaStream_t)stream;
+    uint64_t hn = n;
+    // every scratch word the encoder reads is written earlier in the same
+    // call (k_enc_prep resets the scalars), so nothing needs clearing here
+    G5_CUDA(cudaMemcpyAsync(n_dev, &hn, sizeof hn, cudaMemcpyHostToDevice, s));
+    g5::codec_encode_launch(w, in_dev, n_dev, out_dev, mode, 0, s);
+    G5_CUDA(cudaGetLastError());
+    uint64_t words = 0;
+    G5_CUDA(cudaMemcpyAsync(&words, w.scal + g5::CS_WORDS, sizeof words, cudaMemcpyDeviceToHost, s));
+    G5_CUDA(cudaStreamSynchronize(s));
+    *out_words = (size_t)words;
+    return G5_OK;
+}

@@ -219,6 +219,22 @@ g5_status g5_codec_encode(g5_codec *c, const uint32_t *in_dev, size_t n, uint32_
 g5_status g5_codec_decode(g5_codec *c, const uint32_t *in_dev, size_t words, uint32_t *out_dev,
                           size_t out_cap, size_t *out_n, int mode, void *stream);
 
+/* Same stream as g5_codec_encode, for callers that cannot allocate device
+ * memory: a serving loop that must never block on or fragment the CUDA
+ * allocator between requests, or a process whose device memory belongs to
+ * another allocator (a framework's caching pool) with nothing left for
+ * cudaMalloc.  It needs no g5_codec: its scratch is a fixed 64 KiB array in
+ * the library's device image, held on every GPU that loads the library until
+ * the process exits, and it calls no allocating function.  At most 1,048,576
+ * values per call (more gives G5_ERR_CAPACITY).  The first call on a device
+ * looks up that device's copy of the array (cudaGetSymbolAddress), so make
+ * it before any stream capture.  All calls share the one array: calls that
+ * overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  This entry point has no counterpart in the
+ * reference. */
+g5_status g5_codec_encode_noalloc(const uint32_t *in_dev, size_t n, uint32_t *out_dev,
+                                  size_t *out_words, int mode, void *stream);
+
 /* The CpuSimd plugin (cpu_2d/compression/cpusimd.hh:70-118): int64 host
  * queue -> *compressed (malloc'd by this call, caller frees, as the reference
  * caller does at cpu_2d/globalbfs.hh:903), raw uint32 when size <= threshold.
