@@ -50,6 +50,12 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep Beamer's alpha=14, beta=24")
+    ap.add_argument("--alpha", type=float, default=None)
+    ap.add_argument("--beta", type=float, default=None)
+    ap.add_argument("--host-loop", action="store_true",
+                    help="host-driven level loop (same kernels, one launch each; for ncu, which "
+                         "cannot profile kernels inside graphs with conditional nodes)")
     return ap.parse_args()
 
 
@@ -259,13 +265,31 @@ def main():
     gen_s = time.time() - t0
     roots = g5.select_roots(g, args.roots)
     nr = len(roots)
-    bfs = g5.CudaBFS(g)
+    # Graph500 edge counts (untimed)
+    probe = g5.CudaBFS(g)
+    nedges = []
+    for r in roots:
+        probe.runBFS(int(r))
+        nedges.append(probe.teps_edges())
+    probe.close()
 
-    # Graph500 edge counts and validation (untimed)
-    nedges, all_valid, all_minpar = [], True, True
+    # direction thresholds: autotuned on a sample of the roots (untimed)
+    from gpugraph500_gb300 import tune
+    tuned = None
+    alpha, beta = 14.0, 24.0
+    if args.alpha is not None or args.beta is not None:
+        alpha = args.alpha if args.alpha is not None else alpha
+        beta = args.beta if args.beta is not None else beta
+    elif not args.no_tune:
+        k = min(8, nr)
+        tuned = tune.tune_plain(g5, g, roots[:k], nedges[:k])
+        alpha, beta = tuned["alpha"], tuned["beta"]
+    bfs = g5.CudaBFS(g, alpha=alpha, beta=beta, use_graph=not args.host_loop)
+
+    # Graph500 validation of every root on the device (untimed)
+    all_valid, all_minpar = True, True
     for r in roots:
         bfs.runBFS(int(r))
-        nedges.append(bfs.teps_edges())
         v, mp = bfs.validate(int(r))
         all_valid &= v
         all_minpar &= mp
@@ -313,7 +337,7 @@ def main():
     batched = None
     if not args.no_batch and hasattr(g5.lib(), "g5_batch_run"):
         try:
-            batched = bench_batched(g5, torch, g, roots, nedges, args)
+            batched = bench_batched(g5, torch, g, roots, nedges, args, tune if not args.no_tune else None)
         except g5.G5Error as e:
             batched = {"error": str(e)}
 
@@ -337,7 +361,8 @@ def main():
             "config": {"workload": f"plain BFS, kronecker scale {args.scale} edgefactor 16, {nr} roots",
                        "n": g.n, "nnz": g.nnz, "roots": nr, "parallelism": "replicas" if ws > 1 else "1 GPU",
                        "l2": "inputs larger than L2 (CSR %.1f GB)" % ((g.nnz * 4 + g.n * 8) / 1e9),
-                       "graph_build_s": round(gen_s, 2)},
+                       "graph_build_s": round(gen_s, 2), "alpha": alpha, "beta": beta,
+                       "tuner": tuned["grid"][:6] if tuned else None},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * nr,
                     "d2h_bytes_per_step": 8 * g.n * nr},
             "gpu_launches": None,
@@ -359,9 +384,12 @@ def main():
     return 0
 
 
-def bench_batched(g5, torch, g, roots, nedges, args):
-    bt = g5.Batch([g])
+def bench_batched(g5, torch, g, roots, nedges, args, tune=None):
     nr = len(roots)
+    tuned = tune.tune_batch(g5, torch, [g], [roots]) if tune is not None else None
+    bt = g5.Batch([g])
+    if tuned:
+        bt.set_direction(tuned["alpha"], tuned["beta"])
     out = torch.empty(nr * g.n, dtype=torch.int32, device="cuda")
     for _ in range(args.warmup):
         bt.run(roots, [nr], out)
@@ -371,7 +399,8 @@ def bench_batched(g5, torch, g, roots, nedges, args):
     total = sum(nedges)
     agg = [total / (m * 1e-3) / 1e9 for m in ms]
     bt.close()
-    return {"aggregate_gteps": hmean(agg), "ms_per_batch": statistics.mean(ms)}
+    return {"aggregate_gteps": hmean(agg), "ms_per_batch": statistics.mean(ms),
+            "alpha": tuned["alpha"] if tuned else 14.0, "beta": tuned["beta"] if tuned else 24.0}
 
 
 if __name__ == "__main__":

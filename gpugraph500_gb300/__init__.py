@@ -48,17 +48,21 @@ class G5Error(RuntimeError):
 class BfsConfig(C.Structure):
     _fields_ = [("alpha", C.c_double), ("beta", C.c_double), ("codec", C.c_int),
                 ("codec_threshold", C.c_uint32), ("use_graph", C.c_int),
-                ("max_levels", C.c_int), ("want_levels", C.c_int)]
+                ("max_levels", C.c_int), ("want_levels", C.c_int), ("profile", C.c_int)]
 
 
 class BfsStats(C.Structure):
     _fields_ = [("levels", C.c_int32), ("bottom_up_levels", C.c_int32), ("visited", C.c_int64),
                 ("edges_td", C.c_int64), ("edges_bu", C.c_int64), ("queue_total", C.c_int64),
                 ("codec_words", C.c_int64), ("codec_values", C.c_int64), ("alg_bytes", C.c_int64),
-                ("device_ms", C.c_double)]
+                ("device_ms", C.c_double), ("kernel_ms", C.c_double * 8)]
+
+    KERNELS = ("prologue", "expand", "fixup", "count", "scan", "write", "codec")
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "kernel_ms"}
+        d["kernel_ms"] = dict(zip(self.KERNELS, list(self.kernel_ms)))
+        return d
 
 
 _lib_handle = None
@@ -80,11 +84,13 @@ SIGNATURES = {
     "g5_bfs_create": (_I, [_P, C.POINTER(BfsConfig), C.POINTER(_P)]),
     "g5_bfs_destroy": (_I, [_P]),
     "g5_bfs_run": (_I, [_P, _I64, _P, _P, C.POINTER(BfsStats)]),
+    "g5_bfs_level_log": (_I, [_P, _P, _I, C.POINTER(_I)]),
     "g5_bfs_device_pred": (_I, [_P, C.POINTER(_P)]),
     "g5_bfs_teps_edges": (_I, [_P, C.POINTER(_I64)]),
     "g5_bfs_validate": (_I, [_P, _I64, C.POINTER(_I), C.POINTER(_I)]),
     "g5_batch_create": (_I, [_P, _I, C.POINTER(_P)]),
     "g5_batch_destroy": (_I, [_P]),
+    "g5_batch_set_direction": (_I, [_P, C.c_double, C.c_double]),
     "g5_batch_run": (_I, [_P, _P, _P, _P, C.POINTER(C.c_double)]),
     "g5_codec_bound": (_SZ, [_SZ]),
     "g5_codec_create": (_I, [_SZ, C.POINTER(_P)]),
@@ -215,11 +221,12 @@ class CudaBFS:
 
     def __init__(self, graph: Graph, codec: int = CODEC_NONE, codec_threshold: int = 64,
                  alpha: float = 14.0, beta: float = 24.0, use_graph: bool = True,
-                 want_levels: bool = False, max_levels: int = 4096):
+                 want_levels: bool = False, max_levels: int = 4096, profile: bool = False):
         self.graph = graph
         cfg = default_config()
         cfg.alpha, cfg.beta, cfg.codec, cfg.codec_threshold = alpha, beta, codec, codec_threshold
         cfg.use_graph, cfg.want_levels, cfg.max_levels = int(use_graph), int(want_levels), max_levels
+        cfg.profile = int(profile)
         self.cfg = cfg
         h = C.c_void_p()
         _check(lib().g5_bfs_create(graph._h, C.byref(cfg), C.byref(h)), "g5_bfs_create")
@@ -244,6 +251,13 @@ class CudaBFS:
 
     def getLevels(self) -> np.ndarray:
         return self._level
+
+    def level_log(self) -> np.ndarray:
+        """(levels, 4) int64: direction, frontier vertices, their edges, entries read."""
+        out = np.zeros((4096, 4), np.int64)
+        rows = C.c_int()
+        _check(lib().g5_bfs_level_log(self._h, _ptr(out), 4096, C.byref(rows)), "g5_bfs_level_log")
+        return out[: rows.value].copy()
 
     def device_pred_ptr(self) -> int:
         p = C.c_void_p()
@@ -377,6 +391,9 @@ class Batch:
         h = C.c_void_p()
         _check(lib().g5_batch_create(arr, len(self.graphs), C.byref(h)), "g5_batch_create")
         self._h = h
+
+    def set_direction(self, alpha: float, beta: float) -> None:
+        _check(lib().g5_batch_set_direction(self._h, alpha, beta), "g5_batch_set_direction")
 
     def run(self, roots: np.ndarray, nroots: Sequence[int], pred_out_dev) -> float:
         roots = np.ascontiguousarray(roots, dtype=np.int64)

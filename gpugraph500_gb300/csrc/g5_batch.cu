@@ -11,9 +11,10 @@
 // Per level and per graph the direction is chosen as in the plain search
 // (Beamer's alpha/beta on the union frontier):
 //   top-down   edge-balanced tiles over the active-vertex queue; for an edge
-//              (u, v) the roots new to v are front[u] & ~visited[v]; they are
-//              OR-ed into next[v] and each root's parent slot takes an
-//              atomicMin with u
+//              (u, v) the roots new to v, front[u] & ~visited[v], are OR-ed
+//              into next[v] (L2 atomics only); a fix-up sweep then gives each
+//              new (vertex, root) pair the first frontier hit of the vertex's
+//              ascending adjacency as parent
 //   bottom-up  each vertex not yet visited by every root scans its ascending
 //              adjacency: hit = front[u] & still-needed roots; the first hit
 //              of a root is its parent; the scan stops once no root is needed
@@ -73,6 +74,7 @@ struct BArgs {
     uint32_t nchunks;
     uint64_t ntot;          // padded global vertex count
     const uint32_t *deg;    // per global vertex
+    const uint32_t *heavy;  // one bit per global vertex of degree > 64
     uint64_t *vis, *front, *next;
     uint32_t *pred;         // output parents, root-major per graph
     uint32_t *queue;
@@ -164,16 +166,21 @@ __device__ void bexp_td(const BArgs &a, uint64_t &examined)
                     const GraphDesc &d = a.gd[graph_of(a, ug)];
                     const uint32_t vl = __ldg(d.col + (a.qbase[i] + (int64_t)e));
                     const uint64_t vg = d.vbase + vl;
+                    // roots new to v: light vertices get their parents from
+                    // k_bfix (a short scan of their own adjacency), heavy ones
+                    // (degree > 64) by atomicMin here
                     const uint64_t nb = a.front[ug] & ~a.vis[vg];
                     if (nb) {
-                        atomicOr((unsigned long long *)&a.next[vg], (unsigned long long)nb);
-                        const uint32_t ul = (uint32_t)(ug - d.vbase);
-                        uint64_t x = nb;
-                        while (x) {
-                            const int r = __ffsll((long long)x) - 1;
-                            x &= x - 1;
-                            atomicMin(a.pred + d.pred_base + (uint64_t)r * d.n + vl, ul);
+                        if ((__ldg(a.heavy + (vg >> 5)) >> (vg & 31)) & 1u) {
+                            const uint32_t ul = (uint32_t)(ug - d.vbase);
+                            uint64_t x = nb;
+                            while (x) {
+                                const int r = __ffsll((long long)x) - 1;
+                                x &= x - 1;
+                                atomicMin(a.pred + d.pred_base + (uint64_t)r * d.n + vl, ul);
+                            }
                         }
+                        if (nb & ~a.next[vg]) atomicOr((unsigned long long *)&a.next[vg], (unsigned long long)nb);
                     }
                 }
             }
@@ -184,7 +191,11 @@ __device__ void bexp_td(const BArgs &a, uint64_t &examined)
     }
 }
 
-__device__ void bexp_bu(const BArgs &a, uint64_t &examined)
+// BOTTOM_UP: candidates are the roots that have not visited v; FIXUP (after
+// a top-down level): the roots top-down just marked in next[v].  The first
+// frontier hit of each root along v's ascending adjacency is its parent.
+template <bool FIXUP>
+__device__ void bsweep(const BArgs &a, uint64_t &examined)
 {
     const int lane = g5_lane();
     const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
@@ -194,9 +205,10 @@ __device__ void bexp_bu(const BArgs &a, uint64_t &examined)
         const uint64_t v = w * 32 + lane;
         const int g = graph_of(a, w * 32);
         const GraphDesc &d = a.gd[g];
-        if (d.dir != BU || d.nf == 0) continue;
+        if (d.dir != (FIXUP ? TD : BU) || d.nf == 0) continue;
         const uint64_t vl = v - d.vbase;
-        uint64_t need = ((int64_t)vl < d.n) ? (~a.vis[v] & d.mask) : 0;
+        const bool light = !((__ldg(a.heavy + (v >> 5)) >> lane) & 1u);
+        uint64_t need = ((int64_t)vl < d.n) ? (FIXUP ? (light ? a.next[v] : 0ull) : (~a.vis[v] & d.mask)) : 0;
         int64_t s = 0, e = 0;
         if (need) {
             s = d.row_off[vl];
@@ -268,10 +280,12 @@ __device__ void bexp_bu(const BArgs &a, uint64_t &examined)
             jj = min(jj, ee);
             if (lane == l) {
                 found |= fnd;
+                need = nd;
                 ex += (uint64_t)(jj - st);
             }
         }
-        if (found) atomicOr((unsigned long long *)&a.next[v], (unsigned long long)found);
+        if (!FIXUP && found) atomicOr((unsigned long long *)&a.next[v], (unsigned long long)found);
+        if (FIXUP && need) atomicOr(&a.st->err, 16u);  // cannot happen on a symmetric CSR
         examined += ex;
     }
 }
@@ -281,9 +295,17 @@ __global__ void __launch_bounds__(kB) k_bexp(BArgs a)
     if (a.st->err || a.st->level < 0 || a.st->active == 0) return;
     uint64_t ex_td = 0, ex_bu = 0;
     bexp_td(a, ex_td);
-    bexp_bu(a, ex_bu);
+    bsweep<false>(a, ex_bu);
     (void)ex_td;
     (void)ex_bu;
+}
+
+__global__ void __launch_bounds__(kB) k_bfix(BArgs a)
+{
+    if (a.st->err || a.st->level < 0 || a.st->active == 0) return;
+    uint64_t ex = 0;
+    bsweep<true>(a, ex);
+    (void)ex;
 }
 
 // ---- compaction ---------------------------------------------------------------------------
@@ -498,13 +520,17 @@ __global__ void __launch_bounds__(kB) k_bwrite(BArgs a)
     }
 }
 
-__global__ void k_bdeg(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t ntot, uint32_t *deg)
+__global__ void k_bdeg(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t ntot, uint32_t *deg,
+                       uint32_t *heavy)
 {
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < ntot;
          v += (uint64_t)gridDim.x * blockDim.x) {
         const GraphDesc &d = gd[chunk_graph[v / kChunk]];
         const int64_t vl = (int64_t)(v - d.vbase);
-        deg[v] = vl < d.n ? (uint32_t)(d.row_off[vl + 1] - d.row_off[vl]) : 0u;
+        const uint32_t dv = vl < d.n ? (uint32_t)(d.row_off[vl + 1] - d.row_off[vl]) : 0u;
+        deg[v] = dv;
+        const unsigned h = __ballot_sync(0xFFFFFFFFu, dv > 64u);
+        if ((threadIdx.x & 31) == 0) heavy[v >> 5] = h;
     }
 }
 
@@ -518,6 +544,7 @@ struct g5_batch {
     GraphDesc *gd = nullptr;
     uint8_t *chunk_graph = nullptr;
     uint32_t *deg = nullptr;
+    uint32_t *heavy = nullptr;
     uint64_t *words = nullptr;  // vis | front | next
     uint32_t *queue = nullptr;
     uint64_t *qoff = nullptr;
@@ -550,6 +577,7 @@ void enqueue_batch(g5_batch *b, const BArgs &a, cudaStream_t s, bool body)
     k_bscan<<<1, 1024, 0, s>>>(a);
     k_bwrite<<<a.nchunks, kB, 0, s>>>(a);
     k_bexp<<<g5::grid_for(8), kB, 0, s>>>(a);
+    k_bfix<<<g5::grid_for(8), kB, 0, s>>>(a);
 }
 
 g5_status build_batch_graph(g5_batch *b)
@@ -597,6 +625,7 @@ void free_batch(g5_batch *b)
     cudaFree(b->gd);
     cudaFree(b->chunk_graph);
     cudaFree(b->deg);
+    cudaFree(b->heavy);
     cudaFree(b->words);
     cudaFree(b->queue);
     cudaFree(b->qoff);
@@ -664,6 +693,7 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     B_ALLOC(b->gd, sizeof(GraphDesc) * ngraphs);
     B_ALLOC(b->chunk_graph, cg.size());
     B_ALLOC(b->deg, sizeof(uint32_t) * vb);
+    B_ALLOC(b->heavy, sizeof(uint32_t) * (vb / 32));
     B_ALLOC(b->words, sizeof(uint64_t) * 3 * vb);
     B_ALLOC(b->queue, sizeof(uint32_t) * vb);
     B_ALLOC(b->qoff, sizeof(uint64_t) * (vb + 1));
@@ -685,6 +715,7 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     a.gd = b->gd;
     a.chunk_graph = b->chunk_graph;
     a.deg = b->deg;
+    a.heavy = b->heavy;
     a.vis = b->words;
     a.front = b->words + vb;
     a.next = b->words + 2 * vb;
@@ -698,9 +729,18 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     a.roots = b->roots;
     a.root_off = b->root_off;
     a.level_log = b->level_log;
-    k_bdeg<<<g5::grid_for(8), kB, 0, b->stream>>>(b->gd, b->chunk_graph, vb, b->deg);
+    k_bdeg<<<g5::grid_for(8), kB, 0, b->stream>>>(b->gd, b->chunk_graph, vb, b->deg, b->heavy);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
     *out = b;
+    return G5_OK;
+}
+
+g5_status g5_batch_set_direction(g5_batch *b, double alpha, double beta)
+{
+    if (!b || !(alpha > 0) || !(beta > 0)) return G5_ERR_INVALID_ARG;
+    b->args.alpha = alpha;
+    b->args.beta = beta;
+    b->bound_pred = nullptr;  // rebuild the graph with the new kernel arguments
     return G5_OK;
 }
 

@@ -4,8 +4,9 @@
 // the b40c enactor it drives (b40c/graph/bfs/enactor_multi_gpu_2d.cuh:741-1101)
 // for a 1x1 process grid.  Per level, all on the device:
 //
-//   expand   top-down (queue, edge-balanced tiles, atomicMin parent) or
+//   expand   top-down (queue, edge-balanced tiles, next-bit atomicOr) or
 //            bottom-up (bitmap sweep, first hit in the sorted adjacency)
+//   fixup    after top-down: parents of the new vertices (first frontier hit)
 //   count    popcount + degree sum of the next-frontier bitmap per chunk
 //   scan     chunk prefix sums, Beamer direction switch, loop condition
 //   write    visited |= next, next -> front, sorted queue + edge offsets
@@ -18,8 +19,11 @@
 // cuda_bfs.cu:252-269,397-450,524-529).
 //
 // Parent choice: a vertex discovered at level L+1 gets the smallest adjacent
-// vertex of level L.  Top-down reaches it with a 64-bit atomicMin, bottom-up
-// with the first frontier hit of the ascending adjacency.  This is the parent
+// vertex of level L: the first frontier hit of its ascending adjacency, found
+// by the bottom-up sweep itself or, after a top-down level (which only sets
+// next-frontier bits for vertices of degree <= 64), by a fix-up sweep over the
+// new vertices; vertices of higher degree get it from a 64-bit atomicMin in
+// the top-down kernel instead of a long scan.  This is the parent
 // CPUBFS_bin's ascending first-writer sweep picks (cpu_2d/cpubfs_bin.cpp:
 // 143-180), so parents equal the reference CPU path's, not only valid ones.
 #include <algorithm>
@@ -38,7 +42,8 @@ constexpr int kWarps = kBlock / 32;
 constexpr int kChunkWords = 2048;  // bitmap words per compaction chunk
 constexpr int kWordsPerThread = kChunkWords / kBlock;
 constexpr uint64_t kTile = 256;    // frontier edges per top-down warp tile
-constexpr int kBuSerial = 6;       // bottom-up entries scanned per lane first
+constexpr int kBuSerial = 8;       // entries a lane scans alone before the warp helps
+constexpr uint32_t kHeavy = 64;    // degree above which top-down sets the parent itself
 
 enum : int32_t { DIR_TD = 0, DIR_BU = 1 };
 
@@ -82,6 +87,7 @@ struct BfsArgs {
     uint64_t *qoff;       // edge offset of each queue entry (+ sentinel)
     int64_t *qbase;       // row_off[u] - qoff[i]
     uint32_t *tile_start; // first queue index of each top-down tile
+    const uint32_t *heavy; // one bit per vertex of degree > kHeavy
     uint64_t max_tiles;
     uint64_t *chunk_n;
     uint64_t *chunk_m;
@@ -194,13 +200,16 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
                     // a queued vertex without edges: only a non-symmetric CSR
                     atomicOr(&a.st->err, G5_DEVERR_CAPACITY);
                 } else {
-                    const uint32_t u = a.qsrc[i];
+                    // light vertices: only the next-frontier bit is set here
+                    // (an L2-resident atomic) and k_fixup finds the parent in
+                    // the vertex's short adjacency; heavy vertices, whose scan
+                    // could be long, take the smallest parent by atomicMin
                     const uint32_t v = __ldg(a.col + (a.qbase[i] + (int64_t)e));
-                    const uint32_t vw = a.visited[v >> 5];
-                    if (!((vw >> (v & 31)) & 1u)) {
-                        unsigned long long old =
-                            atomicMin((unsigned long long *)(a.pred + v), (unsigned long long)u);
-                        if (old == ~0ull) atomicOr(a.next + (v >> 5), 1u << (v & 31));
+                    const uint32_t bit = 1u << (v & 31);
+                    if (!(a.visited[v >> 5] & bit)) {
+                        if (__ldg(a.heavy + (v >> 5)) & bit)
+                            atomicMin((unsigned long long *)(a.pred + v), (unsigned long long)a.qsrc[i]);
+                        if (!(a.next[v >> 5] & bit)) atomicOr(a.next + (v >> 5), bit);
                     }
                 }
             }
@@ -211,18 +220,42 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
     }
 }
 
-__device__ void expand_bu(const BfsArgs &a, uint64_t &examined)
+// One warp per 32-vertex word.  BOTTOM_UP: the candidates are the unvisited
+// vertices; a candidate with a neighbour in the frontier joins the next
+// frontier with the first such neighbour of its ascending adjacency as parent.
+// FIXUP (after a top-down level): the candidates are the vertices top-down
+// just discovered; each takes the first frontier neighbour of its adjacency.
+// Either way the parent is the smallest neighbour in the frontier.
+template <bool FIXUP>
+__device__ void sweep(const BfsArgs &a, uint64_t &examined)
 {
     const int lane = g5_lane();
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const uint32_t *__restrict__ front = a.front;
     const uint32_t *__restrict__ col = a.col;
-    for (uint64_t w = gw; w < a.nwords; w += nw) {
-        const uint32_t vis = a.visited[w];
-        if (vis == 0xFFFFFFFFu) continue;
+    // FIXUP candidates are sparse: a warp loads 32 words at once (one per
+    // lane, coalesced) and visits only the non-empty ones.  Bottom-up
+    // candidates are dense: one word per warp step keeps more words in flight.
+    const uint64_t step = FIXUP ? 32 : 1;
+    for (uint64_t w0 = gw * step; w0 < a.nwords; w0 += nw * step) {
+      uint32_t cw = 0;
+      unsigned act;
+      if (FIXUP) {
+          const uint64_t wl = w0 + lane;
+          if (wl < a.nwords) cw = a.next[wl] & ~__ldg(a.heavy + wl);
+          act = __ballot_sync(0xFFFFFFFFu, cw != 0u);
+      } else {
+          cw = ~a.visited[w0];
+          act = cw ? 1u : 0u;
+      }
+      while (act) {
+        const int jw = __ffs(act) - 1;
+        act &= act - 1;
+        const uint64_t w = w0 + jw;
+        const uint32_t cand_word = FIXUP ? __shfl_sync(0xFFFFFFFFu, cw, jw) : cw;
         const uint64_t v = w * 32 + lane;
-        const bool mine = !((vis >> lane) & 1u);
+        const bool mine = (cand_word >> lane) & 1u;
         int64_t s = 0, e = 0;
         if (mine) {
             s = a.row_off[v];
@@ -231,16 +264,27 @@ __device__ void expand_bu(const BfsArgs &a, uint64_t &examined)
         bool found = false;
         uint32_t par = 0;
         int64_t j = s;
+        // first entries per lane, four independent loads at a time
         const int64_t lim = min(e, s + kBuSerial);
-        for (; j < lim; ++j) {
-            const uint32_t u = __ldg(col + j);
-            if ((__ldg(front + (u >> 5)) >> (u & 31)) & 1u) {
+        while (j < lim && !found) {
+            uint32_t u[4];
+            bool h[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) u[k] = (j + k < lim) ? __ldg(col + j + k) : 0u;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                h[k] = (j + k < lim) && ((__ldg(front + (u[k] >> 5)) >> (u[k] & 31)) & 1u);
+            int k = 0;
+            while (k < 4 && j + k < lim && !h[k]) ++k;
+            if (k < 4 && j + k < lim) {
                 found = true;
-                par = u;
-                break;
+                par = u[k];
+                j += k + 1;
+            } else {
+                j = min(j + 4, lim);
             }
         }
-        uint64_t ex = mine ? (uint64_t)(j - s) + (found ? 1 : 0) : 0;
+        uint64_t ex = (uint64_t)(j - s);
         unsigned pend = __ballot_sync(0xFFFFFFFFu, mine && !found && j < e);
         while (pend) {
             const int l = __ffs(pend) - 1;
@@ -275,10 +319,15 @@ __device__ void expand_bu(const BfsArgs &a, uint64_t &examined)
                 ex += (uint64_t)(jj - st);
             }
         }
-        const unsigned fm = __ballot_sync(0xFFFFFFFFu, found);
         if (found) a.pred[v] = (int64_t)par;
-        if (lane == 0 && fm) a.next[w] = fm;
+        if (FIXUP) {
+            if (mine && !found) atomicOr(&a.st->err, G5_DEVERR_CAPACITY);  // cannot happen on a symmetric CSR
+        } else {
+            const unsigned fm = __ballot_sync(0xFFFFFFFFu, found);
+            if (lane == 0 && fm) a.next[w] = fm;
+        }
         examined += ex;
+      }
     }
 }
 
@@ -287,7 +336,24 @@ __global__ void __launch_bounds__(kBlock) k_expand(BfsArgs a)
     uint64_t examined = 0;
     if (a.st->err) return;
     if (a.st->dir == DIR_TD) expand_td(a, examined);
-    else expand_bu(a, examined);
+    else sweep<false>(a, examined);
+    examined = warp_sum_u64(examined);
+    __shared__ uint64_t s_ex[kWarps];
+    if (g5_lane() == 0) s_ex[threadIdx.x >> 5] = examined;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t t = 0;
+        for (int i = 0; i < kWarps; ++i) t += s_ex[i];
+        if (t) atomicAdd((unsigned long long *)&a.st->examined, (unsigned long long)t);
+    }
+}
+
+// Parents of the vertices a top-down level discovered (no-op after bottom-up).
+__global__ void __launch_bounds__(kBlock) k_fixup(BfsArgs a)
+{
+    if (a.st->err || a.st->dir != DIR_TD) return;
+    uint64_t examined = 0;
+    sweep<true>(a, examined);
     examined = warp_sum_u64(examined);
     __shared__ uint64_t s_ex[kWarps];
     if (g5_lane() == 0) s_ex[threadIdx.x >> 5] = examined;
@@ -301,20 +367,45 @@ __global__ void __launch_bounds__(kBlock) k_expand(BfsArgs a)
 
 // ---- compaction: count, scan, write ----------------------------------------------
 
-__device__ __forceinline__ void thread_words(const BfsArgs &a, uint64_t w0, uint32_t *wd)
-{
-#pragma unroll
-    for (int k = 0; k < kWordsPerThread; ++k) wd[k] = (w0 + k < a.nwords) ? a.next[w0 + k] : 0u;
-}
+// A compaction chunk is kChunkWords bitmap words; each of the 8 warps of a
+// block owns 256 consecutive words and walks them 32 at a time: lane l loads
+// word l (coalesced), then for every non-empty word the lanes read the
+// degrees of its set vertices in one coalesced 128-byte load.
+constexpr int kWordsPerWarp = kChunkWords / kWarps;
 
-__device__ __forceinline__ void count_words(const BfsArgs &a, uint64_t w0, const uint32_t *wd,
-                                            uint64_t &cn, uint64_t &cm)
+__device__ __forceinline__ void warp_chunk_counts(const BfsArgs &a, uint64_t wbeg, uint64_t &cn, uint64_t &cm)
 {
+    const int lane = g5_lane();
     cn = 0;
     cm = 0;
+    for (int g = 0; g < kWordsPerWarp; g += 32) {
+        const uint64_t wl = wbeg + g + lane;
+        const uint32_t x = wl < a.nwords ? a.next[wl] : 0u;
+        cn += __popc(x);
+        unsigned act = __ballot_sync(0xFFFFFFFFu, x != 0u);
+        while (act) {
+            const int j = __ffs(act) - 1;
+            act &= act - 1;
+            const uint32_t wj = __shfl_sync(0xFFFFFFFFu, x, j);
+            if ((wj >> lane) & 1u) cm += __ldg(a.deg + (wbeg + g + j) * 32 + lane);
+        }
+    }
+    cn = warp_sum_u64(cn);
+    cm = warp_sum_u64(cm);
+}
+
+// Counting: each thread owns kChunkWords / kBlock consecutive words and sums
+// popcounts and the degrees of their set vertices (independent loads per
+// thread; faster here than the lane-parallel walk of k_write).
+
+__global__ void __launch_bounds__(kBlock) k_count(BfsArgs a)
+{
+    const uint32_t c = blockIdx.x;
+    const uint64_t w0 = (uint64_t)c * kChunkWords + (uint64_t)threadIdx.x * kWordsPerThread;
+    uint64_t cn = 0, cm = 0;
 #pragma unroll
     for (int k = 0; k < kWordsPerThread; ++k) {
-        uint32_t x = wd[k];
+        uint32_t x = (w0 + k < a.nwords) ? a.next[w0 + k] : 0u;
         cn += __popc(x);
         while (x) {
             const int b = __ffs(x) - 1;
@@ -322,16 +413,6 @@ __device__ __forceinline__ void count_words(const BfsArgs &a, uint64_t w0, const
             cm += __ldg(a.deg + (w0 + k) * 32 + b);
         }
     }
-}
-
-__global__ void __launch_bounds__(kBlock) k_count(BfsArgs a)
-{
-    const uint32_t c = blockIdx.x;
-    const uint64_t w0 = (uint64_t)c * kChunkWords + (uint64_t)threadIdx.x * kWordsPerThread;
-    uint32_t wd[kWordsPerThread];
-    thread_words(a, w0, wd);
-    uint64_t cn, cm;
-    count_words(a, w0, wd, cn, cm);
     cn = warp_sum_u64(cn);
     cm = warp_sum_u64(cm);
     __shared__ uint64_t s_n[kWarps], s_m[kWarps];
@@ -443,76 +524,66 @@ __global__ void __launch_bounds__(1024) k_scan(BfsArgs a)
 __global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
 {
     const uint32_t c = blockIdx.x;
-    const uint64_t w0 = (uint64_t)c * kChunkWords + (uint64_t)threadIdx.x * kWordsPerThread;
-    uint32_t wd[kWordsPerThread];
-    thread_words(a, w0, wd);
+    const int lane = g5_lane(), wid = threadIdx.x >> 5;
+    const uint64_t wbeg = (uint64_t)c * kChunkWords + (uint64_t)wid * kWordsPerWarp;
     const int32_t L = a.st->level;  // index of the new frontier
     const bool want_q = a.st->want_queue != 0;
-    // bitmaps
-#pragma unroll
-    for (int k = 0; k < kWordsPerThread; ++k) {
-        const uint64_t w = w0 + k;
-        if (w < a.nwords) {
-            if (wd[k]) {
-                a.visited[w] |= wd[k];
-                a.next[w] = 0;
-            }
-            a.front[w] = wd[k];
-        }
-    }
-    if (!want_q && !a.level) return;
-    uint64_t cn, cm;
-    count_words(a, w0, wd, cn, cm);
-    // block scan of (cn, cm)
-    __shared__ uint64_t s_n[kWarps + 1], s_m[kWarps + 1];
-    const int lane = g5_lane(), wid = threadIdx.x >> 5;
-    uint64_t xn = cn, xm = cm;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint64_t yn = __shfl_up_sync(0xFFFFFFFFu, xn, o);
-        uint64_t ym = __shfl_up_sync(0xFFFFFFFFu, xm, o);
-        if (lane >= o) {
-            xn += yn;
-            xm += ym;
-        }
-    }
-    if (lane == 31) {
-        s_n[wid] = xn;
-        s_m[wid] = xm;
+    // per-warp totals, then the warp's offsets inside the chunk
+    uint64_t cn = 0, cm = 0;
+    if (want_q || a.level) warp_chunk_counts(a, wbeg, cn, cm);
+    __shared__ uint64_t s_n[kWarps], s_m[kWarps];
+    if (lane == 0) {
+        s_n[wid] = cn;
+        s_m[wid] = cm;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        uint64_t an = 0, am = 0;
-        for (int i = 0; i < kWarps; ++i) {
-            uint64_t tn = s_n[i], tm = s_m[i];
-            s_n[i] = an;
-            s_m[i] = am;
-            an += tn;
-            am += tm;
-        }
+    uint64_t pos = a.chunk_n[c], mpos = a.chunk_m[c];
+    for (int i = 0; i < wid; ++i) {
+        pos += s_n[i];
+        mpos += s_m[i];
     }
-    __syncthreads();
-    uint64_t pos = a.chunk_n[c] + s_n[wid] + xn - cn;
-    uint64_t mpos = a.chunk_m[c] + s_m[wid] + xm - cm;
-#pragma unroll
-    for (int k = 0; k < kWordsPerThread; ++k) {
-        uint32_t x = wd[k];
-        while (x) {
-            const int b = __ffs(x) - 1;
-            x &= x - 1;
-            const uint64_t v = (w0 + k) * 32 + b;
-            if (a.level) a.level[v] = L;
-            if (want_q) {
-                const uint64_t d = __ldg(a.deg + v);
-                a.queue[pos] = (uint32_t)v;
-                a.qoff[pos] = mpos;
-                a.qbase[pos] = a.row_off[v] - (int64_t)mpos;
-                uint64_t t = (mpos + kTile - 1) / kTile;
-                const uint64_t tend = (mpos + d + kTile - 1) / kTile;
-                for (; t < tend && t < a.max_tiles; ++t) a.tile_start[t] = (uint32_t)pos;
-                mpos += d;
+    for (int g = 0; g < kWordsPerWarp; g += 32) {
+        const uint64_t wl = wbeg + g + lane;
+        uint32_t x = 0;
+        if (wl < a.nwords) {
+            x = a.next[wl];
+            if (x) {
+                a.visited[wl] |= x;
+                a.next[wl] = 0;
             }
-            ++pos;
+            a.front[wl] = x;
+        }
+        if (!want_q && !a.level) continue;
+        unsigned act = __ballot_sync(0xFFFFFFFFu, x != 0u);
+        while (act) {
+            const int j = __ffs(act) - 1;
+            act &= act - 1;
+            const uint32_t wj = __shfl_sync(0xFFFFFFFFu, x, j);
+            const bool mine = (wj >> lane) & 1u;
+            const uint64_t v = (wbeg + g + j) * 32 + lane;
+            uint64_t d = mine ? (uint64_t)__ldg(a.deg + v) : 0;
+            // inclusive scan of the degrees of this word's vertices
+            uint64_t incl = d;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (mine) {
+                const uint64_t p = pos + __popc(wj & g5_lanemask_lt());
+                const uint64_t mp = mpos + incl - d;
+                if (a.level) a.level[v] = L;
+                if (want_q) {
+                    a.queue[p] = (uint32_t)v;
+                    a.qoff[p] = mp;
+                    a.qbase[p] = a.row_off[v] - (int64_t)mp;
+                    uint64_t t = (mp + kTile - 1) / kTile;
+                    const uint64_t tend = (mp + d + kTile - 1) / kTile;
+                    for (; t < tend && t < a.max_tiles; ++t) a.tile_start[t] = (uint32_t)p;
+                }
+            }
+            pos += __popc(wj);
+            mpos += __shfl_sync(0xFFFFFFFFu, incl, 31);
         }
     }
 }
@@ -635,6 +706,28 @@ __global__ void k_val_edges(const int64_t *__restrict__ row_off, const uint32_t 
     }
 }
 
+// Kernel kinds timed in profile mode.
+enum { KP_PRO = 0, KP_EXPAND, KP_FIXUP, KP_COUNT, KP_SCAN, KP_WRITE, KP_CODEC, KP_N };
+
+struct Prof {
+    bool on = false;
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> kind;
+    size_t used = 0;
+    void mark(int k, cudaStream_t s)
+    {
+        if (!on) return;
+        if (used + 1 > ev.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            ev.push_back(e);
+            kind.push_back(0);
+        }
+        kind[used] = k;
+        cudaEventRecord(ev[used++], s);
+    }
+};
+
 }  // namespace
 
 // ---- workspace --------------------------------------------------------------------
@@ -646,6 +739,8 @@ struct g5_bfs {
     BfsArgs args;
     uint32_t *deg = nullptr;
     uint32_t *bitmaps = nullptr;  // visited | front | next
+    uint32_t *isolated = nullptr; // one bit per vertex of degree 0
+    uint32_t *heavy = nullptr;    // one bit per vertex of degree > kHeavy
     int64_t *pred = nullptr;
     int32_t *level = nullptr;
     uint32_t *queue = nullptr;
@@ -666,6 +761,7 @@ struct g5_bfs {
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    Prof prof;
     bool ran = false;
     int64_t last_root = -1;
 };
@@ -675,18 +771,30 @@ namespace {
 void enqueue_prologue(g5_bfs *b, cudaStream_t s)
 {
     const BfsArgs &a = b->args;
-    cudaMemsetAsync(b->bitmaps, 0, sizeof(uint32_t) * 3 * a.nwords, s);
+    // vertices without edges can never be reached: they start out visited, so
+    // bottom-up sweeps skip them (the root is set again by k_init)
+    cudaMemcpyAsync(b->bitmaps, b->isolated, sizeof(uint32_t) * a.nwords, cudaMemcpyDeviceToDevice, s);
+    cudaMemsetAsync(b->bitmaps + a.nwords, 0, sizeof(uint32_t) * 2 * a.nwords, s);
     cudaMemsetAsync(b->pred, 0xFF, sizeof(int64_t) * (size_t)a.n, s);
     if (b->level) cudaMemsetAsync(b->level, 0xFF, sizeof(int32_t) * (size_t)a.n, s);
     k_init<<<1, kBlock, 0, s>>>(a);
 }
 
-void enqueue_level(g5_bfs *b, const BfsArgs &a, cudaStream_t s)
+void enqueue_level(g5_bfs *b, const BfsArgs &a, cudaStream_t s, Prof *pf = nullptr)
 {
+    Prof dummy;
+    Prof &p = pf ? *pf : dummy;
+    p.mark(KP_EXPAND, s);
     k_expand<<<g5::grid_for(8), kBlock, 0, s>>>(a);
+    p.mark(KP_FIXUP, s);
+    k_fixup<<<g5::grid_for(8), kBlock, 0, s>>>(a);
+    p.mark(KP_COUNT, s);
     k_count<<<a.nchunks, kBlock, 0, s>>>(a);
+    p.mark(KP_SCAN, s);
     k_scan<<<1, 1024, 0, s>>>(a);
+    p.mark(KP_WRITE, s);
     k_write<<<a.nchunks, kBlock, 0, s>>>(a);
+    p.mark(KP_CODEC, s);
     if (a.codec) {
         g5::codec_encode_launch(b->cw, b->queue, &b->st->nf, b->codec_stream, a.codec,
                                 b->cfg.codec_threshold, s);
@@ -744,6 +852,8 @@ g5_status alloc_ws(g5_bfs *b)
     a.max_levels = b->cfg.max_levels;
     G5_CUDA(cudaMalloc(&b->deg, sizeof(uint32_t) * (size_t)n));
     G5_CUDA(cudaMalloc(&b->bitmaps, sizeof(uint32_t) * 3 * a.nwords));
+    G5_CUDA(cudaMalloc(&b->isolated, sizeof(uint32_t) * a.nwords));
+    G5_CUDA(cudaMalloc(&b->heavy, sizeof(uint32_t) * a.nwords));
     G5_CUDA(cudaMalloc(&b->pred, sizeof(int64_t) * (size_t)n));
     if (b->cfg.want_levels) G5_CUDA(cudaMalloc(&b->level, sizeof(int32_t) * (size_t)n));
     G5_CUDA(cudaMalloc(&b->queue, sizeof(uint32_t) * (size_t)n + 16));
@@ -775,6 +885,7 @@ g5_status alloc_ws(g5_bfs *b)
     a.qoff = b->qoff;
     a.qbase = b->qbase;
     a.tile_start = b->tile_start;
+    a.heavy = b->heavy;
     a.chunk_n = b->chunks;
     a.chunk_m = b->chunks + a.nchunks;
     a.st = b->st;
@@ -788,11 +899,20 @@ g5_status alloc_ws(g5_bfs *b)
     return G5_OK;
 }
 
-__global__ void k_degrees(const int64_t *__restrict__ ro, int64_t n, uint32_t *__restrict__ d)
+__global__ void k_degrees(const int64_t *__restrict__ ro, int64_t n, uint32_t *__restrict__ d,
+                          uint32_t *__restrict__ iso, uint32_t *__restrict__ heavy)
 {
-    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
-         v += (int64_t)gridDim.x * blockDim.x)
-        d[v] = (uint32_t)(ro[v + 1] - ro[v]);
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < ((n + 31) & ~(int64_t)31);
+         v += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t dv = v < n ? (uint32_t)(ro[v + 1] - ro[v]) : 0u;
+        if (v < n) d[v] = dv;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, dv == 0 && v < n);
+        const unsigned h = __ballot_sync(0xFFFFFFFFu, dv > kHeavy);
+        if ((threadIdx.x & 31) == 0) {
+            iso[v >> 5] = m;
+            heavy[v >> 5] = h;
+        }
+    }
 }
 
 void free_ws(g5_bfs *b)
@@ -801,6 +921,8 @@ void free_ws(g5_bfs *b)
     if (b->graph) cudaGraphDestroy(b->graph);
     cudaFree(b->deg);
     cudaFree(b->bitmaps);
+    cudaFree(b->isolated);
+    cudaFree(b->heavy);
     cudaFree(b->pred);
     cudaFree(b->level);
     cudaFree(b->queue);
@@ -819,6 +941,7 @@ void free_ws(g5_bfs *b)
     if (b->cfg.codec) g5::codec_work_free(b->cw);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
+    for (cudaEvent_t e : b->prof.ev) cudaEventDestroy(e);
     if (b->stream) cudaStreamDestroy(b->stream);
 }
 
@@ -853,6 +976,7 @@ void g5_bfs_config_default(g5_bfs_config *cfg)
     cfg->use_graph = 1;
     cfg->max_levels = 4096;
     cfg->want_levels = 0;
+    cfg->profile = 0;
 }
 
 g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
@@ -878,7 +1002,7 @@ g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
     cudaEventCreate(&b->ev0);
     cudaEventCreate(&b->ev1);
     if ((st = alloc_ws(b)) != G5_OK) return fail(st);
-    k_degrees<<<g5::grid_for(8), kBlock, 0, b->stream>>>(g->row_off, g->n, b->deg);
+    k_degrees<<<g5::grid_for(8), kBlock, 0, b->stream>>>(g->row_off, g->n, b->deg, b->isolated, b->heavy);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
     if (b->cfg.use_graph && (st = build_graph(b)) != G5_OK) return fail(st);
     *out = b;
@@ -902,16 +1026,18 @@ g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_
     *b->h_root = root;
     G5_CUDA(cudaMemcpyAsync(b->root_dev, b->h_root, sizeof(int64_t), cudaMemcpyHostToDevice, s));
     G5_CUDA(cudaEventRecord(b->ev0, s));
+    b->prof.on = b->cfg.profile && !b->exec;
+    b->prof.used = 0;
     if (b->exec) {
         G5_CUDA(cudaGraphLaunch(b->exec, s));
     } else {
+        b->prof.mark(KP_PRO, s);
         enqueue_prologue(b, s);
         for (int L = 0; L < b->cfg.max_levels; ++L) {
-            enqueue_level(b, b->args, s);
+            enqueue_level(b, b->args, s, &b->prof);
             G5_CUDA(cudaMemcpyAsync(b->h_st, b->st, sizeof(BfsState), cudaMemcpyDeviceToHost, s));
             G5_CUDA(cudaStreamSynchronize(s));
             if (b->h_st->nf == 0 || b->h_st->err) break;
-            if (b->h_st->level + 2 >= b->cfg.max_levels) break;
         }
     }
     G5_CUDA(cudaEventRecord(b->ev1, s));
@@ -927,12 +1053,13 @@ g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_
     b->ran = true;
     b->last_root = root;
     const BfsState &hs = *b->h_st;
-    if (hs.err & G5_DEVERR_LEVELS) return G5_ERR_TIMEOUT;
-    if (hs.err) return G5_ERR_CAPACITY;
-    if (b->cfg.codec && (cscal[g5::CS_ERR] & G5_DEVERR_MISMATCH)) return G5_ERR_MISMATCH;
-    if (b->cfg.codec && cscal[g5::CS_ERR]) return G5_ERR_CORRUPT_STREAM;
+    g5_status rc = G5_OK;
+    if (hs.err & G5_DEVERR_LEVELS) rc = G5_ERR_TIMEOUT;
+    else if (hs.err) rc = G5_ERR_CAPACITY;
+    else if (b->cfg.codec && (cscal[g5::CS_ERR] & G5_DEVERR_MISMATCH)) rc = G5_ERR_MISMATCH;
+    else if (b->cfg.codec && cscal[g5::CS_ERR]) rc = G5_ERR_CORRUPT_STREAM;
     if (stats) {
-        const int nlev = hs.level + 1;
+        const int nlev = std::min(hs.level + 1, b->cfg.max_levels);
         G5_CUDA(cudaMemcpy(b->h_log, b->log, sizeof(LevelRec) * (size_t)nlev, cudaMemcpyDeviceToHost));
         memset(stats, 0, sizeof *stats);
         stats->levels = nlev;
@@ -952,7 +1079,31 @@ g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_
         float ms = 0;
         cudaEventElapsedTime(&ms, b->ev0, b->ev1);
         stats->device_ms = ms;
+        if (b->prof.on && b->prof.used) {
+            // each mark closes the previous interval; the last one ends at ev1
+            for (size_t i = 0; i < b->prof.used; ++i) {
+                float t = 0;
+                cudaEventElapsedTime(&t, b->prof.ev[i], i + 1 < b->prof.used ? b->prof.ev[i + 1] : b->ev1);
+                const int k = b->prof.kind[i];
+                if (k >= 0 && k < 8) stats->kernel_ms[k] += t;
+            }
+        }
     }
+    return rc;
+}
+
+g5_status g5_bfs_level_log(g5_bfs *b, int64_t *out, int max_rows, int *rows)
+{
+    if (!b || !out || !rows || max_rows < 1 || !b->ran) return G5_ERR_INVALID_ARG;
+    const int nlev = std::min(std::min(b->h_st->level + 1, b->cfg.max_levels), max_rows);
+    G5_CUDA(cudaMemcpy(b->h_log, b->log, sizeof(LevelRec) * (size_t)nlev, cudaMemcpyDeviceToHost));
+    for (int L = 0; L < nlev; ++L) {
+        out[4 * L + 0] = b->h_log[L].dir;
+        out[4 * L + 1] = (int64_t)b->h_log[L].nf;
+        out[4 * L + 2] = (int64_t)b->h_log[L].mf;
+        out[4 * L + 3] = (int64_t)b->h_log[L].examined;
+    }
+    *rows = nlev;
     return G5_OK;
 }
 

@@ -1,0 +1,72 @@
+"""Autotuner for the direction-switch thresholds.
+
+Beamer's alpha/beta (SC'12) were tuned for CPUs; on a GPU the cost of a
+top-down edge and of a bottom-up probe differ, so the thresholds are picked by
+measurement: every (alpha, beta) pair of a small grid runs a sample of roots,
+and the pair with the best harmonic-mean TEPS wins.  Searches are timed with
+the library's CUDA events.  The result is cached per (graph size, edge count)
+in memory for the process.
+"""
+from __future__ import annotations
+
+import itertools
+from typing import Sequence
+
+ALPHAS = (4.0, 14.0, 40.0, 120.0, 400.0)
+BETAS = (12.0, 24.0, 64.0, 200.0)
+
+_cache: dict = {}
+
+
+def _hmean_teps(times_ms, nedges):
+    inv = sum((t * 1e-3) / e for t, e in zip(times_ms, nedges))
+    return len(times_ms) / inv / 1e9 if inv > 0 else 0.0
+
+
+def tune_plain(g5, graph, roots: Sequence[int], nedges: Sequence[int], alphas=ALPHAS, betas=BETAS,
+               reps: int = 2) -> dict:
+    """Best (alpha, beta) for the one-root search on this graph."""
+    key = ("plain", graph.n, graph.nnz, tuple(alphas), tuple(betas))
+    if key in _cache:
+        return _cache[key]
+    results = []
+    for a, b in itertools.product(alphas, betas):
+        bfs = g5.CudaBFS(graph, alpha=a, beta=b)
+        best = None
+        for _ in range(reps):
+            ts = []
+            for r in roots:
+                code = bfs.run(int(r), None, None, stats=True)
+                if code != 0:
+                    raise g5.G5Error(code, "tune")
+                ts.append(bfs.stats.device_ms)
+            v = _hmean_teps(ts, nedges)
+            best = v if best is None else max(best, v)
+        bfs.close()
+        results.append((best, a, b))
+    results.sort(reverse=True)
+    out = {"alpha": results[0][1], "beta": results[0][2], "gteps": results[0][0],
+           "grid": [{"alpha": a, "beta": b, "gteps": round(v, 2)} for v, a, b in results]}
+    _cache[key] = out
+    return out
+
+
+def tune_batch(g5, torch, graphs, roots_per_graph, alphas=ALPHAS, betas=BETAS) -> dict:
+    """Best (alpha, beta) for a batched search over the given graphs and roots."""
+    import numpy as np
+
+    bt = g5.Batch(graphs)
+    total = sum(len(r) * g.n for g, r in zip(graphs, roots_per_graph))
+    out = torch.empty(max(total, 1), dtype=torch.int32, device="cuda")
+    roots = np.concatenate([np.asarray(r, np.int64) for r in roots_per_graph])
+    counts = [len(r) for r in roots_per_graph]
+    results = []
+    for a, b in itertools.product(alphas, betas):
+        bt.set_direction(a, b)
+        bt.run(roots, counts, out)  # builds the graph for these arguments
+        ms = min(bt.run(roots, counts, out) for _ in range(2))
+        results.append((ms, a, b))
+    bt.close()
+    results.sort()
+    return {"alpha": results[0][1], "beta": results[0][2], "ms": results[0][0],
+            "grid": [{"alpha": a, "beta": b, "ms": round(m, 3)} for m, a, b in results]}

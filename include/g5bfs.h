@@ -121,6 +121,8 @@ typedef struct g5_bfs_config {
                             node); 0: host-driven loop, one sync per level       */
     int max_levels;      /* safety cap on levels (G5_ERR_TIMEOUT past it)       */
     int want_levels;     /* keep a per-vertex level array                        */
+    int profile;         /* with use_graph = 0: time every launch with CUDA events
+                            into g5_bfs_stats.kernel_ms                          */
 } g5_bfs_config;
 
 /* Fills the defaults: alpha 14, beta 24, no codec, threshold 64, CUDA graph,
@@ -143,6 +145,8 @@ typedef struct g5_bfs_stats {
     int64_t codec_values;     /* sum of values that went through the codec        */
     int64_t alg_bytes;        /* algorithmic HBM bytes of the search              */
     double device_ms;         /* device time of the search (CUDA events)          */
+    double kernel_ms[8];      /* profile mode: prologue, expand, fixup, count,
+                                 scan, write, codec, unused (ms, summed)          */
 } g5_bfs_stats;
 
 /* One BFS from root: GlobalBFS::runBFS (cpu_2d/globalbfs.hh:548-1263) at 1x1
@@ -156,6 +160,11 @@ typedef struct g5_bfs_stats {
  * receives levels, -1 unvisited.  stats may be NULL. */
 g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_out,
                      g5_bfs_stats *stats);
+
+/* Per-level record of the last search, 4 int64 per level: direction
+ * (0 top-down, 1 bottom-up), frontier vertices, their adjacency entries, and
+ * adjacency entries the expansion read.  *rows = levels written. */
+g5_status g5_bfs_level_log(g5_bfs *b, int64_t *out, int max_rows, int *rows);
 
 /* Device pointer to the workspace's int64 parent array of the last search. */
 g5_status g5_bfs_device_pred(g5_bfs *b, const int64_t **pred);
@@ -183,6 +192,10 @@ typedef struct g5_batch g5_batch;
 /* Workspace for batched searches over a set of graphs (one per slot). */
 g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out);
 g5_status g5_batch_destroy(g5_batch *bt);
+
+/* Direction-switch thresholds of the batched search (defaults 14 and 24),
+ * applied to each graph's union frontier. */
+g5_status g5_batch_set_direction(g5_batch *bt, double alpha, double beta);
 
 /* Runs nroots[i] (<= 64) roots on graph i, all graphs in one level loop.
  * roots holds the roots of graph 0, then graph 1, ...  Parents are written
