@@ -48,7 +48,8 @@ class G5Error(RuntimeError):
 class BfsConfig(C.Structure):
     _fields_ = [("alpha", C.c_double), ("beta", C.c_double), ("codec", C.c_int),
                 ("codec_threshold", C.c_uint32), ("use_graph", C.c_int),
-                ("max_levels", C.c_int), ("want_levels", C.c_int), ("profile", C.c_int)]
+                ("max_levels", C.c_int), ("want_levels", C.c_int), ("profile", C.c_int),
+                ("parent_mode", C.c_int)]
 
 
 class BfsStats(C.Structure):
@@ -85,6 +86,7 @@ SIGNATURES = {
     "g5_bfs_destroy": (_I, [_P]),
     "g5_bfs_run": (_I, [_P, _I64, _P, _P, C.POINTER(BfsStats)]),
     "g5_bfs_level_log": (_I, [_P, _P, _I, C.POINTER(_I)]),
+    "g5_bfs_profile_log": (_I, [_P, _P, _P, _I, C.POINTER(_I)]),
     "g5_bfs_device_pred": (_I, [_P, C.POINTER(_P)]),
     "g5_bfs_teps_edges": (_I, [_P, C.POINTER(_I64)]),
     "g5_bfs_validate": (_I, [_P, _I64, C.POINTER(_I), C.POINTER(_I)]),
@@ -221,12 +223,15 @@ class CudaBFS:
 
     def __init__(self, graph: Graph, codec: int = CODEC_NONE, codec_threshold: int = 64,
                  alpha: float = 14.0, beta: float = 24.0, use_graph: bool = True,
-                 want_levels: bool = False, max_levels: int = 4096, profile: bool = False):
+                 want_levels: bool = False, max_levels: int = 4096, profile: bool = False,
+                 parent_mode: Optional[int] = None):
         self.graph = graph
         cfg = default_config()
         cfg.alpha, cfg.beta, cfg.codec, cfg.codec_threshold = alpha, beta, codec, codec_threshold
         cfg.use_graph, cfg.want_levels, cfg.max_levels = int(use_graph), int(want_levels), max_levels
         cfg.profile = int(profile)
+        if parent_mode is not None:
+            cfg.parent_mode = parent_mode
         self.cfg = cfg
         h = C.c_void_p()
         _check(lib().g5_bfs_create(graph._h, C.byref(cfg), C.byref(h)), "g5_bfs_create")
@@ -258,6 +263,15 @@ class CudaBFS:
         rows = C.c_int()
         _check(lib().g5_bfs_level_log(self._h, _ptr(out), 4096, C.byref(rows)), "g5_bfs_level_log")
         return out[: rows.value].copy()
+
+    def profile_log(self) -> list:
+        """Profile mode: [(kernel kind, ms)] for every launch of the last search."""
+        kinds = np.zeros(65536, np.int32)
+        ms = np.zeros(65536, np.float64)
+        rows = C.c_int()
+        _check(lib().g5_bfs_profile_log(self._h, _ptr(kinds), _ptr(ms), 65536, C.byref(rows)),
+               "g5_bfs_profile_log")
+        return [(BfsStats.KERNELS[k], float(t)) for k, t in zip(kinds[: rows.value], ms[: rows.value])]
 
     def device_pred_ptr(self) -> int:
         p = C.c_void_p()

@@ -7,8 +7,9 @@
 //   expand   top-down (queue, edge-balanced tiles, next-bit atomicOr) or
 //            bottom-up (bitmap sweep, first hit in the sorted adjacency)
 //   fixup    after top-down: parents of the new vertices (first frontier hit)
-//   count    popcount + degree sum of the next-frontier bitmap per chunk
-//   scan     chunk prefix sums, Beamer direction switch, loop condition
+//   count    popcount + degree sum of the next-frontier bitmap per chunk; the
+//            last block to finish does the chunk prefix sums, the Beamer
+//            direction switch and the loop condition
 //   write    visited |= next, next -> front, sorted queue + edge offsets
 //   codec    optional s4-bp128 encode + decode of the sorted queue; the
 //            decoded queue feeds the next top-down level
@@ -65,8 +66,9 @@ struct BfsState {
     uint32_t err;
     int32_t want_queue; // 1 if F_L is also held as a sorted queue
     int32_t bu_levels;
-    int32_t pad;
+    int32_t list_mode;  // 1: this bottom-up level sweeps the unvisited list
     uint64_t codec_acc[2]; // encoded words, values through the codec
+    uint64_t ulen;      // unvisited list length
 };
 
 struct BfsArgs {
@@ -88,6 +90,13 @@ struct BfsArgs {
     int64_t *qbase;       // row_off[u] - qoff[i]
     uint32_t *tile_start; // first queue index of each top-down tile
     const uint32_t *heavy; // one bit per vertex of degree > kHeavy
+    const uint32_t *ro32;  // row offsets as uint32 when nnz < 2^32, else null
+    uint32_t *multi;       // vertices a top-down level reached more than once
+    uint32_t *wdeg;        // per word: degree sum of the vertices bottom-up added
+    unsigned *done;        // blocks of k_count finished (reset by the last one)
+    uint32_t *ulist;       // sorted unvisited vertices for a bottom-up level
+    uint64_t *chunk_u;     // per chunk: unvisited vertices after the level
+    int parent_mode;       // 0 atomicMin, 1 heavy atomicMin + fix-up, 2 first writer + fix-up
     uint64_t max_tiles;
     uint64_t *chunk_n;
     uint64_t *chunk_m;
@@ -133,6 +142,8 @@ __global__ void k_init(BfsArgs a)
         st->want_queue = 1;
         st->bu_levels = 0;
         st->codec_acc[0] = st->codec_acc[1] = 0;
+        st->list_mode = 0;
+        st->ulen = 0;
         a.log[0].dir = DIR_TD;
         a.log[0].nf = st->nf;
         a.log[0].mf = st->mf;
@@ -207,9 +218,22 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
                     const uint32_t v = __ldg(a.col + (a.qbase[i] + (int64_t)e));
                     const uint32_t bit = 1u << (v & 31);
                     if (!(a.visited[v >> 5] & bit)) {
-                        if (__ldg(a.heavy + (v >> 5)) & bit)
-                            atomicMin((unsigned long long *)(a.pred + v), (unsigned long long)a.qsrc[i]);
-                        if (!(a.next[v >> 5] & bit)) atomicOr(a.next + (v >> 5), bit);
+                        const unsigned long long u = a.qsrc[i];
+                        if (a.parent_mode == 0 || (__ldg(a.heavy + (v >> 5)) & bit)) {
+                            // parents only decrease during a level, so a read
+                            // value <= u (even a stale one) makes the atomic moot
+                            if ((unsigned long long)a.pred[v] > u)
+                                atomicMin((unsigned long long *)(a.pred + v), u);
+                            if (!(a.next[v >> 5] & bit)) atomicOr(a.next + (v >> 5), bit);
+                        } else if (a.parent_mode == 1) {
+                            if (!(a.next[v >> 5] & bit)) atomicOr(a.next + (v >> 5), bit);
+                        } else {
+                            // first discoverer writes its parent; a vertex
+                            // reached again is left to the fix-up sweep
+                            const uint32_t old = (a.next[v >> 5] & bit) ? bit : atomicOr(a.next + (v >> 5), bit);
+                            if (!(old & bit)) atomicMin((unsigned long long *)(a.pred + v), u);
+                            else if (!(a.multi[v >> 5] & bit)) atomicOr(a.multi + (v >> 5), bit);
+                        }
                     }
                 }
             }
@@ -226,14 +250,103 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
 // FIXUP (after a top-down level): the candidates are the vertices top-down
 // just discovered; each takes the first frontier neighbour of its adjacency.
 // Either way the parent is the smallest neighbour in the frontier.
-template <bool FIXUP>
+// Warp-collective search of each active lane's adjacency [s, e) for its
+// first vertex in the frontier: every lane scans its first kBuSerial entries
+// alone (four independent loads at a time), then the warp finishes the longer
+// lists one at a time, 32 entries per step (the first set ballot bit is the
+// smallest index).  Returns found / par per lane and the entries read.
+template <typename Off>
+__device__ __forceinline__ void first_hit(const BfsArgs &a, bool mine, Off s, Off e, bool &found,
+                                          uint32_t &par, uint64_t &ex)
+{
+    const int lane = g5_lane();
+    const uint32_t *__restrict__ front = a.front;
+    const uint32_t *__restrict__ col = a.col;
+    found = false;
+    par = 0;
+    Off j = s;
+    const Off lim = min(e, (Off)(s + kBuSerial));
+    while (j < lim && !found) {
+        uint32_t u[4];
+        bool h[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) u[k] = (j + k < lim) ? __ldg(col + j + k) : 0u;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            h[k] = (j + k < lim) && ((__ldg(front + (u[k] >> 5)) >> (u[k] & 31)) & 1u);
+        int k = 0;
+        while (k < 4 && j + k < lim && !h[k]) ++k;
+        if (k < 4 && j + k < lim) {
+            found = true;
+            par = u[k];
+            j += k + 1;
+        } else {
+            j = min((Off)(j + 4), lim);
+        }
+    }
+    ex = mine ? (uint64_t)(j - s) : 0;
+    unsigned pend = __ballot_sync(0xFFFFFFFFu, mine && !found && j < e);
+    while (pend) {
+        const int l = __ffs(pend) - 1;
+        pend &= pend - 1;
+        Off jj = __shfl_sync(0xFFFFFFFFu, j, l);
+        const Off ee = __shfl_sync(0xFFFFFFFFu, e, l);
+        const Off st = jj;
+        bool got = false;
+        uint32_t gpar = 0;
+        while (jj < ee) {
+            const Off idx = jj + (Off)lane;
+            uint32_t u = 0;
+            bool hit = false;
+            if (idx < ee) {
+                u = __ldg(col + idx);
+                hit = (__ldg(front + (u >> 5)) >> (u & 31)) & 1u;
+            }
+            const unsigned m = __ballot_sync(0xFFFFFFFFu, hit);
+            if (m) {
+                const int f = __ffs(m) - 1;
+                gpar = __shfl_sync(0xFFFFFFFFu, u, f);
+                got = true;
+                jj += f + 1;
+                break;
+            }
+            jj += 32;
+        }
+        jj = min(jj, ee);
+        if (lane == l) {
+            found = got;
+            par = gpar;
+            ex += (uint64_t)(jj - st);
+        }
+    }
+}
+
+// Row offsets of v: the uint32 copy when nnz < 2^32 (half the bytes, and
+// 32-bit loop indices), else the int64 array.
+__device__ __forceinline__ void load_offsets(const BfsArgs &a, uint64_t v, uint32_t &s, uint32_t &e)
+{
+    s = a.ro32[v];
+    e = a.ro32[v + 1];
+}
+__device__ __forceinline__ void load_offsets(const BfsArgs &a, uint64_t v, int64_t &s, int64_t &e)
+{
+    s = a.row_off[v];
+    e = a.row_off[v + 1];
+}
+
+// One warp per 32-vertex word.  BOTTOM-UP: the candidates are the unvisited
+// vertices; a candidate with a neighbour in the frontier joins the next
+// frontier with the first such neighbour of its ascending adjacency as
+// parent (kept for reference; bottom-up levels normally sweep the unvisited
+// list, bottom_up_list).  FIXUP (after a top-down level, parent modes 1 and
+// 2): the candidates are vertices top-down just discovered; each takes the
+// first frontier neighbour of its adjacency.
+template <bool FIXUP, typename Off>
 __device__ void sweep(const BfsArgs &a, uint64_t &examined)
 {
     const int lane = g5_lane();
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const uint32_t *__restrict__ front = a.front;
-    const uint32_t *__restrict__ col = a.col;
     // FIXUP candidates are sparse: a warp loads 32 words at once (one per
     // lane, coalesced) and visits only the non-empty ones.  Bottom-up
     // candidates are dense: one word per warp step keeps more words in flight.
@@ -243,7 +356,14 @@ __device__ void sweep(const BfsArgs &a, uint64_t &examined)
       unsigned act;
       if (FIXUP) {
           const uint64_t wl = w0 + lane;
-          if (wl < a.nwords) cw = a.next[wl] & ~__ldg(a.heavy + wl);
+          if (wl < a.nwords) {
+              if (a.parent_mode == 2) {
+                  cw = a.multi[wl] & ~__ldg(a.heavy + wl);
+                  if (cw) a.multi[wl] = 0;
+              } else {
+                  cw = a.parent_mode == 1 ? (a.next[wl] & ~__ldg(a.heavy + wl)) : 0u;
+              }
+          }
           act = __ballot_sync(0xFFFFFFFFu, cw != 0u);
       } else {
           cw = ~a.visited[w0];
@@ -256,87 +376,64 @@ __device__ void sweep(const BfsArgs &a, uint64_t &examined)
         const uint32_t cand_word = FIXUP ? __shfl_sync(0xFFFFFFFFu, cw, jw) : cw;
         const uint64_t v = w * 32 + lane;
         const bool mine = (cand_word >> lane) & 1u;
-        int64_t s = 0, e = 0;
-        if (mine) {
-            s = a.row_off[v];
-            e = a.row_off[v + 1];
-        }
-        bool found = false;
-        uint32_t par = 0;
-        int64_t j = s;
-        // first entries per lane, four independent loads at a time
-        const int64_t lim = min(e, s + kBuSerial);
-        while (j < lim && !found) {
-            uint32_t u[4];
-            bool h[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) u[k] = (j + k < lim) ? __ldg(col + j + k) : 0u;
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                h[k] = (j + k < lim) && ((__ldg(front + (u[k] >> 5)) >> (u[k] & 31)) & 1u);
-            int k = 0;
-            while (k < 4 && j + k < lim && !h[k]) ++k;
-            if (k < 4 && j + k < lim) {
-                found = true;
-                par = u[k];
-                j += k + 1;
-            } else {
-                j = min(j + 4, lim);
-            }
-        }
-        uint64_t ex = (uint64_t)(j - s);
-        unsigned pend = __ballot_sync(0xFFFFFFFFu, mine && !found && j < e);
-        while (pend) {
-            const int l = __ffs(pend) - 1;
-            pend &= pend - 1;
-            int64_t jj = __shfl_sync(0xFFFFFFFFu, j, l);
-            const int64_t ee = __shfl_sync(0xFFFFFFFFu, e, l);
-            const int64_t st = jj;
-            bool got = false;
-            uint32_t gpar = 0;
-            while (jj < ee) {
-                const int64_t idx = jj + lane;
-                uint32_t u = 0;
-                bool hit = false;
-                if (idx < ee) {
-                    u = __ldg(col + idx);
-                    hit = (__ldg(front + (u >> 5)) >> (u & 31)) & 1u;
-                }
-                const unsigned m = __ballot_sync(0xFFFFFFFFu, hit);
-                if (m) {
-                    const int f = __ffs(m) - 1;
-                    gpar = __shfl_sync(0xFFFFFFFFu, u, f);
-                    got = true;
-                    jj += f + 1;
-                    break;
-                }
-                jj += 32;
-            }
-            jj = min(jj, ee);
-            if (lane == l) {
-                found = got;
-                par = gpar;
-                ex += (uint64_t)(jj - st);
-            }
-        }
+        Off s = 0, e = 0;
+        if (mine) load_offsets(a, v, s, e);
+        bool found;
+        uint32_t par;
+        uint64_t ex;
+        first_hit<Off>(a, mine, s, e, found, par, ex);
         if (found) a.pred[v] = (int64_t)par;
         if (FIXUP) {
             if (mine && !found) atomicOr(&a.st->err, G5_DEVERR_CAPACITY);  // cannot happen on a symmetric CSR
         } else {
             const unsigned fm = __ballot_sync(0xFFFFFFFFu, found);
-            if (lane == 0 && fm) a.next[w] = fm;
+            if (fm) {
+                // degree sum of the added vertices: the counting pass after a
+                // bottom-up level then reads one word per 32 vertices
+                uint32_t dsum = found ? (uint32_t)(e - s) : 0u;
+#pragma unroll
+                for (int o = 16; o; o >>= 1) dsum += __shfl_xor_sync(0xFFFFFFFFu, dsum, o);
+                if (lane == 0) {
+                    a.next[w] = fm;
+                    a.wdeg[w] = dsum;
+                }
+            }
         }
         examined += ex;
       }
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_expand(BfsArgs a)
+// Bottom-up level over the sorted list of unvisited vertices (written by the
+// previous level's compaction): 32 candidates per warp step, every lane
+// busy, instead of sweeping all words of which many hold no candidate.
+template <typename Off>
+__device__ void bottom_up_list(const BfsArgs &a, uint64_t &examined)
 {
-    uint64_t examined = 0;
-    if (a.st->err) return;
-    if (a.st->dir == DIR_TD) expand_td(a, examined);
-    else sweep<false>(a, examined);
+    const int lane = g5_lane();
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t len = a.st->ulen;
+    const uint32_t *__restrict__ list = a.ulist;
+    for (uint64_t b0 = gw * 32; b0 < len; b0 += nw * 32) {
+        const bool mine = b0 + lane < len;
+        const uint32_t v = mine ? list[b0 + lane] : 0u;
+        Off s = 0, e = 0;
+        if (mine) load_offsets(a, v, s, e);
+        bool found;
+        uint32_t par;
+        uint64_t ex;
+        first_hit<Off>(a, mine, s, e, found, par, ex);
+        if (found) {
+            a.pred[v] = (int64_t)par;
+            atomicOr(a.next + (v >> 5), 1u << (v & 31));
+        }
+        examined += ex;
+    }
+}
+
+__device__ __forceinline__ void add_examined(const BfsArgs &a, uint64_t examined)
+{
     examined = warp_sum_u64(examined);
     __shared__ uint64_t s_ex[kWarps];
     if (g5_lane() == 0) s_ex[threadIdx.x >> 5] = examined;
@@ -348,12 +445,34 @@ __global__ void __launch_bounds__(kBlock) k_expand(BfsArgs a)
     }
 }
 
-// Parents of the vertices a top-down level discovered (no-op after bottom-up).
-__global__ void __launch_bounds__(kBlock) k_fixup(BfsArgs a)
+// Top-down expansion of the level (no-op when the level is bottom-up).
+__global__ void __launch_bounds__(kBlock, 8) k_td(BfsArgs a)
 {
     if (a.st->err || a.st->dir != DIR_TD) return;
     uint64_t examined = 0;
-    sweep<true>(a, examined);
+    expand_td(a, examined);
+    add_examined(a, examined);
+}
+
+// Bottom-up expansion of the level (no-op when the level is top-down): the
+// word sweep for the first bottom-up level, the unvisited list afterwards.
+template <typename Off>
+__global__ void __launch_bounds__(kBlock, 8) k_bu(BfsArgs a)
+{
+    if (a.st->err || a.st->dir != DIR_BU) return;
+    uint64_t examined = 0;
+    if (a.st->list_mode) bottom_up_list<Off>(a, examined);
+    else sweep<false, Off>(a, examined);
+    add_examined(a, examined);
+}
+
+// Parents of the vertices a top-down level discovered (no-op after bottom-up).
+__global__ void __launch_bounds__(kBlock) k_fixup(BfsArgs a)
+{
+    if (a.st->err || a.st->dir != DIR_TD || a.parent_mode == 0) return;
+    uint64_t examined = 0;
+    if (a.ro32) sweep<true, uint32_t>(a, examined);
+    else sweep<true, int64_t>(a, examined);
     examined = warp_sum_u64(examined);
     __shared__ uint64_t s_ex[kWarps];
     if (g5_lane() == 0) s_ex[threadIdx.x >> 5] = examined;
@@ -398,15 +517,23 @@ __device__ __forceinline__ void warp_chunk_counts(const BfsArgs &a, uint64_t wbe
 // popcounts and the degrees of their set vertices (independent loads per
 // thread; faster here than the lane-parallel walk of k_write).
 
+__device__ void scan_and_decide(const BfsArgs &a);
+
 __global__ void __launch_bounds__(kBlock) k_count(BfsArgs a)
 {
     const uint32_t c = blockIdx.x;
     const uint64_t w0 = (uint64_t)c * kChunkWords + (uint64_t)threadIdx.x * kWordsPerThread;
-    uint64_t cn = 0, cm = 0;
+    const bool bu = a.st->dir == DIR_BU && !a.st->list_mode;  // word sweep: degree sums present
+    uint64_t cn = 0, cm = 0, cu = 0;
 #pragma unroll
     for (int k = 0; k < kWordsPerThread; ++k) {
         uint32_t x = (w0 + k < a.nwords) ? a.next[w0 + k] : 0u;
+        if (a.st->dir == DIR_BU && w0 + k < a.nwords) cu += __popc(~(a.visited[w0 + k] | x));
         cn += __popc(x);
+        if (bu) {
+            if (x) cm += a.wdeg[w0 + k];
+            continue;
+        }
         while (x) {
             const int b = __ffs(x) - 1;
             x &= x - 1;
@@ -415,27 +542,43 @@ __global__ void __launch_bounds__(kBlock) k_count(BfsArgs a)
     }
     cn = warp_sum_u64(cn);
     cm = warp_sum_u64(cm);
-    __shared__ uint64_t s_n[kWarps], s_m[kWarps];
+    cu = warp_sum_u64(cu);
+    __shared__ uint64_t s_n[kWarps], s_m[kWarps], s_u[kWarps];
     if (g5_lane() == 0) {
         s_n[threadIdx.x >> 5] = cn;
         s_m[threadIdx.x >> 5] = cm;
+        s_u[threadIdx.x >> 5] = cu;
     }
     __syncthreads();
+    __shared__ unsigned s_last;
     if (threadIdx.x == 0) {
-        uint64_t tn = 0, tm = 0;
+        uint64_t tn = 0, tm = 0, tu = 0;
         for (int i = 0; i < kWarps; ++i) {
             tn += s_n[i];
             tm += s_m[i];
+            tu += s_u[i];
         }
         a.chunk_n[c] = tn;
         a.chunk_m[c] = tm;
+        a.chunk_u[c] = tu;
+        __threadfence();
+        s_last = atomicAdd(a.done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+        // every other block has published its counts
+        __threadfence();
+        scan_and_decide(a);
+        if (threadIdx.x == 0) *a.done = 0;
     }
 }
 
-// Block-wide exclusive scan of one u64 per thread (1024 threads).
+// Block-wide exclusive scan of one u64 per thread (blockDim.x a multiple of
+// 32, at most 1024); s_warp holds 33 entries.
 __device__ uint64_t block_excl_scan_1024(uint64_t v, uint64_t *s_warp, uint64_t &total)
 {
     const int lane = g5_lane(), wid = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
     uint64_t x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -445,7 +588,7 @@ __device__ uint64_t block_excl_scan_1024(uint64_t v, uint64_t *s_warp, uint64_t 
     if (lane == 31) s_warp[wid] = x;
     __syncthreads();
     if (wid == 0) {
-        uint64_t y = s_warp[lane];
+        uint64_t y = lane < nwarps ? s_warp[lane] : 0;
         uint64_t z = y;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -462,26 +605,33 @@ __device__ uint64_t block_excl_scan_1024(uint64_t v, uint64_t *s_warp, uint64_t 
     return r;
 }
 
-__global__ void __launch_bounds__(1024) k_scan(BfsArgs a)
+// Chunk prefix sums, the direction switch and the loop condition; run by
+// the last block of k_count to finish (it sees every chunk's count).
+__device__ void scan_and_decide(const BfsArgs &a)
 {
     __shared__ uint64_t s_w[33];
     const uint32_t C = a.nchunks;
-    const uint32_t per = (C + 1023) / 1024;
+    const uint32_t per = (C + blockDim.x - 1) / blockDim.x;
     const uint32_t b0 = threadIdx.x * per;
-    uint64_t ln = 0, lm = 0;
+    uint64_t ln = 0, lm = 0, lu = 0;
     for (uint32_t i = 0; i < per && b0 + i < C; ++i) {
-        ln += a.chunk_n[b0 + i];
-        lm += a.chunk_m[b0 + i];
+        ln += __ldcg(a.chunk_n + b0 + i);
+        lm += __ldcg(a.chunk_m + b0 + i);
+        lu += __ldcg(a.chunk_u + b0 + i);
     }
-    uint64_t tn, tm;
+    uint64_t tn, tm, tu;
     uint64_t on = block_excl_scan_1024(ln, s_w, tn);
     uint64_t om = block_excl_scan_1024(lm, s_w, tm);
+    uint64_t ou = block_excl_scan_1024(lu, s_w, tu);
     for (uint32_t i = 0; i < per && b0 + i < C; ++i) {
-        const uint64_t xn = a.chunk_n[b0 + i], xm = a.chunk_m[b0 + i];
+        const uint64_t xn = __ldcg(a.chunk_n + b0 + i), xm = __ldcg(a.chunk_m + b0 + i);
+        const uint64_t xu = __ldcg(a.chunk_u + b0 + i);
         a.chunk_n[b0 + i] = on;
         a.chunk_m[b0 + i] = om;
+        a.chunk_u[b0 + i] = ou;
         on += xn;
         om += xm;
+        ou += xu;
     }
     if (threadIdx.x == 0) {
         BfsState *st = a.st;
@@ -495,6 +645,10 @@ __global__ void __launch_bounds__(1024) k_scan(BfsArgs a)
             if ((double)tn < (double)a.n / a.beta && tn < st->nf) nd = DIR_TD;
         }
         const bool want_q = (nd == DIR_TD) || a.codec != 0;
+        // a bottom-up level right after another one sweeps the unvisited
+        // list k_write is about to write; the first one sweeps the words
+        st->list_mode = (st->dir == DIR_BU && nd == DIR_BU) ? 1 : 0;
+        st->ulen = tu;
         st->level = L + 1;
         st->dir = nd;
         st->nf = tn;
@@ -528,30 +682,55 @@ __global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
     const uint64_t wbeg = (uint64_t)c * kChunkWords + (uint64_t)wid * kWordsPerWarp;
     const int32_t L = a.st->level;  // index of the new frontier
     const bool want_q = a.st->want_queue != 0;
+    const bool want_u = a.st->list_mode != 0;  // next level is bottom-up
     // per-warp totals, then the warp's offsets inside the chunk
-    uint64_t cn = 0, cm = 0;
+    uint64_t cn = 0, cm = 0, cu = 0;
     if (want_q || a.level) warp_chunk_counts(a, wbeg, cn, cm);
-    __shared__ uint64_t s_n[kWarps], s_m[kWarps];
+    if (want_u) {
+        for (int g = 0; g < kWordsPerWarp; g += 32) {
+            const uint64_t wl = wbeg + g + lane;
+            if (wl < a.nwords) cu += __popc(~(a.visited[wl] | a.next[wl]));
+        }
+        cu = warp_sum_u64(cu);
+    }
+    __shared__ uint64_t s_n[kWarps], s_m[kWarps], s_u[kWarps];
     if (lane == 0) {
         s_n[wid] = cn;
         s_m[wid] = cm;
+        s_u[wid] = cu;
     }
     __syncthreads();
-    uint64_t pos = a.chunk_n[c], mpos = a.chunk_m[c];
+    uint64_t pos = a.chunk_n[c], mpos = a.chunk_m[c], upos = a.chunk_u[c];
     for (int i = 0; i < wid; ++i) {
         pos += s_n[i];
         mpos += s_m[i];
+        upos += s_u[i];
     }
     for (int g = 0; g < kWordsPerWarp; g += 32) {
         const uint64_t wl = wbeg + g + lane;
-        uint32_t x = 0;
+        uint32_t x = 0, unv = 0;
         if (wl < a.nwords) {
             x = a.next[wl];
+            const uint32_t vis = a.visited[wl] | x;
             if (x) {
-                a.visited[wl] |= x;
+                a.visited[wl] = vis;
                 a.next[wl] = 0;
             }
             a.front[wl] = x;
+            unv = ~vis;
+        }
+        if (want_u) {
+            // unvisited vertices of these 32 words, in order: one word at a
+            // time across the warp so the list writes are coalesced
+            unsigned uact = __ballot_sync(0xFFFFFFFFu, unv != 0u);
+            while (uact) {
+                const int j = __ffs(uact) - 1;
+                uact &= uact - 1;
+                const uint32_t uj = __shfl_sync(0xFFFFFFFFu, unv, j);
+                if ((uj >> lane) & 1u)
+                    a.ulist[upos + __popc(uj & g5_lanemask_lt())] = (uint32_t)((wbeg + g + j) * 32 + lane);
+                upos += __popc(uj);
+            }
         }
         if (!want_q && !a.level) continue;
         unsigned act = __ballot_sync(0xFFFFFFFFu, x != 0u);
@@ -741,6 +920,11 @@ struct g5_bfs {
     uint32_t *bitmaps = nullptr;  // visited | front | next
     uint32_t *isolated = nullptr; // one bit per vertex of degree 0
     uint32_t *heavy = nullptr;    // one bit per vertex of degree > kHeavy
+    uint32_t *ro32 = nullptr;     // uint32 copy of the row offsets (nnz < 2^32)
+    uint32_t *multi = nullptr;    // reached more than once in a top-down level
+    uint32_t *wdeg = nullptr;     // per-word degree sums written by bottom-up
+    uint32_t *ulist = nullptr;    // sorted unvisited vertices (n entries)
+    unsigned *done = nullptr;     // k_count's finished-block counter
     int64_t *pred = nullptr;
     int32_t *level = nullptr;
     uint32_t *queue = nullptr;
@@ -785,13 +969,13 @@ void enqueue_level(g5_bfs *b, const BfsArgs &a, cudaStream_t s, Prof *pf = nullp
     Prof dummy;
     Prof &p = pf ? *pf : dummy;
     p.mark(KP_EXPAND, s);
-    k_expand<<<g5::grid_for(8), kBlock, 0, s>>>(a);
+    k_td<<<g5::grid_for(8), kBlock, 0, s>>>(a);
+    if (a.ro32) k_bu<uint32_t><<<g5::grid_for(8), kBlock, 0, s>>>(a);
+    else k_bu<int64_t><<<g5::grid_for(8), kBlock, 0, s>>>(a);
     p.mark(KP_FIXUP, s);
-    k_fixup<<<g5::grid_for(8), kBlock, 0, s>>>(a);
+    if (a.parent_mode != 0) k_fixup<<<g5::grid_for(8), kBlock, 0, s>>>(a);
     p.mark(KP_COUNT, s);
     k_count<<<a.nchunks, kBlock, 0, s>>>(a);
-    p.mark(KP_SCAN, s);
-    k_scan<<<1, 1024, 0, s>>>(a);
     p.mark(KP_WRITE, s);
     k_write<<<a.nchunks, kBlock, 0, s>>>(a);
     p.mark(KP_CODEC, s);
@@ -854,13 +1038,20 @@ g5_status alloc_ws(g5_bfs *b)
     G5_CUDA(cudaMalloc(&b->bitmaps, sizeof(uint32_t) * 3 * a.nwords));
     G5_CUDA(cudaMalloc(&b->isolated, sizeof(uint32_t) * a.nwords));
     G5_CUDA(cudaMalloc(&b->heavy, sizeof(uint32_t) * a.nwords));
+    if (g->nnz < ((int64_t)1 << 32)) G5_CUDA(cudaMalloc(&b->ro32, sizeof(uint32_t) * (size_t)(n + 1)));
+    G5_CUDA(cudaMalloc(&b->multi, sizeof(uint32_t) * a.nwords));
+    G5_CUDA(cudaMalloc(&b->wdeg, sizeof(uint32_t) * a.nwords));
+    G5_CUDA(cudaMalloc(&b->ulist, sizeof(uint32_t) * (size_t)n + 16));
+    G5_CUDA(cudaMalloc(&b->done, sizeof(unsigned)));
+    G5_CUDA(cudaMemset(b->done, 0, sizeof(unsigned)));
+    G5_CUDA(cudaMemset(b->multi, 0, sizeof(uint32_t) * a.nwords));
     G5_CUDA(cudaMalloc(&b->pred, sizeof(int64_t) * (size_t)n));
     if (b->cfg.want_levels) G5_CUDA(cudaMalloc(&b->level, sizeof(int32_t) * (size_t)n));
     G5_CUDA(cudaMalloc(&b->queue, sizeof(uint32_t) * (size_t)n + 16));
     G5_CUDA(cudaMalloc(&b->qoff, sizeof(uint64_t) * (size_t)(n + 1)));
     G5_CUDA(cudaMalloc(&b->qbase, sizeof(int64_t) * (size_t)n));
     G5_CUDA(cudaMalloc(&b->tile_start, sizeof(uint32_t) * a.max_tiles));
-    G5_CUDA(cudaMalloc(&b->chunks, sizeof(uint64_t) * 2 * a.nchunks));
+    G5_CUDA(cudaMalloc(&b->chunks, sizeof(uint64_t) * 3 * a.nchunks));
     G5_CUDA(cudaMalloc(&b->st, sizeof(BfsState)));
     G5_CUDA(cudaMalloc(&b->log, sizeof(LevelRec) * (size_t)b->cfg.max_levels));
     G5_CUDA(cudaMalloc(&b->root_dev, sizeof(int64_t)));
@@ -886,8 +1077,15 @@ g5_status alloc_ws(g5_bfs *b)
     a.qbase = b->qbase;
     a.tile_start = b->tile_start;
     a.heavy = b->heavy;
+    a.ro32 = b->ro32;
+    a.multi = b->multi;
+    a.wdeg = b->wdeg;
+    a.ulist = b->ulist;
+    a.done = b->done;
+    a.parent_mode = b->cfg.parent_mode;
     a.chunk_n = b->chunks;
     a.chunk_m = b->chunks + a.nchunks;
+    a.chunk_u = b->chunks + 2 * a.nchunks;
     a.st = b->st;
     a.log = b->log;
     a.root_dev = b->root_dev;
@@ -900,10 +1098,14 @@ g5_status alloc_ws(g5_bfs *b)
 }
 
 __global__ void k_degrees(const int64_t *__restrict__ ro, int64_t n, uint32_t *__restrict__ d,
-                          uint32_t *__restrict__ iso, uint32_t *__restrict__ heavy)
+                          uint32_t *__restrict__ iso, uint32_t *__restrict__ heavy, uint32_t *__restrict__ ro32)
 {
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < ((n + 31) & ~(int64_t)31);
          v += (int64_t)gridDim.x * blockDim.x) {
+        if (ro32 && v < n) {
+            ro32[v] = (uint32_t)ro[v];  // ro32[n] is written by thread 0
+            if (v == 0) ro32[n] = (uint32_t)ro[n];
+        }
         const uint32_t dv = v < n ? (uint32_t)(ro[v + 1] - ro[v]) : 0u;
         if (v < n) d[v] = dv;
         const unsigned m = __ballot_sync(0xFFFFFFFFu, dv == 0 && v < n);
@@ -923,6 +1125,11 @@ void free_ws(g5_bfs *b)
     cudaFree(b->bitmaps);
     cudaFree(b->isolated);
     cudaFree(b->heavy);
+    cudaFree(b->ro32);
+    cudaFree(b->multi);
+    cudaFree(b->wdeg);
+    cudaFree(b->ulist);
+    cudaFree(b->done);
     cudaFree(b->pred);
     cudaFree(b->level);
     cudaFree(b->queue);
@@ -977,6 +1184,7 @@ void g5_bfs_config_default(g5_bfs_config *cfg)
     cfg->max_levels = 4096;
     cfg->want_levels = 0;
     cfg->profile = 0;
+    cfg->parent_mode = 0;
 }
 
 g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
@@ -988,7 +1196,8 @@ g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
     if (cfg) b->cfg = *cfg;
     else g5_bfs_config_default(&b->cfg);
     if (b->cfg.max_levels < 2) b->cfg.max_levels = 2;
-    if (b->cfg.codec < 0 || b->cfg.codec > 2 || b->cfg.alpha <= 0 || b->cfg.beta <= 0) {
+    if (b->cfg.codec < 0 || b->cfg.codec > 2 || b->cfg.alpha <= 0 || b->cfg.beta <= 0 ||
+        b->cfg.parent_mode < 0 || b->cfg.parent_mode > 2) {
         delete b;
         return G5_ERR_INVALID_ARG;
     }
@@ -1002,7 +1211,8 @@ g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
     cudaEventCreate(&b->ev0);
     cudaEventCreate(&b->ev1);
     if ((st = alloc_ws(b)) != G5_OK) return fail(st);
-    k_degrees<<<g5::grid_for(8), kBlock, 0, b->stream>>>(g->row_off, g->n, b->deg, b->isolated, b->heavy);
+    k_degrees<<<g5::grid_for(8), kBlock, 0, b->stream>>>(g->row_off, g->n, b->deg, b->isolated, b->heavy,
+                                                          b->ro32);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
     if (b->cfg.use_graph && (st = build_graph(b)) != G5_OK) return fail(st);
     *out = b;
@@ -1104,6 +1314,20 @@ g5_status g5_bfs_level_log(g5_bfs *b, int64_t *out, int max_rows, int *rows)
         out[4 * L + 3] = (int64_t)b->h_log[L].examined;
     }
     *rows = nlev;
+    return G5_OK;
+}
+
+g5_status g5_bfs_profile_log(g5_bfs *b, int32_t *kinds, double *ms, int max_rows, int *rows)
+{
+    if (!b || !kinds || !ms || !rows || max_rows < 1) return G5_ERR_INVALID_ARG;
+    int k = 0;
+    for (size_t i = 0; i < b->prof.used && k < max_rows; ++i, ++k) {
+        float t = 0;
+        cudaEventElapsedTime(&t, b->prof.ev[i], i + 1 < b->prof.used ? b->prof.ev[i + 1] : b->ev1);
+        kinds[k] = b->prof.kind[i];
+        ms[k] = t;
+    }
+    *rows = k;
     return G5_OK;
 }
 

@@ -123,10 +123,15 @@ typedef struct g5_bfs_config {
     int want_levels;     /* keep a per-vertex level array                        */
     int profile;         /* with use_graph = 0: time every launch with CUDA events
                             into g5_bfs_stats.kernel_ms                          */
+    int parent_mode;     /* how a top-down level finds parents (same result):
+                            0 atomicMin per edge; 1 atomicMin for vertices of
+                            degree > 64, a scan of the adjacency for the rest;
+                            2 as 1, but the first discoverer's atomicMin stands
+                            unless the vertex is reached twice               */
 } g5_bfs_config;
 
 /* Fills the defaults: alpha 14, beta 24, no codec, threshold 64, CUDA graph,
- * 4096 levels, no level array. */
+ * 4096 levels, no level array, no profiling, parent_mode 0. */
 void g5_bfs_config_default(g5_bfs_config *cfg);
 
 /* Per-search workspace on one graph; not thread safe (one per host thread),
@@ -165,6 +170,10 @@ g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_
  * (0 top-down, 1 bottom-up), frontier vertices, their adjacency entries, and
  * adjacency entries the expansion read.  *rows = levels written. */
 g5_status g5_bfs_level_log(g5_bfs *b, int64_t *out, int max_rows, int *rows);
+
+/* Profile mode: per launch of the last search, the kernel kind (index into
+ * g5_bfs_stats.kernel_ms) and its CUDA-event time in ms. */
+g5_status g5_bfs_profile_log(g5_bfs *b, int32_t *kinds, double *ms, int max_rows, int *rows);
 
 /* Device pointer to the workspace's int64 parent array of the last search. */
 g5_status g5_bfs_device_pred(g5_bfs *b, const int64_t **pred);

@@ -71,6 +71,16 @@ def test_direction_extremes():
         run_all_roots(ro, col, roots, alpha=alpha, beta=beta)
 
 
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_parent_modes_agree(mode):
+    """The three top-down parent strategies give the same (reference) parents."""
+    e = orc.kronecker(13)
+    ro, col = orc.build_csr(1 << 13, e)
+    roots = orc.select_roots(ro, 6)
+    for alpha in (14.0, 1e9):
+        run_all_roots(ro, col, roots, parent_mode=mode, alpha=alpha)
+
+
 def test_gpu_generator_and_csr_match_oracle():
     for scale in (6, 10, 13):
         g = g5.Graph.kronecker(scale)
