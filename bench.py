@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="keep Beamer's alpha=14, beta=24")
     ap.add_argument("--alpha", type=float, default=None)
     ap.add_argument("--beta", type=float, default=None)
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="only the batched search, host-driven with per-kernel CUDA events (for ncu)")
     ap.add_argument("--host-loop", action="store_true",
                     help="host-driven level loop (same kernels, one launch each; for ncu, which "
                          "cannot profile kernels inside graphs with conditional nodes)")
@@ -265,6 +267,13 @@ def main():
     gen_s = time.time() - t0
     roots = g5.select_roots(g, args.roots)
     nr = len(roots)
+    if args.profile_batch:
+        bt = g5.Batch([g])
+        out = torch.empty(nr * g.n, dtype=torch.int32, device="cuda")
+        bt.run(roots, [nr], out)
+        prof = bt.profile(roots, [nr], out)
+        print(json.dumps({"profile_batch": prof, "scale": args.scale, "roots": nr}))
+        return 0
     # Graph500 edge counts (untimed)
     probe = g5.CudaBFS(g)
     nedges = []

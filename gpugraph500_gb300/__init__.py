@@ -93,6 +93,7 @@ SIGNATURES = {
     "g5_batch_create": (_I, [_P, _I, C.POINTER(_P)]),
     "g5_batch_destroy": (_I, [_P]),
     "g5_batch_set_direction": (_I, [_P, C.c_double, C.c_double]),
+    "g5_batch_profile": (_I, [_P, _P, _P, _P, _P, _P, _I, C.POINTER(_I)]),
     "g5_batch_run": (_I, [_P, _P, _P, _P, C.POINTER(C.c_double)]),
     "g5_codec_bound": (_SZ, [_SZ]),
     "g5_codec_create": (_I, [_SZ, C.POINTER(_P)]),
@@ -405,6 +406,18 @@ class Batch:
         h = C.c_void_p()
         _check(lib().g5_batch_create(arr, len(self.graphs), C.byref(h)), "g5_batch_create")
         self._h = h
+
+    def profile(self, roots: np.ndarray, nroots: Sequence[int], pred_out_dev) -> dict:
+        """Host-driven run with per-kernel CUDA-event totals and active vertices per level."""
+        roots = np.ascontiguousarray(roots, dtype=np.int64)
+        nr = np.ascontiguousarray(nroots, dtype=np.int32)
+        ms = np.zeros(5, np.float64)
+        act = np.zeros(1024, np.int64)
+        lv = C.c_int()
+        _check(lib().g5_batch_profile(self._h, _ptr(roots), _ptr(nr), _ptr(pred_out_dev), _ptr(ms), _ptr(act),
+                                      1024, C.byref(lv)), "g5_batch_profile")
+        return {"kernel_ms": dict(zip(("count", "scan", "write", "expand", "fixup"), ms.tolist())),
+                "active": act[: lv.value].tolist()}
 
     def set_direction(self, alpha: float, beta: float) -> None:
         _check(lib().g5_batch_set_direction(self._h, alpha, beta), "g5_batch_set_direction")

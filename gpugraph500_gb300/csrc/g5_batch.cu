@@ -12,9 +12,8 @@
 // (Beamer's alpha/beta on the union frontier):
 //   top-down   edge-balanced tiles over the active-vertex queue; for an edge
 //              (u, v) the roots new to v, front[u] & ~visited[v], are OR-ed
-//              into next[v] (L2 atomics only); a fix-up sweep then gives each
-//              new (vertex, root) pair the first frontier hit of the vertex's
-//              ascending adjacency as parent
+//              into next[v] and each such root's parent slot takes an
+//              atomicMin with u (skipped when the slot is already <= u)
 //   bottom-up  each vertex not yet visited by every root scans its ascending
 //              adjacency: hit = front[u] & still-needed roots; the first hit
 //              of a root is its parent; the scan stops once no root is needed
@@ -57,6 +56,8 @@ struct GraphDesc {
     uint64_t nf, mf;     // active vertices and their adjacency entries
     uint64_t mu;         // adjacency entries of not fully visited vertices
     uint64_t examined;
+    uint64_t amask;      // roots whose frontier is not empty (this level)
+    uint64_t amask_next; // being collected by k_bwrite for the next level
 };
 
 struct BState {
@@ -75,6 +76,7 @@ struct BArgs {
     uint64_t ntot;          // padded global vertex count
     const uint32_t *deg;    // per global vertex
     const uint32_t *heavy;  // one bit per global vertex of degree > 64
+    const uint32_t *iso;    // one bit per global vertex of degree 0
     uint64_t *vis, *front, *next;
     uint32_t *pred;         // output parents, root-major per graph
     uint32_t *queue;
@@ -120,6 +122,8 @@ __global__ void k_binit(BArgs a)
             d.dir = TD;
             d.mu = (uint64_t)d.nnz;
             d.examined = 0;
+            d.amask = 0;
+            d.amask_next = 0;
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -171,14 +175,13 @@ __device__ void bexp_td(const BArgs &a, uint64_t &examined)
                     // (degree > 64) by atomicMin here
                     const uint64_t nb = a.front[ug] & ~a.vis[vg];
                     if (nb) {
-                        if ((__ldg(a.heavy + (vg >> 5)) >> (vg & 31)) & 1u) {
-                            const uint32_t ul = (uint32_t)(ug - d.vbase);
-                            uint64_t x = nb;
-                            while (x) {
-                                const int r = __ffsll((long long)x) - 1;
-                                x &= x - 1;
-                                atomicMin(a.pred + d.pred_base + (uint64_t)r * d.n + vl, ul);
-                            }
+                        const uint32_t ul = (uint32_t)(ug - d.vbase);
+                        uint64_t x = nb;
+                        while (x) {
+                            const int r = __ffsll((long long)x) - 1;
+                            x &= x - 1;
+                            uint32_t *slot = a.pred + d.pred_base + (uint64_t)r * d.n + vl;
+                            if (*slot > ul) atomicMin(slot, ul);
                         }
                         if (nb & ~a.next[vg]) atomicOr((unsigned long long *)&a.next[vg], (unsigned long long)nb);
                     }
@@ -208,7 +211,10 @@ __device__ void bsweep(const BArgs &a, uint64_t &examined)
         if (d.dir != (FIXUP ? TD : BU) || d.nf == 0) continue;
         const uint64_t vl = v - d.vbase;
         const bool light = !((__ldg(a.heavy + (v >> 5)) >> lane) & 1u);
-        uint64_t need = ((int64_t)vl < d.n) ? (FIXUP ? (light ? a.next[v] : 0ull) : (~a.vis[v] & d.mask)) : 0;
+        const bool iso = (__ldg(a.iso + (v >> 5)) >> lane) & 1u;
+        // roots with an empty frontier cannot reach v this level; vertices
+        // without edges are never reached
+        uint64_t need = ((int64_t)vl < d.n && !iso) ? (FIXUP ? (light ? a.next[v] : 0ull) : (~a.vis[v] & d.amask)) : 0;
         int64_t s = 0, e = 0;
         if (need) {
             s = d.row_off[vl];
@@ -290,14 +296,20 @@ __device__ void bsweep(const BArgs &a, uint64_t &examined)
     }
 }
 
-__global__ void __launch_bounds__(kB) k_bexp(BArgs a)
+// Top-down part of a level (graphs expanding top-down) and bottom-up part
+// (graphs expanding bottom-up): two kernels so each gets its own registers.
+__global__ void __launch_bounds__(kB, 8) k_btd(BArgs a)
+{
+    if (a.st->err || a.st->level < 0 || a.st->active == 0 || a.st->qedges == 0) return;
+    uint64_t ex = 0;
+    bexp_td(a, ex);
+}
+
+__global__ void __launch_bounds__(kB, 6) k_bbu(BArgs a)
 {
     if (a.st->err || a.st->level < 0 || a.st->active == 0) return;
-    uint64_t ex_td = 0, ex_bu = 0;
-    bexp_td(a, ex_td);
-    bsweep<false>(a, ex_bu);
-    (void)ex_td;
-    (void)ex_bu;
+    uint64_t ex = 0;
+    bsweep<false>(a, ex);
 }
 
 __global__ void __launch_bounds__(kB) k_bfix(BArgs a)
@@ -314,16 +326,23 @@ __global__ void __launch_bounds__(kB) k_bcount(BArgs a)
 {
     const uint32_t c = blockIdx.x;
     const uint64_t v0 = (uint64_t)c * kChunk + (uint64_t)threadIdx.x * kPerThread;
-    uint64_t cn = 0, cm = 0;
+    uint64_t cn = 0, cm = 0, act = 0;
 #pragma unroll
     for (int k = 0; k < kPerThread; ++k) {
-        if (a.next[v0 + k]) {
+        const uint64_t x = a.next[v0 + k];
+        if (x) {
             ++cn;
             cm += a.deg[v0 + k];
+            act |= x;
         }
     }
     cn = wsum(cn);
     cm = wsum(cm);
+    // roots present in the next frontier of this chunk's graph
+#pragma unroll
+    for (int o = 16; o; o >>= 1) act |= __shfl_xor_sync(0xFFFFFFFFu, act, o);
+    if (g5_lane() == 0 && act)
+        atomicOr((unsigned long long *)&a.gd[a.chunk_graph[c]].amask_next, (unsigned long long)act);
     __shared__ uint64_t s_n[kW], s_m[kW];
     if (g5_lane() == 0) {
         s_n[threadIdx.x >> 5] = cn;
@@ -354,11 +373,29 @@ __global__ void __launch_bounds__(1024) k_bscan(BArgs a)
     }
     __syncthreads();
     const uint32_t C = a.nchunks;
-    for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
-        const int g = a.chunk_graph[c];
-        if (a.chunk_n[c]) {
-            atomicAdd((unsigned long long *)&s_gn[g], (unsigned long long)a.chunk_n[c]);
-            atomicAdd((unsigned long long *)&s_gm[g], (unsigned long long)a.chunk_m[c]);
+    {
+        // each thread sums a contiguous run of chunks (mostly one graph) and
+        // flushes once per graph change: few shared atomics per thread
+        const uint32_t per0 = (C + blockDim.x - 1) / blockDim.x;
+        const uint32_t c0 = threadIdx.x * per0, c1 = min(C, c0 + per0);
+        int g = -1;
+        uint64_t sn = 0, sm = 0;
+        for (uint32_t c = c0; c < c1; ++c) {
+            const int gc = a.chunk_graph[c];
+            if (gc != g) {
+                if (g >= 0 && sn) {
+                    atomicAdd((unsigned long long *)&s_gn[g], (unsigned long long)sn);
+                    atomicAdd((unsigned long long *)&s_gm[g], (unsigned long long)sm);
+                }
+                g = gc;
+                sn = sm = 0;
+            }
+            sn += a.chunk_n[c];
+            sm += a.chunk_m[c];
+        }
+        if (g >= 0 && sn) {
+            atomicAdd((unsigned long long *)&s_gn[g], (unsigned long long)sn);
+            atomicAdd((unsigned long long *)&s_gm[g], (unsigned long long)sm);
         }
     }
     __syncthreads();
@@ -379,6 +416,8 @@ __global__ void __launch_bounds__(1024) k_bscan(BArgs a)
         d.dir = nd;
         d.nf = tn;
         d.mf = tm;
+        d.amask = d.amask_next & d.mask;
+        d.amask_next = 0;
         s_gdir[threadIdx.x] = nd;
     }
     __syncthreads();
@@ -521,7 +560,7 @@ __global__ void __launch_bounds__(kB) k_bwrite(BArgs a)
 }
 
 __global__ void k_bdeg(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t ntot, uint32_t *deg,
-                       uint32_t *heavy)
+                       uint32_t *heavy, uint32_t *iso)
 {
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < ntot;
          v += (uint64_t)gridDim.x * blockDim.x) {
@@ -530,7 +569,11 @@ __global__ void k_bdeg(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t
         const uint32_t dv = vl < d.n ? (uint32_t)(d.row_off[vl + 1] - d.row_off[vl]) : 0u;
         deg[v] = dv;
         const unsigned h = __ballot_sync(0xFFFFFFFFu, dv > 64u);
-        if ((threadIdx.x & 31) == 0) heavy[v >> 5] = h;
+        const unsigned z = __ballot_sync(0xFFFFFFFFu, dv == 0u);
+        if ((threadIdx.x & 31) == 0) {
+            heavy[v >> 5] = h;
+            iso[v >> 5] = z;
+        }
     }
 }
 
@@ -545,6 +588,7 @@ struct g5_batch {
     uint8_t *chunk_graph = nullptr;
     uint32_t *deg = nullptr;
     uint32_t *heavy = nullptr;
+    uint32_t *iso = nullptr;
     uint64_t *words = nullptr;  // vis | front | next
     uint32_t *queue = nullptr;
     uint64_t *qoff = nullptr;
@@ -566,18 +610,32 @@ struct g5_batch {
 
 namespace {
 
-void enqueue_batch(g5_batch *b, const BArgs &a, cudaStream_t s, bool body)
+void enqueue_batch(g5_batch *b, const BArgs &a, cudaStream_t s, bool body, std::vector<cudaEvent_t> *ev = nullptr)
 {
+    auto mark = [&]() {
+        if (ev) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            cudaEventRecord(e, s);
+            ev->push_back(e);
+        }
+    };
     if (!body) {
         cudaMemsetAsync(b->words, 0, sizeof(uint64_t) * 3 * a.ntot, s);
         k_binit<<<std::max(1, a.ngraphs), kB, 0, s>>>(a);
         return;
     }
+    mark();
     k_bcount<<<a.nchunks, kB, 0, s>>>(a);
+    mark();
     k_bscan<<<1, 1024, 0, s>>>(a);
+    mark();
     k_bwrite<<<a.nchunks, kB, 0, s>>>(a);
-    k_bexp<<<g5::grid_for(8), kB, 0, s>>>(a);
-    k_bfix<<<g5::grid_for(8), kB, 0, s>>>(a);
+    mark();
+    k_btd<<<g5::grid_for(8), kB, 0, s>>>(a);
+    k_bbu<<<g5::grid_for(8), kB, 0, s>>>(a);
+    mark();
+    mark();
 }
 
 g5_status build_batch_graph(g5_batch *b)
@@ -626,6 +684,7 @@ void free_batch(g5_batch *b)
     cudaFree(b->chunk_graph);
     cudaFree(b->deg);
     cudaFree(b->heavy);
+    cudaFree(b->iso);
     cudaFree(b->words);
     cudaFree(b->queue);
     cudaFree(b->qoff);
@@ -694,6 +753,7 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     B_ALLOC(b->chunk_graph, cg.size());
     B_ALLOC(b->deg, sizeof(uint32_t) * vb);
     B_ALLOC(b->heavy, sizeof(uint32_t) * (vb / 32));
+    B_ALLOC(b->iso, sizeof(uint32_t) * (vb / 32));
     B_ALLOC(b->words, sizeof(uint64_t) * 3 * vb);
     B_ALLOC(b->queue, sizeof(uint32_t) * vb);
     B_ALLOC(b->qoff, sizeof(uint64_t) * (vb + 1));
@@ -716,6 +776,7 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     a.chunk_graph = b->chunk_graph;
     a.deg = b->deg;
     a.heavy = b->heavy;
+    a.iso = b->iso;
     a.vis = b->words;
     a.front = b->words + vb;
     a.next = b->words + 2 * vb;
@@ -729,7 +790,7 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     a.roots = b->roots;
     a.root_off = b->root_off;
     a.level_log = b->level_log;
-    k_bdeg<<<g5::grid_for(8), kB, 0, b->stream>>>(b->gd, b->chunk_graph, vb, b->deg, b->heavy);
+    k_bdeg<<<g5::grid_for(8), kB, 0, b->stream>>>(b->gd, b->chunk_graph, vb, b->deg, b->heavy, b->iso);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
     *out = b;
     return G5_OK;
@@ -742,6 +803,57 @@ g5_status g5_batch_set_direction(g5_batch *b, double alpha, double beta)
     b->args.beta = beta;
     b->bound_pred = nullptr;  // rebuild the graph with the new kernel arguments
     return G5_OK;
+}
+
+g5_status g5_batch_profile(g5_batch *b, const int64_t *roots_host, const int *nroots, uint32_t *pred_out_dev,
+                           double *kernel_ms, int64_t *level_active, int max_levels, int *levels)
+{
+    // host-driven level loop with CUDA events around every launch: kernel_ms
+    // gets count, scan, write, expand, fixup totals (ms); level_active the
+    // active vertices of each level
+    if (!b || !roots_host || !nroots || !pred_out_dev || !kernel_ms || !levels) return G5_ERR_INVALID_ARG;
+    const int ng = (int)b->graphs.size();
+    uint64_t pb = 0;
+    int off = 0;
+    for (int i = 0; i < ng; ++i) {
+        if (nroots[i] < 0 || nroots[i] > 64) return G5_ERR_INVALID_ARG;
+        GraphDesc &d = b->hgd[i];
+        d.nroots = nroots[i];
+        d.mask = nroots[i] == 64 ? ~0ull : ((1ull << nroots[i]) - 1);
+        d.pred_base = pb;
+        pb += (uint64_t)nroots[i] * (uint64_t)d.n;
+        b->h_root_off[i] = off;
+        for (int r = 0; r < nroots[i]; ++r) b->h_roots[off + r] = roots_host[off + r];
+        off += nroots[i];
+    }
+    b->h_root_off[ng] = off;
+    cudaStream_t s = b->stream;
+    BArgs a = b->args;
+    a.pred = pred_out_dev;
+    a.use_cond = 0;
+    G5_CUDA(cudaMemcpyAsync(b->gd, b->hgd.data(), sizeof(GraphDesc) * ng, cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaMemcpyAsync(b->roots, b->h_roots, sizeof(int64_t) * (off ? off : 1), cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaMemcpyAsync(b->root_off, b->h_root_off, sizeof(int32_t) * (ng + 1), cudaMemcpyHostToDevice, s));
+    if (pb) G5_CUDA(cudaMemsetAsync(pred_out_dev, 0xFF, sizeof(uint32_t) * pb, s));
+    enqueue_batch(b, a, s, false);
+    for (int k = 0; k < 5; ++k) kernel_ms[k] = 0;
+    int L = 0;
+    for (; L < kMaxLevels; ++L) {
+        std::vector<cudaEvent_t> ev;
+        enqueue_batch(b, a, s, true, &ev);
+        G5_CUDA(cudaMemcpyAsync(b->h_st, b->st, sizeof(BState), cudaMemcpyDeviceToHost, s));
+        G5_CUDA(cudaStreamSynchronize(s));
+        for (size_t k = 0; k + 1 < ev.size(); ++k) {
+            float t = 0;
+            cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+            kernel_ms[k] += t;
+        }
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+        if (level_active && L < max_levels) level_active[L] = (int64_t)b->h_st->active;
+        if (b->h_st->active == 0 || b->h_st->err) break;
+    }
+    *levels = L + 1;
+    return b->h_st->err ? G5_ERR_CAPACITY : G5_OK;
 }
 
 g5_status g5_batch_destroy(g5_batch *b)

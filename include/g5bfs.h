@@ -202,6 +202,15 @@ typedef struct g5_batch g5_batch;
 g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out);
 g5_status g5_batch_destroy(g5_batch *bt);
 
+/* The same search as g5_batch_run with a host-driven level loop and CUDA
+ * events around every launch (for profiling): kernel_ms[5] receives the
+ * total ms of the count, scan, write, expand and fix-up kernels;
+ * level_active (nullable, max_levels entries) the active vertices per level;
+ * *levels the levels run. */
+g5_status g5_batch_profile(g5_batch *bt, const int64_t *roots_host, const int *nroots,
+                           uint32_t *pred_out_dev, double *kernel_ms, int64_t *level_active,
+                           int max_levels, int *levels);
+
 /* Direction-switch thresholds of the batched search (defaults 14 and 24),
  * applied to each graph's union frontier. */
 g5_status g5_batch_set_direction(g5_batch *bt, double alpha, double beta);
