@@ -53,6 +53,11 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="keep Beamer's alpha=14, beta=24")
     ap.add_argument("--alpha", type=float, default=None)
     ap.add_argument("--beta", type=float, default=None)
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-codec", action="store_true")
+    ap.add_argument("--serve-rates", default="1000,5000,20000")
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--profile-batch", action="store_true",
                     help="only the batched search, host-driven with per-kernel CUDA events (for ncu)")
     ap.add_argument("--host-loop", action="store_true",
@@ -350,6 +355,14 @@ def main():
         except g5.G5Error as e:
             batched = {"error": str(e)}
 
+    serve = mixed = codec = None
+    if rank == 0 and not args.no_serve:
+        serve = bench_serve(g5, g, args)
+    if rank == 0 and not args.no_mixed:
+        mixed = bench_mixed(g5, torch, args)
+    if rank == 0 and not args.no_codec:
+        codec = bench_codec(g5, torch, args)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         ro, col = g.csr()
@@ -383,10 +396,19 @@ def main():
             "plain": {"hmean_gteps": value_rank, "mean_ms": statistics.mean(dev_ms),
                       "p99_ms": float(np.percentile(dev_ms, 99)), "levels": recs[0][3] if recs else None},
             "batched": batched,
+            "serve": serve,
+            "mixed_batch": mixed,
+            "codec": codec,
             "cpu_baseline": cpu,
         }
-        launches = sum(rec[3] for rec in recs[:nr]) * 4 + 4 * nr
-        line["gpu_launches"] = launches * args.steps
+        if batched and "aggregate_gteps" in batched:
+            line["batched_over_plain"] = batched["aggregate_gteps"] / value_rank if value_rank else None
+        if serve:
+            # headline: the lowest offered rate (the others saturate the scale-26 graph)
+            line["p99_query_ms"] = serve["rates"][0]["p99_ms"]
+            line["p50_query_ms"] = serve["rates"][0]["p50_ms"]
+        # per search: k_init + (k_td, k_bu, k_count, k_write) per level
+        line["gpu_launches"] = sum(1 + 4 * rec[3] for rec in recs)
         print(json.dumps(line))
     bfs.close()
     g.close()
@@ -410,6 +432,159 @@ def bench_batched(g5, torch, g, roots, nedges, args, tune=None):
     bt.close()
     return {"aggregate_gteps": hmean(agg), "ms_per_batch": statistics.mean(ms),
             "alpha": tuned["alpha"] if tuned else 14.0, "beta": tuned["beta"] if tuned else 24.0}
+
+
+def bench_serve(g5, big, args):
+    """Continuous-batching server over resident Kronecker graphs (the big one
+    is the bench graph); seeded Poisson arrivals, graph chosen uniformly."""
+    scales = [s for s in (20, 22, 24) if s < args.scale] + [args.scale]
+    graphs = [g5.Graph.kronecker(s) for s in scales[:-1]] + [big]
+    pools, nedge = [], []
+    for gr in graphs:
+        roots = g5.select_roots(gr, 64)
+        b = g5.CudaBFS(gr)
+        ne = {}
+        for r in roots:
+            b.runBFS(int(r))
+            ne[int(r)] = b.teps_edges()
+        b.close()
+        pools.append(roots)
+        nedge.append(ne)
+    budget = 64 << 30
+    sv = g5.Server(graphs, mem_budget=budget, keep_results=False, mode=g5.Server.STREAMS)
+    slots = sv.slots()
+    rng = np.random.default_rng(12345)
+    out = []
+    for rate in [float(x) for x in args.serve_rates.split(",")]:
+        n = int(rate * args.serve_seconds)
+        gaps = rng.exponential(1.0 / rate, n)
+        which = rng.integers(0, len(graphs), n)
+        picks = [int(pools[w][rng.integers(0, len(pools[w]))]) for w in which]
+        st0 = sv.stats()
+        t0 = time.perf_counter()
+        due = t0
+        tickets = []
+        for k in range(n):
+            due += gaps[k]
+            while time.perf_counter() < due:
+                pass
+            tickets.append((sv.submit(int(which[k]), picks[k]), int(which[k]), picks[k]))
+        lat, edges = [], 0
+        for t, w, r in tickets:
+            sv.wait(t, 600.0)
+            _, l, _ = sv.result(t, with_pred=False)
+            lat.append(l)
+            edges += nedge[w][r]
+        wall = time.perf_counter() - t0
+        st1 = sv.stats()
+        out.append({"rate_qps": rate, "queries": n, "p50_ms": float(np.percentile(lat, 50)),
+                    "p99_ms": float(np.percentile(lat, 99)), "gteps": edges / wall / 1e9,
+                    "wall_s": wall, "level_steps": st1["steps"] - st0["steps"]})
+    sv.close()
+    for gr in graphs[:-1]:
+        gr.close()
+    return {"graphs_scales": scales, "slots": slots, "mem_budget_bytes": budget, "mode": "streams",
+            "rates": out}
+
+
+def bench_mixed(g5, torch, args):
+    """One batched launch over 8 graphs of uneven scale, 16 roots each."""
+    scales = [s for s in (18, 19, 20, 21, 22, 22, 23, 24) if s <= args.scale]
+    graphs = [g5.Graph.kronecker(s) for s in scales]
+    roots = [g5.select_roots(gr, 16) for gr in graphs]
+    total_edges = 0
+    for gr, rs in zip(graphs, roots):
+        b = g5.CudaBFS(gr)
+        for r in rs:
+            b.runBFS(int(r))
+            total_edges += b.teps_edges()
+        b.close()
+    bt = g5.Batch(graphs)
+    out = torch.empty(sum(16 * gr.n for gr in graphs), dtype=torch.int32, device="cuda")
+    allroots = np.concatenate(roots)
+    counts = [len(r) for r in roots]
+    for _ in range(2):
+        bt.run(allroots, counts, out)
+    ms = [bt.run(allroots, counts, out) for _ in range(3)]
+    bt.close()
+    for gr in graphs:
+        gr.close()
+    return {"scales": scales, "roots_per_graph": 16, "ms": float(np.median(ms)),
+            "aggregate_gteps": total_edges / (np.median(ms) * 1e-3) / 1e9}
+
+
+def bench_codec(g5, torch, args):
+    """s4-bp128 encode/decode on every level queue of 16 roots of a scale-24
+    graph, and the 8-way frontier-bitmap OR on 2^24-bit bitmaps."""
+    scale = min(24, args.scale)
+    gr = g5.Graph.kronecker(scale)
+    roots = g5.select_roots(gr, 16)
+    b = g5.CudaBFS(gr, want_levels=True)
+    queues = []
+    lev = np.empty(gr.n, np.int32)
+    for r in roots:
+        b.run(int(r), None, lev)
+        order = np.argsort(lev, kind="stable")
+        ls = lev[order]
+        for L in range(1, int(lev.max()) + 1):
+            lo, hi = np.searchsorted(ls, L), np.searchsorted(ls, L + 1)
+            if hi > lo:
+                queues.append(np.sort(order[lo:hi]).astype(np.uint32))
+    b.close()
+    maxn = max(len(q) for q in queues)
+    c = g5.Codec(maxn + 256)
+    din = torch.empty(maxn + 256, dtype=torch.int32, device="cuda")
+    dout = torch.empty(g5.Codec.bound(maxn) + 64, dtype=torch.int32, device="cuda")
+    back = torch.empty(maxn + 256, dtype=torch.int32, device="cuda")
+    stats = {}
+    for mode, name in ((g5.CODEC_D4, "d4"), (g5.CODEC_DM, "dm")):
+        enc_s = dec_s = 0.0
+        words = vals = 0
+        for q in queues:
+            din[: len(q)] = torch.from_numpy(q.view(np.int32)).cuda()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            w = c.encode(din, len(q), dout, mode, stream=torch.cuda.current_stream().cuda_stream)
+            e1.record(); torch.cuda.synchronize()
+            enc_s += e0.elapsed_time(e1) * 1e-3
+            e0.record()
+            m = c.decode(dout, w, back, maxn + 256, mode, stream=torch.cuda.current_stream().cuda_stream)
+            e1.record(); torch.cuda.synchronize()
+            dec_s += e0.elapsed_time(e1) * 1e-3
+            assert m == len(q)
+            words += w
+            vals += len(q)
+        stats[name] = {"encode_GBps": 4 * vals / enc_s / 1e9, "decode_GBps": 4 * vals / dec_s / 1e9,
+                       "ratio_words_per_value": words / vals}
+    c.close()
+    gr.close()
+    # bitmap OR: 8 sources of 2^24 bits, densities 1..60 %, 12 independent sets
+    # round-robin so the footprint (12 x 9 x 2 MB = 216 MB) exceeds L2
+    words64 = (1 << 24) // 64
+    rng = np.random.default_rng(7)
+    res = {}
+    for dens in (0.01, 0.05, 0.1, 0.2, 0.4, 0.6):
+        sets = []
+        for _ in range(12):
+            srcs = []
+            for _ in range(8):
+                bits = rng.random(1 << 24) < dens
+                srcs.append(torch.from_numpy(np.packbits(bits, bitorder="little").view(np.int64)).cuda())
+            sets.append((torch.zeros(words64, dtype=torch.int64, device="cuda"), srcs))
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        reps = 24
+        e0.record()
+        for k in range(reps):
+            dst, srcs = sets[k % len(sets)]
+            g5.bitmap_or(dst, srcs, words64, stream=torch.cuda.current_stream().cuda_stream)
+        e1.record(); torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3 / reps
+        res[str(dens)] = {"GBps": 10 * words64 * 8 / t / 1e9, "us": t * 1e6}
+    return {"queues": len(queues), "values": vals, "max_queue": maxn, "codecs": stats,
+            "bitmap_or_8x2^24": res, "bitmap_or_bytes_per_call": 10 * words64 * 8,
+            "l2": "12 bitmap sets used round-robin (216 MB > L2)"}
 
 
 if __name__ == "__main__":

@@ -95,6 +95,17 @@ SIGNATURES = {
     "g5_batch_set_direction": (_I, [_P, C.c_double, C.c_double]),
     "g5_batch_profile": (_I, [_P, _P, _P, _P, _P, _P, _I, C.POINTER(_I)]),
     "g5_batch_run": (_I, [_P, _P, _P, _P, C.POINTER(C.c_double)]),
+    "g5_batch_serve_begin": (_I, [_P, _P, _P]),
+    "g5_batch_serve_step": (_I, [_P, _P, _P, _P, _I, _P, _P, C.POINTER(C.c_double)]),
+    "g5_bfs_launch": (_I, [_P, _I64]),
+    "g5_bfs_poll": (_I, [_P, C.POINTER(_I), C.POINTER(C.c_double)]),
+    "g5_server_create": (_I, [_P, _I, _SZ, _I, _I, C.POINTER(_P)]),
+    "g5_server_slots": (_I, [_P, _P]),
+    "g5_server_submit": (_I, [_P, _I, _I64, C.POINTER(_U64)]),
+    "g5_server_wait": (_I, [_P, _U64, C.c_double, C.POINTER(_I)]),
+    "g5_server_result": (_I, [_P, _U64, _P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "g5_server_stats": (_I, [_P, C.POINTER(_U64), C.POINTER(_U64), C.POINTER(C.c_double)]),
+    "g5_server_destroy": (_I, [_P]),
     "g5_codec_bound": (_SZ, [_SZ]),
     "g5_codec_create": (_I, [_SZ, C.POINTER(_P)]),
     "g5_codec_destroy": (_I, [_P]),
@@ -433,6 +444,64 @@ class Batch:
     def close(self) -> None:
         if self._h:
             lib().g5_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Resident graphs answering single-root queries with continuous batching (g5_server)."""
+
+    STREAMS, LEVELS = 0, 1
+
+    def __init__(self, graphs: Sequence[Graph], mem_budget: int, keep_results: bool = True, mode: int = 0):
+        self.graphs = list(graphs)
+        arr = (C.c_void_p * len(self.graphs))(*[g._h.value for g in self.graphs])
+        h = C.c_void_p()
+        _check(lib().g5_server_create(arr, len(self.graphs), int(mem_budget), int(keep_results), int(mode),
+                                      C.byref(h)), "g5_server_create")
+        self._h = h
+
+    def slots(self) -> list:
+        out = np.zeros(len(self.graphs), np.int32)
+        _check(lib().g5_server_slots(self._h, _ptr(out)), "g5_server_slots")
+        return out.tolist()
+
+    def submit(self, graph: int, root: int) -> int:
+        t = C.c_uint64()
+        _check(lib().g5_server_submit(self._h, graph, int(root), C.byref(t)), "g5_server_submit")
+        return t.value
+
+    def wait(self, ticket: int, timeout_s: float = 60.0) -> bool:
+        done = C.c_int()
+        _check(lib().g5_server_wait(self._h, ticket, timeout_s, C.byref(done)), "g5_server_wait")
+        return bool(done.value)
+
+    def result(self, ticket: int, with_pred: bool = True):
+        """(parents or None, latency ms, queueing ms); frees the query's slot."""
+        n = None
+        pred = None
+        lat, q = C.c_double(), C.c_double()
+        if with_pred:
+            # the graph of the ticket is not known here; size for the largest
+            n = max(g.n for g in self.graphs)
+            pred = np.empty(n, np.int64)
+        _check(lib().g5_server_result(self._h, ticket, _ptr(pred), C.byref(lat), C.byref(q)),
+               "g5_server_result")
+        return pred, lat.value, q.value
+
+    def stats(self) -> dict:
+        st, cp, ms = C.c_uint64(), C.c_uint64(), C.c_double()
+        _check(lib().g5_server_stats(self._h, C.byref(st), C.byref(cp), C.byref(ms)), "g5_server_stats")
+        return {"steps": st.value, "completed": cp.value, "device_ms": ms.value}
+
+    def close(self) -> None:
+        if self._h:
+            lib().g5_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -92,6 +92,7 @@ struct BArgs {
     cudaGraphConditionalHandle cond;
     int use_cond;
     uint64_t *level_log;    // per level: active vertices
+    int serving;            // continuous batching: no level cap, fixed m_u
 };
 
 __device__ __forceinline__ uint64_t wsum(uint64_t v)
@@ -403,8 +404,9 @@ __global__ void __launch_bounds__(1024) k_bscan(BArgs a)
         GraphDesc &d = a.gd[threadIdx.x];
         const uint64_t tn = s_gn[threadIdx.x], tm = s_gm[threadIdx.x];
         int nd = d.dir;
-        // Beamer's switch on the union frontier of the graph's roots
-        const uint64_t mu_after = d.mu >= tm ? d.mu - tm : 0;
+        // Beamer's switch on the union frontier of the graph's roots (when
+        // serving, roots come and go, so m_u stays the whole graph)
+        const uint64_t mu_after = a.serving ? (uint64_t)d.nnz : (d.mu >= tm ? d.mu - tm : 0);
         if (a.st->level >= 0) {
             if (d.dir == TD) {
                 if ((double)tm > (double)mu_after / a.alpha) nd = BU;
@@ -486,7 +488,7 @@ __global__ void __launch_bounds__(1024) k_bscan(BArgs a)
         a.qoff[tot_n] = tot_m;
         if (st->level < kMaxLevels) a.level_log[st->level] = act;
         bool cont = act > 0 && st->err == 0;
-        if (cont && st->level + 1 >= kMaxLevels) {
+        if (cont && !a.serving && st->level + 1 >= kMaxLevels) {
             st->err |= 8u;
             cont = false;
         }
@@ -559,6 +561,37 @@ __global__ void __launch_bounds__(kB) k_bwrite(BArgs a)
     }
 }
 
+// Continuous batching: roots admitted into free slots (bit r of their
+// graph) join the next level as its frontier; retired roots' visited bits are
+// cleared so the slot can be reused.
+struct Admit {
+    int32_t graph;
+    int32_t slot;
+    int64_t root;
+};
+
+__global__ void k_sadmit(BArgs a, const Admit *adm, int nadm)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nadm; i += gridDim.x * blockDim.x) {
+        const Admit x = adm[i];
+        const GraphDesc &d = a.gd[x.graph];
+        atomicOr((unsigned long long *)&a.next[d.vbase + x.root], 1ull << x.slot);
+        a.pred[d.pred_base + (uint64_t)x.slot * d.n + x.root] = (uint32_t)x.root;
+    }
+}
+
+__global__ void k_sclear(BArgs a, const uint64_t *clear_mask)
+{
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < a.ntot;
+         v += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t m = clear_mask[graph_of(a, v)];
+        if (m) {
+            const uint64_t x = a.vis[v];
+            if (x & m) a.vis[v] = x & ~m;
+        }
+    }
+}
+
 __global__ void k_bdeg(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t ntot, uint32_t *deg,
                        uint32_t *heavy, uint32_t *iso)
 {
@@ -603,6 +636,8 @@ struct g5_batch {
     int32_t *h_root_off = nullptr;
     BState *h_st = nullptr;
     uint32_t *bound_pred = nullptr;  // pred pointer the graph was built for
+    void *adm_dev = nullptr;          // serving: admissions + retire masks
+    void *adm_host = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -695,6 +730,8 @@ void free_batch(g5_batch *b)
     cudaFree(b->roots);
     cudaFree(b->root_off);
     cudaFree(b->level_log);
+    cudaFree(b->adm_dev);
+    cudaFreeHost(b->adm_host);
     cudaFreeHost(b->h_roots);
     cudaFreeHost(b->h_root_off);
     cudaFreeHost(b->h_st);
@@ -856,6 +893,99 @@ g5_status g5_batch_profile(g5_batch *b, const int64_t *roots_host, const int *nr
     return b->h_st->err ? G5_ERR_CAPACITY : G5_OK;
 }
 
+g5_status g5_batch_serve_begin(g5_batch *b, uint32_t *pred_dev, const int *slots)
+{
+    // every graph gets `slots[g]` root slots whose parents live in pred_dev,
+    // root-major per graph (graph 0 slot 0, slot 1, ..., graph 1 ...)
+    if (!b || !pred_dev || !slots) return G5_ERR_INVALID_ARG;
+    const int ng = (int)b->graphs.size();
+    uint64_t pb = 0;
+    for (int i = 0; i < ng; ++i) {
+        if (slots[i] < 0 || slots[i] > 64) return G5_ERR_INVALID_ARG;
+        GraphDesc &d = b->hgd[i];
+        d.nroots = slots[i];
+        d.mask = slots[i] == 64 ? ~0ull : ((1ull << slots[i]) - 1);
+        d.pred_base = pb;
+        d.dir = TD;
+        d.mu = (uint64_t)d.nnz;
+        d.nf = d.mf = d.examined = d.amask = d.amask_next = 0;
+        pb += (uint64_t)slots[i] * (uint64_t)d.n;
+    }
+    cudaStream_t s = b->stream;
+    b->args.pred = pred_dev;
+    b->args.serving = 1;
+    b->args.use_cond = 0;
+    if (!b->adm_dev) G5_CUDA(cudaMalloc(&b->adm_dev, sizeof(Admit) * 64 * ng + sizeof(uint64_t) * ng));
+    if (!b->adm_host) G5_CUDA(cudaMallocHost(&b->adm_host, sizeof(Admit) * 64 * ng + sizeof(uint64_t) * ng));
+    G5_CUDA(cudaMemcpyAsync(b->gd, b->hgd.data(), sizeof(GraphDesc) * ng, cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaMemsetAsync(b->words, 0, sizeof(uint64_t) * 3 * b->args.ntot, s));
+    BState z;
+    memset(&z, 0, sizeof z);
+    z.level = 0;
+    *b->h_st = z;
+    G5_CUDA(cudaMemcpyAsync(b->st, b->h_st, sizeof(BState), cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaStreamSynchronize(s));
+    return G5_OK;
+}
+
+g5_status g5_batch_serve_step(g5_batch *b, const int32_t *adm_graph, const int32_t *adm_slot,
+                              const int64_t *adm_root, int nadm, const uint64_t *retire_mask,
+                              uint64_t *active_mask, double *device_ms)
+{
+    // one level of continuous batching: clear the visited bits of retired
+    // slots, start the admitted roots, run one level; active_mask[g] gets the
+    // slots whose frontier is still non-empty
+    if (!b || (nadm && (!adm_graph || !adm_slot || !adm_root)) || !active_mask || !b->args.serving)
+        return G5_ERR_INVALID_ARG;
+    const int ng = (int)b->graphs.size();
+    if (nadm > 64 * ng) return G5_ERR_CAPACITY;
+    cudaStream_t s = b->stream;
+    Admit *ah = reinterpret_cast<Admit *>(b->adm_host);
+    uint64_t *rh = reinterpret_cast<uint64_t *>(ah + 64 * ng);
+    bool any_retire = false;
+    for (int g = 0; g < ng; ++g) {
+        rh[g] = retire_mask ? retire_mask[g] : 0;
+        any_retire |= rh[g] != 0;
+    }
+    for (int i = 0; i < nadm; ++i) {
+        const int g = adm_graph[i];
+        if (g < 0 || g >= ng || adm_slot[i] < 0 || adm_slot[i] >= b->hgd[g].nroots || adm_root[i] < 0 ||
+            adm_root[i] >= b->hgd[g].n)
+            return G5_ERR_INVALID_ARG;
+        ah[i].graph = g;
+        ah[i].slot = adm_slot[i];
+        ah[i].root = adm_root[i];
+    }
+    Admit *ad = reinterpret_cast<Admit *>(b->adm_dev);
+    uint64_t *rd = reinterpret_cast<uint64_t *>(ad + 64 * ng);
+    G5_CUDA(cudaEventRecord(b->ev0, s));
+    if (any_retire || nadm) {
+        G5_CUDA(cudaMemcpyAsync(b->adm_dev, b->adm_host, sizeof(Admit) * 64 * ng + sizeof(uint64_t) * ng,
+                                cudaMemcpyHostToDevice, s));
+    }
+    if (any_retire) k_sclear<<<g5::grid_for(8), kB, 0, s>>>(b->args, rd);
+    for (int i = 0; i < nadm; ++i) {
+        const GraphDesc &d = b->hgd[ah[i].graph];
+        G5_CUDA(cudaMemsetAsync(b->args.pred + d.pred_base + (uint64_t)ah[i].slot * d.n, 0xFF,
+                                sizeof(uint32_t) * (size_t)d.n, s));
+    }
+    if (nadm) k_sadmit<<<1, 128, 0, s>>>(b->args, ad, nadm);
+    enqueue_batch(b, b->args, s, true);
+    G5_CUDA(cudaEventRecord(b->ev1, s));
+    G5_CUDA(cudaMemcpyAsync(b->hgd.data(), b->gd, sizeof(GraphDesc) * ng, cudaMemcpyDeviceToHost, s));
+    G5_CUDA(cudaMemcpyAsync(b->h_st, b->st, sizeof(BState), cudaMemcpyDeviceToHost, s));
+    G5_CUDA(cudaStreamSynchronize(s));
+    // active slots: in the frontier the step just wrote (collected by the
+    // count kernel) plus anything the expansion put into the next frontier
+    for (int g = 0; g < ng; ++g) active_mask[g] = b->hgd[g].amask;
+    if (device_ms) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+        *device_ms = ms;
+    }
+    return b->h_st->err ? G5_ERR_CAPACITY : G5_OK;
+}
+
 g5_status g5_batch_destroy(g5_batch *b)
 {
     if (!b) return G5_ERR_INVALID_ARG;
@@ -890,6 +1020,7 @@ g5_status g5_batch_run(g5_batch *b, const int64_t *roots_host, const int *nroots
     b->h_root_off[ng] = off;
     cudaStream_t s = b->stream;
     b->args.pred = pred_out_dev;
+    b->args.serving = 0;
     if (!b->exec || b->bound_pred != pred_out_dev) {
         G5_TRY(build_batch_graph(b));
         b->bound_pred = pred_out_dev;

@@ -1331,6 +1331,44 @@ g5_status g5_bfs_profile_log(g5_bfs *b, int32_t *kinds, double *ms, int max_rows
     return G5_OK;
 }
 
+g5_status g5_bfs_launch(g5_bfs *b, int64_t root)
+{
+    // asynchronous search on the workspace's stream (CUDA-graph workspaces
+    // only): completion is polled with g5_bfs_poll
+    if (!b || root < 0 || root >= b->g->n || !b->exec) return G5_ERR_INVALID_ARG;
+    cudaStream_t s = b->stream;
+    *b->h_root = root;
+    G5_CUDA(cudaMemcpyAsync(b->root_dev, b->h_root, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaEventRecord(b->ev0, s));
+    G5_CUDA(cudaGraphLaunch(b->exec, s));
+    G5_CUDA(cudaEventRecord(b->ev1, s));
+    G5_CUDA(cudaMemcpyAsync(b->h_st, b->st, sizeof(BfsState), cudaMemcpyDeviceToHost, s));
+    b->ran = true;
+    b->last_root = root;
+    return G5_OK;
+}
+
+g5_status g5_bfs_poll(g5_bfs *b, int *done, double *device_ms)
+{
+    if (!b || !done) return G5_ERR_INVALID_ARG;
+    const cudaError_t e = cudaStreamQuery(b->stream);
+    if (e == cudaErrorNotReady) {
+        *done = 0;
+        return G5_OK;
+    }
+    G5_CUDA(e);
+    *done = 1;
+    if (device_ms) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+        *device_ms = ms;
+    }
+    const BfsState &hs = *b->h_st;
+    if (hs.err & G5_DEVERR_LEVELS) return G5_ERR_TIMEOUT;
+    if (hs.err) return G5_ERR_CAPACITY;
+    return G5_OK;
+}
+
 g5_status g5_bfs_device_pred(g5_bfs *b, const int64_t **pred)
 {
     if (!b || !pred) return G5_ERR_INVALID_ARG;

@@ -1,0 +1,431 @@
+// g5_server.cpp -- BFS query serving with continuous batching.
+//
+// The reference answers one root at a time (cpu_2d/main.cpp:419-462).  Here a
+// server keeps several graphs resident and answers single-root queries as
+// they arrive: a worker thread steps the batched level loop of all graphs
+// one level at a time; between steps, finished roots retire (their frontier
+// became empty, so their parent arrays are complete) and queued queries are
+// admitted into free root slots.  A query therefore starts at the next level
+// boundary instead of waiting for a whole batch, and its work shares every
+// adjacency read with the other queries of its graph that are in flight.
+//
+// Two slot kinds: one-root search workspaces on their own streams (queries
+// start as soon as a workspace is free and run concurrently), or root bits
+// of the bit-sliced level loop (queries join at the next level boundary and
+// share every adjacency read with the other roots of their graph).
+// Admission is by device memory: a graph gets as many slots (at most 64) as
+// its share of the budget holds.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "g5_internal.h"
+#include "g5bfs.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Query {
+    int graph = 0;
+    int64_t root = 0;
+    int slot = -1;
+    int state = 0;  // 0 queued, 1 running, 2 done, 3 released
+    Clock::time_point t_submit, t_start, t_done;
+};
+
+}  // namespace
+
+struct g5_server {
+    std::vector<g5_graph *> graphs;
+    int mode = G5_SERVE_STREAMS;
+    std::vector<std::vector<g5_bfs *>> ws;  // streams mode: workspaces per graph
+    g5_batch *bt = nullptr;
+    uint32_t *pred = nullptr;             // parents of every slot (device)
+    std::vector<uint64_t> pred_base;      // per graph
+    std::vector<int> slots;               // per graph
+    std::vector<std::vector<uint64_t>> slot_query;  // ticket per slot (0 free)
+    std::vector<uint64_t> retire;         // per graph: slots to clear next step
+    std::vector<std::deque<uint64_t>> queue;
+    std::unordered_map<uint64_t, Query> queries;
+    uint64_t next_ticket = 1;
+    int keep_results = 1;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::thread worker;
+    std::atomic<bool> stop{false};
+    g5_status error = G5_OK;
+    // statistics
+    uint64_t steps = 0, completed = 0;
+    double device_ms = 0;
+};
+
+namespace {
+
+// Streams mode: every slot is a one-root search workspace with its own
+// stream; launched searches run concurrently and are polled for completion.
+void worker_streams(g5_server *sv)
+{
+    cudaSetDevice(sv->graphs[0]->device);
+    const int ng = (int)sv->graphs.size();
+    std::vector<std::vector<int>> running(ng);
+    for (int g = 0; g < ng; ++g) running[g].assign(sv->slots[g], 0);
+    int nrun = 0;
+    while (!sv->stop.load()) {
+        {
+            std::unique_lock<std::mutex> lk(sv->mu);
+            for (int g = 0; g < ng; ++g) {
+                for (int s = 0; s < sv->slots[g] && !sv->queue[g].empty(); ++s) {
+                    if (sv->slot_query[g][s] != 0) continue;
+                    const uint64_t t = sv->queue[g].front();
+                    sv->queue[g].pop_front();
+                    Query &q = sv->queries[t];
+                    q.slot = s;
+                    q.state = 1;
+                    q.t_start = Clock::now();
+                    sv->slot_query[g][s] = t;
+                    const g5_status st = g5_bfs_launch(sv->ws[g][s], q.root);
+                    if (st != G5_OK) {
+                        sv->error = st;
+                        sv->stop.store(true);
+                        sv->cv_done.notify_all();
+                        return;
+                    }
+                    running[g][s] = 1;
+                    ++nrun;
+                }
+            }
+            if (nrun == 0) {
+                sv->cv_work.wait_for(lk, std::chrono::milliseconds(2));
+                continue;
+            }
+        }
+        bool any_done = false;
+        for (int g = 0; g < ng; ++g) {
+            for (int s = 0; s < sv->slots[g]; ++s) {
+                if (!running[g][s]) continue;
+                int done = 0;
+                double ms = 0;
+                const g5_status st = g5_bfs_poll(sv->ws[g][s], &done, &ms);
+                if (!done) continue;
+                running[g][s] = 0;
+                --nrun;
+                any_done = true;
+                std::lock_guard<std::mutex> lk(sv->mu);
+                if (st != G5_OK) {
+                    sv->error = st;
+                    sv->stop.store(true);
+                    sv->cv_done.notify_all();
+                    return;
+                }
+                sv->steps += 1;
+                sv->device_ms += ms;
+                const uint64_t t = sv->slot_query[g][s];
+                Query &q = sv->queries[t];
+                q.state = 2;
+                q.t_done = Clock::now();
+                sv->completed += 1;
+                if (!sv->keep_results) {
+                    q.state = 3;
+                    sv->slot_query[g][s] = 0;
+                }
+            }
+        }
+        if (any_done) {
+            std::lock_guard<std::mutex> lk(sv->mu);
+            sv->cv_done.notify_all();
+        } else {
+            std::this_thread::sleep_for(std::chrono::microseconds(20));
+        }
+    }
+}
+
+// Levels mode: every slot is a root bit of the graph's bit-sliced level
+// loop, stepped one level at a time.
+void worker_loop(g5_server *sv)
+{
+    cudaSetDevice(sv->graphs[0]->device);
+    const int ng = (int)sv->graphs.size();
+    std::vector<int32_t> ag, as;
+    std::vector<int64_t> ar;
+    std::vector<uint64_t> active(ng, 0), retire(ng, 0), inflight(ng, 0);
+    while (!sv->stop.load()) {
+        ag.clear();
+        as.clear();
+        ar.clear();
+        {
+            std::unique_lock<std::mutex> lk(sv->mu);
+            // admit queued queries into free slots (a slot retired in the last
+            // step is cleared by this step before its new root starts)
+            for (int g = 0; g < ng; ++g) {
+                for (int s = 0; s < sv->slots[g] && !sv->queue[g].empty(); ++s) {
+                    if (sv->slot_query[g][s] != 0 || (sv->retire[g] >> s) & 1ull) continue;
+                    const uint64_t t = sv->queue[g].front();
+                    sv->queue[g].pop_front();
+                    Query &q = sv->queries[t];
+                    q.slot = s;
+                    q.state = 1;
+                    q.t_start = Clock::now();
+                    sv->slot_query[g][s] = t;
+                    ag.push_back(g);
+                    as.push_back(s);
+                    ar.push_back(q.root);
+                    inflight[g] |= 1ull << s;
+                }
+                retire[g] = sv->retire[g];
+                sv->retire[g] = 0;
+            }
+            bool any_inflight = false;
+            for (int g = 0; g < ng; ++g) any_inflight |= inflight[g] != 0;
+            bool any_retire = false;
+            for (int g = 0; g < ng; ++g) any_retire |= retire[g] != 0;
+            if (!any_inflight && ag.empty() && !any_retire) {
+                sv->cv_work.wait_for(lk, std::chrono::milliseconds(2));
+                continue;
+            }
+        }
+        double ms = 0;
+        g5_status st = g5_batch_serve_step(sv->bt, ag.data(), as.data(), ar.data(), (int)ag.size(), retire.data(),
+                                           active.data(), &ms);
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->steps += 1;
+        sv->device_ms += ms;
+        if (st != G5_OK) {
+            sv->error = st;
+            sv->stop.store(true);
+            sv->cv_done.notify_all();
+            return;
+        }
+        const Clock::time_point now = Clock::now();
+        for (int g = 0; g < ng; ++g) {
+            const uint64_t fin = inflight[g] & ~active[g];
+            if (!fin) continue;
+            inflight[g] &= ~fin;
+            for (int s = 0; s < sv->slots[g]; ++s) {
+                if (!((fin >> s) & 1ull)) continue;
+                const uint64_t t = sv->slot_query[g][s];
+                Query &q = sv->queries[t];
+                q.state = 2;
+                q.t_done = now;
+                sv->completed += 1;
+                if (!sv->keep_results) {
+                    // results are not kept: the slot is free at once
+                    q.state = 3;
+                    sv->slot_query[g][s] = 0;
+                    sv->retire[g] |= 1ull << s;
+                }
+            }
+        }
+        sv->cv_done.notify_all();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+g5_status g5_server_create(g5_graph *const *graphs, int ngraphs, size_t mem_budget, int keep_results, int mode,
+                           g5_server **out)
+{
+    if (!graphs || ngraphs < 1 || ngraphs > 64 || !out) return G5_ERR_INVALID_ARG;
+    if (mode != G5_SERVE_STREAMS && mode != G5_SERVE_LEVELS) return G5_ERR_INVALID_ARG;
+    *out = nullptr;
+    g5_server *sv = new g5_server();
+    sv->keep_results = keep_results ? 1 : 0;
+    sv->mode = mode;
+    uint64_t total_n = 0;
+    for (int i = 0; i < ngraphs; ++i) {
+        if (!graphs[i]) {
+            delete sv;
+            return G5_ERR_INVALID_ARG;
+        }
+        sv->graphs.push_back(graphs[i]);
+        total_n += (uint64_t)graphs[i]->n;
+    }
+    if (mode == G5_SERVE_STREAMS) {
+        // memory-based admission: workspaces per graph from an equal share
+        g5_bfs_config cfg;
+        g5_bfs_config_default(&cfg);
+        cfg.alpha = 40.0;
+        cfg.beta = 200.0;
+        for (int i = 0; i < ngraphs; ++i) {
+            const uint64_t per = 48ull * (uint64_t)graphs[i]->n + (uint64_t)graphs[i]->nnz / 64 + (1u << 20);
+            uint64_t k = std::min<uint64_t>(64, (mem_budget / (uint64_t)ngraphs) / per);
+            if (k == 0) {
+                for (auto &v : sv->ws)
+                    for (g5_bfs *b : v) g5_bfs_destroy(b);
+                delete sv;
+                return G5_ERR_OOM;
+            }
+            sv->ws.emplace_back();
+            for (uint64_t j = 0; j < k; ++j) {
+                g5_bfs *b = nullptr;
+                const g5_status st = g5_bfs_create(graphs[i], &cfg, &b);
+                if (st != G5_OK) {
+                    for (auto &v : sv->ws)
+                        for (g5_bfs *x : v) g5_bfs_destroy(x);
+                    delete sv;
+                    return st;
+                }
+                sv->ws.back().push_back(b);
+            }
+            sv->slots.push_back((int)k);
+            sv->slot_query.emplace_back(k, 0);
+        }
+        sv->retire.assign(ngraphs, 0);
+        sv->queue.resize(ngraphs);
+        sv->worker = std::thread(worker_streams, sv);
+        *out = sv;
+        return G5_OK;
+    }
+    // memory-based admission: slots per graph from an equal share of the budget
+    uint64_t pb = 0;
+    for (int i = 0; i < ngraphs; ++i) {
+        const uint64_t share = mem_budget / (uint64_t)ngraphs;
+        uint64_t s = share / (4ull * (uint64_t)graphs[i]->n);
+        s = std::min<uint64_t>(64, s);
+        if (s == 0) {
+            delete sv;
+            return G5_ERR_OOM;
+        }
+        sv->slots.push_back((int)s);
+        sv->pred_base.push_back(pb);
+        pb += s * (uint64_t)graphs[i]->n;
+        sv->slot_query.emplace_back(s, 0);
+    }
+    sv->retire.assign(ngraphs, 0);
+    sv->queue.resize(ngraphs);
+    if (cudaMalloc(&sv->pred, sizeof(uint32_t) * pb) != cudaSuccess) {
+        cudaGetLastError();
+        delete sv;
+        return G5_ERR_OOM;
+    }
+    g5_status st = g5_batch_create(graphs, ngraphs, &sv->bt);
+    if (st == G5_OK) st = g5_batch_serve_begin(sv->bt, sv->pred, sv->slots.data());
+    if (st != G5_OK) {
+        if (sv->bt) g5_batch_destroy(sv->bt);
+        cudaFree(sv->pred);
+        delete sv;
+        return st;
+    }
+    sv->worker = std::thread(worker_loop, sv);
+    *out = sv;
+    return G5_OK;
+}
+
+g5_status g5_server_slots(g5_server *sv, int *slots)
+{
+    if (!sv || !slots) return G5_ERR_INVALID_ARG;
+    for (size_t i = 0; i < sv->slots.size(); ++i) slots[i] = sv->slots[i];
+    return G5_OK;
+}
+
+g5_status g5_server_submit(g5_server *sv, int graph, int64_t root, uint64_t *ticket)
+{
+    if (!sv || !ticket || graph < 0 || graph >= (int)sv->graphs.size()) return G5_ERR_INVALID_ARG;
+    if (root < 0 || root >= sv->graphs[graph]->n) return G5_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (sv->error != G5_OK) return sv->error;
+    const uint64_t t = sv->next_ticket++;
+    Query q;
+    q.graph = graph;
+    q.root = root;
+    q.t_submit = Clock::now();
+    sv->queries[t] = q;
+    sv->queue[graph].push_back(t);
+    *ticket = t;
+    sv->cv_work.notify_one();
+    return G5_OK;
+}
+
+g5_status g5_server_wait(g5_server *sv, uint64_t ticket, double timeout_s, int *done)
+{
+    if (!sv || !done) return G5_ERR_INVALID_ARG;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->queries.find(ticket);
+    if (it == sv->queries.end()) return G5_ERR_INVALID_ARG;
+    const auto deadline = Clock::now() + std::chrono::duration<double>(timeout_s);
+    while (sv->queries[ticket].state < 2 && sv->error == G5_OK) {
+        if (sv->cv_done.wait_until(lk, deadline) == std::cv_status::timeout) break;
+    }
+    *done = sv->queries[ticket].state >= 2;
+    return sv->error;
+}
+
+g5_status g5_server_result(g5_server *sv, uint64_t ticket, int64_t *pred_host, double *latency_ms,
+                           double *queue_ms)
+{
+    // copies a finished query's parents (int64, -1 unvisited; may be NULL)
+    // and frees its slot
+    if (!sv) return G5_ERR_INVALID_ARG;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->queries.find(ticket);
+    if (it == sv->queries.end() || it->second.state < 2) return G5_ERR_INVALID_ARG;
+    Query q = it->second;
+    if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(q.t_done - q.t_submit).count();
+    if (queue_ms) *queue_ms = std::chrono::duration<double, std::milli>(q.t_start - q.t_submit).count();
+    if (q.state == 2 && pred_host && sv->mode == G5_SERVE_STREAMS) {
+        const int64_t n = sv->graphs[q.graph]->n;
+        const int64_t *src = nullptr;
+        g5_bfs_device_pred(sv->ws[q.graph][q.slot], &src);
+        lk.unlock();
+        if (cudaMemcpy(pred_host, src, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return G5_ERR_CUDA;
+        lk.lock();
+    } else if (q.state == 2 && pred_host) {
+        const int64_t n = sv->graphs[q.graph]->n;
+        std::vector<uint32_t> tmp((size_t)n);
+        const uint32_t *src = sv->pred + sv->pred_base[q.graph] + (uint64_t)q.slot * (uint64_t)n;
+        lk.unlock();
+        // the slot is not reused before it is released below
+        if (cudaMemcpy(tmp.data(), src, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return G5_ERR_CUDA;
+        for (int64_t v = 0; v < n; ++v) pred_host[v] = tmp[v] == 0xFFFFFFFFu ? -1 : (int64_t)tmp[v];
+        lk.lock();
+    }
+    Query &qq = sv->queries[ticket];
+    if (qq.state == 2) {
+        sv->slot_query[qq.graph][qq.slot] = 0;
+        if (sv->mode == G5_SERVE_LEVELS) sv->retire[qq.graph] |= 1ull << qq.slot;
+        qq.state = 3;
+        sv->cv_work.notify_one();
+    }
+    sv->queries.erase(ticket);
+    return G5_OK;
+}
+
+g5_status g5_server_stats(g5_server *sv, uint64_t *steps, uint64_t *completed, double *device_ms)
+{
+    if (!sv) return G5_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (steps) *steps = sv->steps;
+    if (completed) *completed = sv->completed;
+    if (device_ms) *device_ms = sv->device_ms;
+    return sv->error;
+}
+
+g5_status g5_server_destroy(g5_server *sv)
+{
+    if (!sv) return G5_ERR_INVALID_ARG;
+    sv->stop.store(true);
+    sv->cv_work.notify_all();
+    if (sv->worker.joinable()) sv->worker.join();
+    for (auto &v : sv->ws)
+        for (g5_bfs *b : v) g5_bfs_destroy(b);
+    if (sv->bt) g5_batch_destroy(sv->bt);
+    cudaFree(sv->pred);
+    delete sv;
+    return G5_OK;
+}
+
+}  // extern "C"

@@ -166,6 +166,14 @@ typedef struct g5_bfs_stats {
 g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_out,
                      g5_bfs_stats *stats);
 
+/* Asynchronous form of g5_bfs_run for a CUDA-graph workspace: launches the
+ * search on the workspace's own stream and returns; g5_bfs_poll sets *done
+ * once it has finished (and its status is the search's).  Parents stay in
+ * the workspace (g5_bfs_device_pred).  Workspaces on one graph run
+ * concurrently. */
+g5_status g5_bfs_launch(g5_bfs *b, int64_t root);
+g5_status g5_bfs_poll(g5_bfs *b, int *done, double *device_ms);
+
 /* Per-level record of the last search, 4 int64 per level: direction
  * (0 top-down, 1 bottom-up), frontier vertices, their adjacency entries, and
  * adjacency entries the expansion read.  *rows = levels written. */
@@ -222,6 +230,57 @@ g5_status g5_batch_set_direction(g5_batch *bt, double alpha, double beta);
  * Same parent choice as g5_bfs_run. */
 g5_status g5_batch_run(g5_batch *bt, const int64_t *roots_host, const int *nroots,
                        uint32_t *pred_out_dev, double *device_ms);
+
+/* Continuous batching on a batch workspace (used by the server below).
+ * serve_begin gives graph g `slots[g]` (<= 64) root slots whose uint32
+ * parents live in pred_dev, root-major per graph.  Each serve_step clears the
+ * visited bits of the slots in retire_mask[g], starts the admitted roots
+ * (adm_graph/adm_slot/adm_root, nadm entries) in their slots and runs one
+ * level of every graph; active_mask[g] receives the slots whose frontier was
+ * not empty in that level (a slot that was running and is not active has
+ * finished: its parents are complete). */
+g5_status g5_batch_serve_begin(g5_batch *bt, uint32_t *pred_dev, const int *slots);
+g5_status g5_batch_serve_step(g5_batch *bt, const int32_t *adm_graph, const int32_t *adm_slot,
+                              const int64_t *adm_root, int nadm, const uint64_t *retire_mask,
+                              uint64_t *active_mask, double *device_ms);
+
+/* ------------------------------------------------------------------------ */
+/* Serving: resident graphs, single-root queries, continuous batching        */
+/* ------------------------------------------------------------------------ */
+
+/* The reference answers one root at a time (cpu_2d/main.cpp:419-462); the
+ * server answers queries as they arrive, on graphs that stay resident.  A
+ * worker thread admits queued queries into free slots and retires finished
+ * ones while others run, so queries that arrive while others are on the GPU
+ * start as soon as a slot is free and their work overlaps on the device.
+ *   mode G5_SERVE_STREAMS: a slot is a one-root search workspace with its
+ *     own stream; slots per graph = the graph's equal share of mem_budget
+ *     divided by the workspace size (at most 64).
+ *   mode G5_SERVE_LEVELS: a slot is a root bit of the graph's bit-sliced
+ *     level loop, which is stepped one level at a time; queries join at the
+ *     next level boundary; slots = share / (4 bytes x vertices), at most 64.
+ * Queries beyond the free slots wait in a FIFO per graph (memory-based
+ * admission).  keep_results = 0 frees a slot as soon as its query finishes
+ * (results are discarded). */
+typedef struct g5_server g5_server;
+
+enum { G5_SERVE_STREAMS = 0, G5_SERVE_LEVELS = 1 };
+
+g5_status g5_server_create(g5_graph *const *graphs, int ngraphs, size_t mem_budget,
+                           int keep_results, int mode, g5_server **out);
+/* Slots per graph chosen by the admission rule. */
+g5_status g5_server_slots(g5_server *sv, int *slots);
+/* Thread safe: queues one query; *ticket identifies it. */
+g5_status g5_server_submit(g5_server *sv, int graph, int64_t root, uint64_t *ticket);
+/* Waits up to timeout_s seconds; *done = 1 when the query has finished. */
+g5_status g5_server_wait(g5_server *sv, uint64_t ticket, double timeout_s, int *done);
+/* Finished query: copies its parents (int64, -1 unvisited, root -> root;
+ * pred_host may be NULL), its latency from submission to completion and its
+ * queueing time, and forgets the query (frees its slot). */
+g5_status g5_server_result(g5_server *sv, uint64_t ticket, int64_t *pred_host, double *latency_ms,
+                           double *queue_ms);
+g5_status g5_server_stats(g5_server *sv, uint64_t *steps, uint64_t *completed, double *device_ms);
+g5_status g5_server_destroy(g5_server *sv);
 
 /* ------------------------------------------------------------------------ */
 /* s4-bp128 frontier codec on the device                                     */

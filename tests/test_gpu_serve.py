@@ -1,0 +1,103 @@
+"""Serving with continuous batching: every query's parents are the same
+alone and in a mix of concurrent queries on several graphs, and equal the
+oracle's; memory-based admission queues what does not fit."""
+import numpy as np
+import pytest
+
+import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+g5 = pytest.importorskip("gpugraph500_gb300")
+
+
+@pytest.fixture(scope="module")
+def graphs():
+    gs = [g5.Graph.kronecker(s) for s in (10, 11, 12)]
+    yield gs
+    for g in gs:
+        g.close()
+
+
+def run_queries(sv, queries, concurrent):
+    out = {}
+    if concurrent:
+        tickets = [(sv.submit(gi, r), gi, r) for gi, r in queries]
+        for t, gi, r in tickets:
+            assert sv.wait(t, 60.0)
+            pred, lat, q = sv.result(t)
+            out[(gi, r)] = pred
+    else:
+        for gi, r in queries:
+            t = sv.submit(gi, r)
+            assert sv.wait(t, 60.0)
+            pred, lat, q = sv.result(t)
+            out[(gi, r)] = pred
+    return out
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_alone_and_mixed_agree_with_oracle(graphs, mode):
+    csrs = [g.csr() for g in graphs]
+    roots = [g5.select_roots(g, 20) for g in graphs]
+    rng = np.random.default_rng(0)
+    queries = [(gi, int(r)) for gi in range(3) for r in roots[gi]]
+    order = rng.permutation(len(queries))
+    queries = [queries[i] for i in order]
+    sv = g5.Server(graphs, mem_budget=1 << 30, mode=mode)
+    assert min(sv.slots()) >= 2
+    alone = run_queries(sv, queries, concurrent=False)
+    mixed = run_queries(sv, queries, concurrent=True)
+    for (gi, r), p in alone.items():
+        n = graphs[gi].n
+        want, _ = orc.bfs(csrs[gi][0], csrs[gi][1], r)
+        assert np.array_equal(p[:n], want), (gi, r)
+        assert np.array_equal(mixed[(gi, r)][:n], p[:n]), (gi, r)
+    st = sv.stats()
+    assert st["completed"] == 2 * len(queries)
+    sv.close()
+
+
+@pytest.mark.parametrize("mode,per_slot", [(0, 48), (1, 4)])
+def test_memory_admission_queues(graphs, mode, per_slot):
+    # budget for about 3 slots of the largest graph: queries beyond the slots wait
+    g = graphs[2]
+    extra = 3 * (g.nnz // 64 + (1 << 20)) if mode == 0 else 0
+    sv = g5.Server([g], mem_budget=3 * per_slot * g.n + extra, mode=mode)
+    assert 1 <= sv.slots()[0] <= 3
+    ro, col = g.csr()
+    roots = g5.select_roots(g, 12)
+    tickets = [sv.submit(0, int(r)) for r in roots]
+    queued = 0
+    for t, r in zip(tickets, roots):
+        assert sv.wait(t, 60.0)
+        pred, lat, q = sv.result(t)
+        queued += q > 0
+        want, _ = orc.bfs(ro, col, int(r))
+        assert np.array_equal(pred[:g.n], want)
+    sv.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_repeated_slot_reuse(graphs, mode):
+    g = graphs[0]
+    ro, col = g.csr()
+    sv = g5.Server([g], mem_budget=2 * (48 * g.n + g.nnz // 64 + (1 << 20)), mode=mode)
+    roots = g5.select_roots(g, 10)
+    for rep in range(3):
+        for r in roots:
+            t = sv.submit(0, int(r))
+            assert sv.wait(t, 60.0)
+            pred, _, _ = sv.result(t)
+            want, _ = orc.bfs(ro, col, int(r))
+            assert np.array_equal(pred[:g.n], want)
+    sv.close()
+
+
+def test_bad_queries(graphs):
+    sv = g5.Server(graphs[:1], mem_budget=1 << 26)
+    with pytest.raises(g5.G5Error):
+        sv.submit(0, graphs[0].n)
+    with pytest.raises(g5.G5Error):
+        sv.submit(5, 0)
+    sv.close()
