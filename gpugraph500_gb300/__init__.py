@@ -93,8 +93,9 @@ SIGNATURES = {
     "g5_batch_create": (_I, [_P, _I, C.POINTER(_P)]),
     "g5_batch_destroy": (_I, [_P]),
     "g5_batch_set_direction": (_I, [_P, C.c_double, C.c_double]),
-    "g5_batch_profile": (_I, [_P, _P, _P, _P, _P, _P, _I, C.POINTER(_I)]),
+    "g5_batch_profile": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _I, C.POINTER(_I)]),
     "g5_batch_run": (_I, [_P, _P, _P, _P, C.POINTER(C.c_double)]),
+    "g5_batch_root_parents": (_I, [_P, C.c_int64, _I, _I, _P, _P]),
     "g5_batch_serve_begin": (_I, [_P, _P, _P]),
     "g5_batch_serve_step": (_I, [_P, _P, _P, _P, _I, _P, _P, C.POINTER(C.c_double)]),
     "g5_bfs_launch": (_I, [_P, _I64]),
@@ -408,8 +409,19 @@ class GpuSimd:
         return res
 
 
+def batch_root_parents(pred_dev, n: int, nroots: int, r: int, dst_dev) -> None:
+    """dst[v] = pred[v * nroots + r]: one root's parents out of a vertex-major
+    batch array (device buffers with a data_ptr(), or raw device pointers)."""
+    _check(lib().g5_batch_root_parents(_ptr(pred_dev), n, nroots, r, _ptr(dst_dev), None),
+           "g5_batch_root_parents")
+
+
 class Batch:
-    """Batched BFS over up to 64 roots per graph in one level loop (g5_batch)."""
+    """Batched BFS over up to 64 roots per graph in one level loop (g5_batch).
+
+    Parents come out vertex-major per graph: graph g's block holds
+    n_g x nroots[g] uint32 entries, vertex v's parent for root j at
+    [v * nroots[g] + j]."""
 
     def __init__(self, graphs: Sequence[Graph]):
         self.graphs = list(graphs)
@@ -424,11 +436,17 @@ class Batch:
         nr = np.ascontiguousarray(nroots, dtype=np.int32)
         ms = np.zeros(5, np.float64)
         act = np.zeros(1024, np.int64)
+        lms = np.zeros(1024, np.float64)
+        lex = np.zeros(1024, np.int64)
+        ldir = np.zeros(1024, np.int32)
         lv = C.c_int()
         _check(lib().g5_batch_profile(self._h, _ptr(roots), _ptr(nr), _ptr(pred_out_dev), _ptr(ms), _ptr(act),
-                                      1024, C.byref(lv)), "g5_batch_profile")
+                                      _ptr(lms), _ptr(lex), _ptr(ldir), 1024, C.byref(lv)), "g5_batch_profile")
+        ex = lex[: lv.value]
         return {"kernel_ms": dict(zip(("count", "scan", "write", "expand", "fixup"), ms.tolist())),
-                "active": act[: lv.value].tolist()}
+                "active": act[: lv.value].tolist(), "expand_ms": lms[: lv.value].tolist(),
+                "examined": np.diff(ex, prepend=0).tolist(),
+                "dirs": ["".join(c for c, bit in (("T", 1), ("B", 2)) if d & bit) for d in ldir[: lv.value]]}
 
     def set_direction(self, alpha: float, beta: float) -> None:
         _check(lib().g5_batch_set_direction(self._h, alpha, beta), "g5_batch_set_direction")

@@ -49,7 +49,7 @@ struct GraphDesc {
     int64_t n;
     int64_t nnz;
     uint64_t vbase;      // first global vertex id
-    uint64_t pred_base;  // offset of root 0's parent array in pred_out
+    uint64_t pred_base;  // offset of vertex 0's parents in pred_out (nroots per vertex)
     uint64_t mask;       // one bit per root
     int32_t nroots;
     int32_t dir;         // direction for the current level
@@ -66,6 +66,8 @@ struct BState {
     uint64_t active;     // active vertices over all graphs (this level)
     uint64_t qlen;       // queue length (top-down graphs only)
     uint64_t qedges;     // its adjacency entries
+    uint64_t examined;   // adjacency entries examined, all levels
+    uint32_t dirs;       // this level: bit 0 a graph expands top-down, bit 1 bottom-up
 };
 
 struct BArgs {
@@ -78,7 +80,7 @@ struct BArgs {
     const uint32_t *heavy;  // one bit per global vertex of degree > 64
     const uint32_t *iso;    // one bit per global vertex of degree 0
     uint64_t *vis, *front, *next;
-    uint32_t *pred;         // output parents, root-major per graph
+    uint32_t *pred;         // output parents, vertex-major per graph: [v][nroots]
     uint32_t *queue;
     uint64_t *qoff;
     int64_t *qbase;
@@ -117,7 +119,7 @@ __global__ void k_binit(BArgs a)
                 continue;
             }
             atomicOr((unsigned long long *)&a.next[d.vbase + root], 1ull << r);
-            a.pred[d.pred_base + (uint64_t)r * d.n + root] = (uint32_t)root;
+            a.pred[d.pred_base + (uint64_t)root * d.nroots + r] = (uint32_t)root;
         }
         if (threadIdx.x == 0) {
             d.dir = TD;
@@ -130,6 +132,7 @@ __global__ void k_binit(BArgs a)
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.st->level = -1;
         a.st->err = 0;
+        a.st->examined = 0;
     }
 }
 
@@ -171,9 +174,8 @@ __device__ void bexp_td(const BArgs &a, uint64_t &examined)
                     const GraphDesc &d = a.gd[graph_of(a, ug)];
                     const uint32_t vl = __ldg(d.col + (a.qbase[i] + (int64_t)e));
                     const uint64_t vg = d.vbase + vl;
-                    // roots new to v: light vertices get their parents from
-                    // k_bfix (a short scan of their own adjacency), heavy ones
-                    // (degree > 64) by atomicMin here
+                    // roots new to v: the smallest frontier neighbour is the
+                    // parent (atomicMin, after a plain read to skip most)
                     const uint64_t nb = a.front[ug] & ~a.vis[vg];
                     if (nb) {
                         const uint32_t ul = (uint32_t)(ug - d.vbase);
@@ -181,7 +183,7 @@ __device__ void bexp_td(const BArgs &a, uint64_t &examined)
                         while (x) {
                             const int r = __ffsll((long long)x) - 1;
                             x &= x - 1;
-                            uint32_t *slot = a.pred + d.pred_base + (uint64_t)r * d.n + vl;
+                            uint32_t *slot = a.pred + d.pred_base + (uint64_t)vl * d.nroots + r;
                             if (*slot > ul) atomicMin(slot, ul);
                         }
                         if (nb & ~a.next[vg]) atomicOr((unsigned long long *)&a.next[vg], (unsigned long long)nb);
@@ -195,49 +197,59 @@ __device__ void bexp_td(const BArgs &a, uint64_t &examined)
     }
 }
 
-// BOTTOM_UP: candidates are the roots that have not visited v; FIXUP (after
-// a top-down level): the roots top-down just marked in next[v].  The first
-// frontier hit of each root along v's ascending adjacency is its parent.
-template <bool FIXUP>
-__device__ void bsweep(const BArgs &a, uint64_t &examined)
+// Bottom-up: the candidates of v are the roots that have not visited it;
+// the first frontier hit of each root along v's ascending adjacency is its
+// parent.  A warp takes 32 consecutive vertices (never two graphs: graphs
+// are chunk aligned).  Each lane first probes v's first kSerial entries with
+// independent loads and keeps the hits as (parent, roots) events in shared
+// memory; vertices still missing roots are then scanned by the whole warp,
+// 64 entries per step, whose first hits per root (an exclusive prefix OR over
+// the lanes) are written at once.  The serial hits are written last, lane r
+// taking root r of each vertex: each vertex's parents are one contiguous run
+// of nroots words, so those stores are contiguous.
+__global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
 {
-    const int lane = g5_lane();
+    __shared__ uint64_t s_evm[kW][kSerial][32];
+    __shared__ uint32_t s_evu[kW][kSerial][32];
+    if (a.st->err || a.st->level < 0 || a.st->active == 0) return;
+    const int lane = g5_lane(), wib = threadIdx.x >> 5;
     const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
-    // one warp per 32 consecutive vertices (never spans two chunks)
+    uint64_t examined = 0;
     for (uint64_t w = gw; w < a.ntot / 32; w += nw) {
         const uint64_t v = w * 32 + lane;
-        const int g = graph_of(a, w * 32);
-        const GraphDesc &d = a.gd[g];
-        if (d.dir != (FIXUP ? TD : BU) || d.nf == 0) continue;
+        const GraphDesc &d = a.gd[graph_of(a, w * 32)];
+        if (d.dir != BU || d.nf == 0) continue;
         const uint64_t vl = v - d.vbase;
-        const bool light = !((__ldg(a.heavy + (v >> 5)) >> lane) & 1u);
+        const uint32_t R = (uint32_t)d.nroots;
         const bool iso = (__ldg(a.iso + (v >> 5)) >> lane) & 1u;
         // roots with an empty frontier cannot reach v this level; vertices
         // without edges are never reached
-        uint64_t need = ((int64_t)vl < d.n && !iso) ? (FIXUP ? (light ? a.next[v] : 0ull) : (~a.vis[v] & d.amask)) : 0;
+        uint64_t need = ((int64_t)vl < d.n && !iso) ? (~a.vis[v] & d.amask) : 0;
         int64_t s = 0, e = 0;
         if (need) {
             s = d.row_off[vl];
             e = d.row_off[vl + 1];
         }
-        uint64_t found = 0;
+        // serial probes: all loads first, then the hits in adjacency order
+        uint32_t u[kSerial];
+        uint64_t f[kSerial];
+#pragma unroll
+        for (int k = 0; k < kSerial; ++k) u[k] = (need && s + k < e) ? __ldg(d.col + s + k) : 0xFFFFFFFFu;
+#pragma unroll
+        for (int k = 0; k < kSerial; ++k) f[k] = u[k] != 0xFFFFFFFFu ? a.front[d.vbase + u[k]] : 0ull;
+        uint64_t found = 0, sfound = 0;
         int64_t j = s;
-        const int64_t lim = min(e, s + kSerial);
-        for (; j < lim && need; ++j) {
-            const uint32_t u = __ldg(d.col + j);
-            const uint64_t hit = a.front[d.vbase + u] & need;
-            if (hit) {
-                uint64_t x = hit;
-                while (x) {
-                    const int r = __ffsll((long long)x) - 1;
-                    x &= x - 1;
-                    a.pred[d.pred_base + (uint64_t)r * d.n + vl] = u;
-                }
-                found |= hit;
-                need &= ~hit;
-            }
+#pragma unroll
+        for (int k = 0; k < kSerial; ++k) {
+            const uint64_t hit = f[k] & need;
+            s_evm[wib][k][lane] = hit;
+            s_evu[wib][k][lane] = u[k];
+            need &= ~hit;
+            sfound |= hit;
+            if (u[k] != 0xFFFFFFFFu && (need | hit)) j = s + k + 1;
         }
+        found = sfound;
         uint64_t ex = (uint64_t)(j - s);
         unsigned pend = __ballot_sync(0xFFFFFFFFu, need && j < e);
         while (pend) {
@@ -246,43 +258,42 @@ __device__ void bsweep(const BArgs &a, uint64_t &examined)
             int64_t jj = __shfl_sync(0xFFFFFFFFu, j, l);
             const int64_t ee = __shfl_sync(0xFFFFFFFFu, e, l);
             uint64_t nd = __shfl_sync(0xFFFFFFFFu, need, l);
-            const uint64_t vll = __shfl_sync(0xFFFFFFFFu, vl, l);
+            uint32_t *pv = a.pred + d.pred_base + (uint64_t)__shfl_sync(0xFFFFFFFFu, vl, l) * R;
             const int64_t st = jj;
             uint64_t fnd = 0;
             while (jj < ee && nd) {
-                const int64_t idx = jj + lane;
-                uint32_t u = 0;
-                uint64_t hit = 0;
-                if (idx < ee) {
-                    u = __ldg(d.col + idx);
-                    hit = a.front[d.vbase + u] & nd;
-                }
-                unsigned hm = __ballot_sync(0xFFFFFFFFu, hit != 0);
-                int last = 31;
-                while (hm) {
-                    const int f = __ffs(hm) - 1;
-                    hm &= hm - 1;
-                    const uint64_t hf = __shfl_sync(0xFFFFFFFFu, hit, f) & nd;
-                    if (hf) {
-                        const uint32_t uf = __shfl_sync(0xFFFFFFFFu, u, f);
-                        // lanes write the parent slots of the new roots in parallel
-                        uint64_t x = hf;
-                        int k = 0;
-                        while (x) {
-                            const int r = __ffsll((long long)x) - 1;
-                            x &= x - 1;
-                            if ((k & 31) == lane) a.pred[d.pred_base + (uint64_t)r * d.n + vll] = uf;
-                            ++k;
-                        }
-                        fnd |= hf;
-                        nd &= ~hf;
-                        if (!nd) {
-                            last = f;
-                            break;
-                        }
+                // two windows of 32 entries: loads of both first
+                const int64_t i0 = jj + lane, i1 = jj + 32 + lane;
+                const uint32_t u0 = i0 < ee ? __ldg(d.col + i0) : 0xFFFFFFFFu;
+                const uint32_t u1 = i1 < ee ? __ldg(d.col + i1) : 0xFFFFFFFFu;
+                const uint64_t h0 = u0 != 0xFFFFFFFFu ? a.front[d.vbase + u0] : 0ull;
+                const uint64_t h1 = u1 != 0xFFFFFFFFu ? a.front[d.vbase + u1] : 0ull;
+#pragma unroll
+                for (int half = 0; half < 2; ++half) {
+                    if (!nd) break;
+                    const uint64_t hit = (half ? h1 : h0) & nd;
+                    const uint32_t uu = half ? u1 : u0;
+                    // first lane of each root: exclusive prefix OR over the lanes
+                    uint64_t incl = hit;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint64_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                        if (lane >= o) incl |= y;
                     }
+                    uint64_t excl = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
+                    if (lane == 0) excl = 0;
+                    uint64_t x = hit & ~excl;
+                    while (x) {
+                        const int r = __ffsll((long long)x) - 1;
+                        x &= x - 1;
+                        pv[r] = uu;
+                    }
+                    const uint64_t all = __shfl_sync(0xFFFFFFFFu, incl, 31);
+                    const unsigned cov = __ballot_sync(0xFFFFFFFFu, (incl & nd) == nd);
+                    fnd |= all;
+                    nd &= ~all;
+                    jj += nd ? 32 : __ffs(cov);
                 }
-                jj += nd ? 32 : last + 1;
             }
             jj = min(jj, ee);
             if (lane == l) {
@@ -291,34 +302,39 @@ __device__ void bsweep(const BArgs &a, uint64_t &examined)
                 ex += (uint64_t)(jj - st);
             }
         }
-        if (!FIXUP && found) atomicOr((unsigned long long *)&a.next[v], (unsigned long long)found);
-        if (FIXUP && need) atomicOr(&a.st->err, 16u);  // cannot happen on a symmetric CSR
+        __syncwarp();
+        // serial hits: lane r takes root r (and r + 32) of each vertex
+        unsigned vm = __ballot_sync(0xFFFFFFFFu, sfound != 0);
+        while (vm) {
+            const int vi = __ffs(vm) - 1;
+            vm &= vm - 1;
+            const uint64_t sf = __shfl_sync(0xFFFFFFFFu, sfound, vi);
+            uint32_t *pv = a.pred + d.pred_base + (v - lane + vi - d.vbase) * R;
+            for (uint32_t r = lane; r < R; r += 32) {
+                if (!((sf >> r) & 1ull)) continue;
+                uint32_t p = 0;
+#pragma unroll
+                for (int k = kSerial - 1; k >= 0; --k)
+                    if ((s_evm[wib][k][vi] >> r) & 1ull) p = s_evu[wib][k][vi];
+                pv[r] = p;
+            }
+        }
+        __syncwarp();
+        if (found) a.next[v] |= found;  // only this lane writes v in a bottom-up level
         examined += ex;
     }
+    examined = wsum(examined);
+    if (lane == 0 && examined) atomicAdd((unsigned long long *)&a.st->examined, (unsigned long long)examined);
 }
 
-// Top-down part of a level (graphs expanding top-down) and bottom-up part
-// (graphs expanding bottom-up): two kernels so each gets its own registers.
+// Top-down part of a level (graphs expanding top-down).
 __global__ void __launch_bounds__(kB, 8) k_btd(BArgs a)
 {
     if (a.st->err || a.st->level < 0 || a.st->active == 0 || a.st->qedges == 0) return;
     uint64_t ex = 0;
     bexp_td(a, ex);
-}
-
-__global__ void __launch_bounds__(kB, 6) k_bbu(BArgs a)
-{
-    if (a.st->err || a.st->level < 0 || a.st->active == 0) return;
-    uint64_t ex = 0;
-    bsweep<false>(a, ex);
-}
-
-__global__ void __launch_bounds__(kB) k_bfix(BArgs a)
-{
-    if (a.st->err || a.st->level < 0 || a.st->active == 0) return;
-    uint64_t ex = 0;
-    bsweep<true>(a, ex);
-    (void)ex;
+    ex = wsum(ex);
+    if (g5_lane() == 0 && ex) atomicAdd((unsigned long long *)&a.st->examined, (unsigned long long)ex);
 }
 
 // ---- compaction ---------------------------------------------------------------------------
@@ -372,6 +388,7 @@ __global__ void __launch_bounds__(1024) k_bscan(BArgs a)
         s_gn[g] = 0;
         s_gm[g] = 0;
     }
+    if (threadIdx.x == 0) a.st->dirs = 0;
     __syncthreads();
     const uint32_t C = a.nchunks;
     {
@@ -421,6 +438,7 @@ __global__ void __launch_bounds__(1024) k_bscan(BArgs a)
         d.amask = d.amask_next & d.mask;
         d.amask_next = 0;
         s_gdir[threadIdx.x] = nd;
+        if (tn) atomicOr(&a.st->dirs, nd == TD ? 1u : 2u);
     }
     __syncthreads();
     // exclusive prefix over chunks of top-down graphs
@@ -576,20 +594,40 @@ __global__ void k_sadmit(BArgs a, const Admit *adm, int nadm)
         const Admit x = adm[i];
         const GraphDesc &d = a.gd[x.graph];
         atomicOr((unsigned long long *)&a.next[d.vbase + x.root], 1ull << x.slot);
-        a.pred[d.pred_base + (uint64_t)x.slot * d.n + x.root] = (uint32_t)x.root;
+        a.pred[d.pred_base + (uint64_t)x.root * d.nroots + x.slot] = (uint32_t)x.root;
     }
 }
 
 __global__ void k_sclear(BArgs a, const uint64_t *clear_mask)
 {
+    // a retired slot's visited vertices get their parent entry back to
+    // 0xFFFFFFFF: every entry of a free slot is unvisited again
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < a.ntot;
          v += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t m = clear_mask[graph_of(a, v)];
+        const int g = graph_of(a, v);
+        const uint64_t m = clear_mask[g];
         if (m) {
             const uint64_t x = a.vis[v];
-            if (x & m) a.vis[v] = x & ~m;
+            if (x & m) {
+                a.vis[v] = x & ~m;
+                const GraphDesc &d = a.gd[g];
+                uint32_t *p = a.pred + d.pred_base + (v - d.vbase) * d.nroots;
+                uint64_t y = x & m;
+                while (y) {
+                    const int r = __ffsll((long long)y) - 1;
+                    y &= y - 1;
+                    p[r] = 0xFFFFFFFFu;
+                }
+            }
         }
     }
+}
+
+// One root's parents out of the vertex-major array: dst[v] = pred[v * R + r].
+__global__ void k_gather_root(const uint32_t *pred, uint32_t R, uint32_t r, int64_t n, uint32_t *dst)
+{
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        dst[v] = pred[(uint64_t)v * R + r];
 }
 
 __global__ void k_bdeg(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t ntot, uint32_t *deg,
@@ -668,7 +706,7 @@ void enqueue_batch(g5_batch *b, const BArgs &a, cudaStream_t s, bool body, std::
     k_bwrite<<<a.nchunks, kB, 0, s>>>(a);
     mark();
     k_btd<<<g5::grid_for(8), kB, 0, s>>>(a);
-    k_bbu<<<g5::grid_for(8), kB, 0, s>>>(a);
+    k_bbu<<<g5::grid_for(4), kB, 0, s>>>(a);
     mark();
     mark();
 }
@@ -843,7 +881,9 @@ g5_status g5_batch_set_direction(g5_batch *b, double alpha, double beta)
 }
 
 g5_status g5_batch_profile(g5_batch *b, const int64_t *roots_host, const int *nroots, uint32_t *pred_out_dev,
-                           double *kernel_ms, int64_t *level_active, int max_levels, int *levels)
+                           double *kernel_ms, int64_t *level_active, double *level_expand_ms, int64_t *level_examined, int32_t *level_dirs,
+                           int max_levels,
+                           int *levels)
 {
     // host-driven level loop with CUDA events around every launch: kernel_ms
     // gets count, scan, write, expand, fixup totals (ms); level_active the
@@ -884,7 +924,10 @@ g5_status g5_batch_profile(g5_batch *b, const int64_t *roots_host, const int *nr
             float t = 0;
             cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
             kernel_ms[k] += t;
+            if (k == 3 && level_expand_ms && L < max_levels) level_expand_ms[L] = t;
         }
+        if (level_examined && L < max_levels) level_examined[L] = (int64_t)b->h_st->examined;
+        if (level_dirs && L < max_levels) level_dirs[L] = (int32_t)b->h_st->dirs;
         for (cudaEvent_t e : ev) cudaEventDestroy(e);
         if (level_active && L < max_levels) level_active[L] = (int64_t)b->h_st->active;
         if (b->h_st->active == 0 || b->h_st->err) break;
@@ -919,6 +962,9 @@ g5_status g5_batch_serve_begin(g5_batch *b, uint32_t *pred_dev, const int *slots
     if (!b->adm_host) G5_CUDA(cudaMallocHost(&b->adm_host, sizeof(Admit) * 64 * ng + sizeof(uint64_t) * ng));
     G5_CUDA(cudaMemcpyAsync(b->gd, b->hgd.data(), sizeof(GraphDesc) * ng, cudaMemcpyHostToDevice, s));
     G5_CUDA(cudaMemsetAsync(b->words, 0, sizeof(uint64_t) * 3 * b->args.ntot, s));
+    // every entry starts unvisited; a retired slot's entries are reset by
+    // k_sclear, so an admitted root always starts from a clean column
+    if (pb) G5_CUDA(cudaMemsetAsync(pred_dev, 0xFF, sizeof(uint32_t) * pb, s));
     BState z;
     memset(&z, 0, sizeof z);
     z.level = 0;
@@ -964,11 +1010,6 @@ g5_status g5_batch_serve_step(g5_batch *b, const int32_t *adm_graph, const int32
                                 cudaMemcpyHostToDevice, s));
     }
     if (any_retire) k_sclear<<<g5::grid_for(8), kB, 0, s>>>(b->args, rd);
-    for (int i = 0; i < nadm; ++i) {
-        const GraphDesc &d = b->hgd[ah[i].graph];
-        G5_CUDA(cudaMemsetAsync(b->args.pred + d.pred_base + (uint64_t)ah[i].slot * d.n, 0xFF,
-                                sizeof(uint32_t) * (size_t)d.n, s));
-    }
     if (nadm) k_sadmit<<<1, 128, 0, s>>>(b->args, ad, nadm);
     enqueue_batch(b, b->args, s, true);
     G5_CUDA(cudaEventRecord(b->ev1, s));
@@ -984,6 +1025,18 @@ g5_status g5_batch_serve_step(g5_batch *b, const int32_t *adm_graph, const int32
         *device_ms = ms;
     }
     return b->h_st->err ? G5_ERR_CAPACITY : G5_OK;
+}
+
+g5_status g5_batch_root_parents(const uint32_t *pred_dev, int64_t n, int nroots, int r, uint32_t *dst_dev,
+                                void *stream)
+{
+    if (!pred_dev || !dst_dev || n < 0 || nroots < 1 || nroots > 64 || r < 0 || r >= nroots)
+        return G5_ERR_INVALID_ARG;
+    if (n == 0) return G5_OK;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)g5::grid_for(8));
+    k_gather_root<<<blocks, 256, 0, s>>>(pred_dev, (uint32_t)nroots, (uint32_t)r, n, dst_dev);
+    return cudaGetLastError() == cudaSuccess ? G5_OK : G5_ERR_CUDA;
 }
 
 g5_status g5_batch_destroy(g5_batch *b)

@@ -385,11 +385,18 @@ g5_status g5_server_result(g5_server *sv, uint64_t ticket, int64_t *pred_host, d
     } else if (q.state == 2 && pred_host) {
         const int64_t n = sv->graphs[q.graph]->n;
         std::vector<uint32_t> tmp((size_t)n);
-        const uint32_t *src = sv->pred + sv->pred_base[q.graph] + (uint64_t)q.slot * (uint64_t)n;
+        const uint32_t *src = sv->pred + sv->pred_base[q.graph];
+        const int R = sv->slots[q.graph];
         lk.unlock();
-        // the slot is not reused before it is released below
-        if (cudaMemcpy(tmp.data(), src, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
-            return G5_ERR_CUDA;
+        // the slot is not reused before it is released below; its column is
+        // gathered out of the vertex-major array first
+        uint32_t *col = nullptr;
+        if (cudaMalloc(&col, sizeof(uint32_t) * (size_t)std::max<int64_t>(n, 1)) != cudaSuccess) return G5_ERR_OOM;
+        g5_status gs = g5_batch_root_parents(src, n, R, q.slot, col, nullptr);
+        if (gs == G5_OK && cudaMemcpy(tmp.data(), col, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
+            gs = G5_ERR_CUDA;
+        cudaFree(col);
+        if (gs != G5_OK) return gs;
         for (int64_t v = 0; v < n; ++v) pred_host[v] = tmp[v] == 0xFFFFFFFFu ? -1 : (int64_t)tmp[v];
         lk.lock();
     }

@@ -213,10 +213,14 @@ g5_status g5_batch_destroy(g5_batch *bt);
 /* The same search as g5_batch_run with a host-driven level loop and CUDA
  * events around every launch (for profiling): kernel_ms[5] receives the
  * total ms of the count, scan, write, expand and fix-up kernels;
- * level_active (nullable, max_levels entries) the active vertices per level;
+ * level_active, level_expand_ms, level_examined and level_dirs (nullable,
+ * max_levels entries) the active vertices, the expansion ms, the adjacency
+ * entries examined so far (cumulative) and the directions (bit 0 some graph
+ * top-down, bit 1 some graph bottom-up) of each level;
  * *levels the levels run. */
 g5_status g5_batch_profile(g5_batch *bt, const int64_t *roots_host, const int *nroots,
                            uint32_t *pred_out_dev, double *kernel_ms, int64_t *level_active,
+                           double *level_expand_ms, int64_t *level_examined, int32_t *level_dirs,
                            int max_levels, int *levels);
 
 /* Direction-switch thresholds of the batched search (defaults 14 and 24),
@@ -225,15 +229,24 @@ g5_status g5_batch_set_direction(g5_batch *bt, double alpha, double beta);
 
 /* Runs nroots[i] (<= 64) roots on graph i, all graphs in one level loop.
  * roots holds the roots of graph 0, then graph 1, ...  Parents are written
- * as uint32 (0xFFFFFFFF unvisited, root -> root) to pred_out (device) in
- * root-major order: graph 0 root 0 (n0 entries), root 1, ... then graph 1.
+ * as uint32 (0xFFFFFFFF unvisited, root -> root) to pred_out (device),
+ * vertex-major per graph: graph 0 occupies n0 x nroots[0] entries, the
+ * parent of vertex v for root j at [v * nroots[0] + j]; graph 1 follows.
+ * (Each vertex's parents are contiguous, so a level's writes are
+ * contiguous per warp.)  g5_batch_root_parents extracts one root's array.
  * Same parent choice as g5_bfs_run. */
 g5_status g5_batch_run(g5_batch *bt, const int64_t *roots_host, const int *nroots,
                        uint32_t *pred_out_dev, double *device_ms);
 
+/* One root's parents out of a vertex-major batch array of n vertices and
+ * nroots parents per vertex: dst[v] = pred[v * nroots + r] (device arrays,
+ * stream may be NULL). */
+g5_status g5_batch_root_parents(const uint32_t *pred_dev, int64_t n, int nroots, int r, uint32_t *dst_dev,
+                                void *stream);
+
 /* Continuous batching on a batch workspace (used by the server below).
  * serve_begin gives graph g `slots[g]` (<= 64) root slots whose uint32
- * parents live in pred_dev, root-major per graph.  Each serve_step clears the
+ * parents live in pred_dev, vertex-major per graph (slots[g] per vertex).  Each serve_step clears the
  * visited bits of the slots in retire_mask[g], starts the admitted roots
  * (adm_graph/adm_slot/adm_root, nadm entries) in their slots and runs one
  * level of every graph; active_mask[g] receives the slots whose frontier was

@@ -26,9 +26,10 @@ def check_batch(graphs, csrs, roots_per_graph):
     got = out.cpu().numpy().view(np.uint32)
     off = 0
     for g, (ro, col), rs in zip(graphs, csrs, roots_per_graph):
-        for r in rs:
-            assert np.array_equal(got[off:off + g.n], oracle_u32(ro, col, r)), r
-            off += g.n
+        block = got[off:off + g.n * len(rs)].reshape(g.n, len(rs))  # vertex-major
+        for j, r in enumerate(rs):
+            assert np.array_equal(block[:, j], oracle_u32(ro, col, r)), r
+        off += g.n * len(rs)
     return bt
 
 
@@ -61,6 +62,22 @@ def test_hand_graph_and_duplicate_roots():
     roots = [0, 20, 40, 50, 60, 65, 0]
     check_batch([g], [(ro, col)], [roots]).close()
     g.close()
+
+
+def test_root_parents_extraction():
+    g = g5.Graph.kronecker(11)
+    ro, col = g.csr()
+    roots = g5.select_roots(g, 9)
+    bt = check_batch([g], [(ro, col)], [roots])
+    out = torch.empty(9 * g.n, dtype=torch.int32, device="cuda")
+    bt.run(np.asarray(roots, np.int64), [9], out)
+    dst = torch.empty(g.n, dtype=torch.int32, device="cuda")
+    for j, r in enumerate(roots):
+        g5.batch_root_parents(out, g.n, 9, j, dst)
+        assert np.array_equal(dst.cpu().numpy().view(np.uint32), oracle_u32(ro, col, r))
+    with pytest.raises(g5.G5Error):
+        g5.batch_root_parents(out, g.n, 9, 9, dst)
+    bt.close(); g.close()
 
 
 def test_invalid_roots_rejected():
