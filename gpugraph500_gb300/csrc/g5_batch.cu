@@ -20,9 +20,21 @@
 // Both give every root the smallest previous-level neighbour as parent, the
 // same parent as the plain search and the reference CPU BFS.
 //
+// The search runs on a copy of each graph whose vertices are numbered by
+// descending degree: the few high-degree vertices, which most adjacency
+// entries point at, then share a small range of the frontier array that stays
+// in L2 while the bottom-up levels probe it at random.  Each row keeps its
+// neighbours in original-id order, so the first hit along a row is still the
+// smallest original id; parents and roots are translated at the boundary and
+// the output is indexed by original ids.  The bottom-up sweep itself walks
+// the vertices in original-id order, which spreads the long rows over the
+// warps.
+//
 // Vertex ranges of the graphs are padded to whole compaction chunks so every
 // chunk belongs to one graph; the level loop is one CUDA graph (conditional
 // while node) like the plain search.
+#include <cub/cub.cuh>
+
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -44,8 +56,10 @@ constexpr int kMaxLevels = 1024;
 enum : int32_t { TD = 0, BU = 1 };
 
 struct GraphDesc {
-    const int64_t *row_off;
-    const uint32_t *col;
+    const int64_t *row_off;  // degree-ordered copy: rows by new id
+    const uint32_t *col;     // new ids, each row in original-id order
+    const uint32_t *orig;    // new id -> original id
+    const uint32_t *perm;    // original id -> new id
     int64_t n;
     int64_t nnz;
     uint64_t vbase;      // first global vertex id
@@ -79,6 +93,7 @@ struct BArgs {
     const uint32_t *deg;    // per global vertex
     const uint32_t *heavy;  // one bit per global vertex of degree > 64
     const uint32_t *iso;    // one bit per global vertex of degree 0
+    const uint32_t *iso0;   // the same bits in original-id order
     uint64_t *vis, *front, *next;
     uint32_t *pred;         // output parents, vertex-major per graph: [v][nroots]
     uint32_t *queue;
@@ -118,7 +133,7 @@ __global__ void k_binit(BArgs a)
                 atomicOr(&a.st->err, 1u);
                 continue;
             }
-            atomicOr((unsigned long long *)&a.next[d.vbase + root], 1ull << r);
+            atomicOr((unsigned long long *)&a.next[d.vbase + d.perm[root]], 1ull << r);
             a.pred[d.pred_base + (uint64_t)root * d.nroots + r] = (uint32_t)root;
         }
         if (threadIdx.x == 0) {
@@ -178,12 +193,13 @@ __device__ void bexp_td(const BArgs &a, uint64_t &examined)
                     // parent (atomicMin, after a plain read to skip most)
                     const uint64_t nb = a.front[ug] & ~a.vis[vg];
                     if (nb) {
-                        const uint32_t ul = (uint32_t)(ug - d.vbase);
+                        const uint32_t ul = __ldg(d.orig + (ug - d.vbase));
+                        uint32_t *pv = a.pred + d.pred_base + (uint64_t)__ldg(d.orig + vl) * d.nroots;
                         uint64_t x = nb;
                         while (x) {
                             const int r = __ffsll((long long)x) - 1;
                             x &= x - 1;
-                            uint32_t *slot = a.pred + d.pred_base + (uint64_t)vl * d.nroots + r;
+                            uint32_t *slot = pv + r;
                             if (*slot > ul) atomicMin(slot, ul);
                         }
                         if (nb & ~a.next[vg]) atomicOr((unsigned long long *)&a.next[vg], (unsigned long long)nb);
@@ -217,15 +233,20 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
     const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
     uint64_t examined = 0;
     for (uint64_t w = gw; w < a.ntot / 32; w += nw) {
-        const uint64_t v = w * 32 + lane;
+        // vertices in original-id order: high-degree vertices, which have
+        // the lowest new ids, spread over the warps
+        const uint64_t go = w * 32 + lane;
         const GraphDesc &d = a.gd[graph_of(a, w * 32)];
         if (d.dir != BU || d.nf == 0) continue;
-        const uint64_t vl = v - d.vbase;
+        const uint64_t ol = go - d.vbase;
         const uint32_t R = (uint32_t)d.nroots;
-        const bool iso = (__ldg(a.iso + (v >> 5)) >> lane) & 1u;
+        const bool iso = (__ldg(a.iso0 + (go >> 5)) >> lane) & 1u;
+        const bool real = (int64_t)ol < d.n && !iso;
+        const uint64_t vl = real ? __ldg(d.perm + ol) : 0;
+        const uint64_t v = d.vbase + vl;
         // roots with an empty frontier cannot reach v this level; vertices
         // without edges are never reached
-        uint64_t need = ((int64_t)vl < d.n && !iso) ? (~a.vis[v] & d.amask) : 0;
+        uint64_t need = real ? (~a.vis[v] & d.amask) : 0;
         int64_t s = 0, e = 0;
         if (need) {
             s = d.row_off[vl];
@@ -244,13 +265,96 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
         for (int k = 0; k < kSerial; ++k) {
             const uint64_t hit = f[k] & need;
             s_evm[wib][k][lane] = hit;
-            s_evu[wib][k][lane] = u[k];
+            if (hit) s_evu[wib][k][lane] = __ldg(d.orig + u[k]);
             need &= ~hit;
             sfound |= hit;
             if (u[k] != 0xFFFFFFFFu && (need | hit)) j = s + k + 1;
         }
         found = sfound;
+        const uint32_t vo = (uint32_t)ol;  // original id of v: its parents' row
         uint64_t ex = (uint64_t)(j - s);
+        // short rows: pending vertices with at most 64 entries left are
+        // packed whole, in lane order, into windows of 64 slots (slots lane
+        // and lane + 32); each root's first hit in a row is found with a
+        // segmented prefix OR over the slots
+        while (true) {
+            const bool sh = need && j < e && e - j <= 64;
+            if (!__ballot_sync(0xFFFFFFFFu, sh)) break;
+            const uint32_t r = sh ? (uint32_t)(e - j) : 0u;
+            uint32_t inc = r;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+                if (lane >= o) inc += y;
+            }
+            const uint32_t start = inc - r;
+            const bool in = sh && inc <= 64;  // row fits in this window
+            uint32_t uq[2], s0q[2];
+            uint64_t hq[2], vq[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const uint32_t k = (uint32_t)lane + 32u * q;
+                // owner of slot k: the last lane whose row starts at or before k
+                int ow = 0;
+#pragma unroll
+                for (int step = 16; step; step >>= 1) {
+                    const uint32_t sv = __shfl_sync(0xFFFFFFFFu, start, ow + step);
+                    if (sv <= k) ow += step;
+                }
+                const uint32_t s0 = __shfl_sync(0xFFFFFFFFu, start, ow);
+                const uint32_t ro = __shfl_sync(0xFFFFFFFFu, in ? r : 0u, ow);
+                const int64_t jo = __shfl_sync(0xFFFFFFFFu, j, ow);
+                const uint64_t no = __shfl_sync(0xFFFFFFFFu, need, ow);
+                vq[q] = __shfl_sync(0xFFFFFFFFu, (uint64_t)vo, ow);
+                s0q[q] = s0;
+                const bool live = k < s0 + ro;
+                uq[q] = live ? __ldg(d.col + jo + (int64_t)(k - s0)) : 0xFFFFFFFFu;
+                hq[q] = no;
+            }
+#pragma unroll
+            for (int q = 0; q < 2; ++q) hq[q] = uq[q] != 0xFFFFFFFFu ? (a.front[d.vbase + uq[q]] & hq[q]) : 0ull;
+            // segmented inclusive prefix OR: slots 0..31, then 32..63 with
+            // the carry of a row that crosses slot 32
+            uint64_t ia = hq[0], ib = hq[1];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t ya = __shfl_up_sync(0xFFFFFFFFu, ia, o);
+                const uint64_t yb = __shfl_up_sync(0xFFFFFFFFu, ib, o);
+                if (lane >= o && (uint32_t)lane - o >= s0q[0]) ia |= ya;
+                if (lane >= o && (uint32_t)lane + 32u - o >= s0q[1]) ib |= yb;
+            }
+            const uint64_t ca = __shfl_sync(0xFFFFFFFFu, ia, 31);
+            if (s0q[1] < 32) ib |= ca;
+            const uint64_t pa = __shfl_up_sync(0xFFFFFFFFu, ia, 1);
+            const uint64_t pb = __shfl_up_sync(0xFFFFFFFFu, ib, 1);
+            const uint64_t ea = (uint32_t)lane > s0q[0] ? pa : 0ull;
+            const uint64_t eb = (uint32_t)lane + 32u > s0q[1] ? (lane ? pb : ca) : 0ull;
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                uint64_t x = hq[q] & ~(q ? eb : ea);
+                if (x) {
+                    uint32_t *pv = a.pred + d.pred_base + vq[q] * R;
+                    const uint32_t uo = __ldg(d.orig + uq[q]);
+                    while (x) {
+                        const int rr = __ffsll((long long)x) - 1;
+                        x &= x - 1;
+                        pv[rr] = uo;
+                    }
+                }
+            }
+            // each packed row takes its total from its last slot
+            const uint32_t lk = in ? start + r - 1 : 0u;
+            const uint64_t ta = __shfl_sync(0xFFFFFFFFu, ia, (int)(lk & 31));
+            const uint64_t tb = __shfl_sync(0xFFFFFFFFu, ib, (int)(lk & 31));
+            if (in) {
+                const uint64_t seg = lk < 32 ? ta : tb;
+                need &= ~seg;
+                found |= seg;
+                ex += r;
+                j = e;
+            }
+        }
+        // long rows: one vertex at a time, four windows of 32 entries per step
         unsigned pend = __ballot_sync(0xFFFFFFFFu, need && j < e);
         while (pend) {
             const int l = __ffs(pend) - 1;
@@ -258,21 +362,23 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
             int64_t jj = __shfl_sync(0xFFFFFFFFu, j, l);
             const int64_t ee = __shfl_sync(0xFFFFFFFFu, e, l);
             uint64_t nd = __shfl_sync(0xFFFFFFFFu, need, l);
-            uint32_t *pv = a.pred + d.pred_base + (uint64_t)__shfl_sync(0xFFFFFFFFu, vl, l) * R;
+            uint32_t *pv = a.pred + d.pred_base + (uint64_t)__shfl_sync(0xFFFFFFFFu, vo, l) * R;
             const int64_t st = jj;
             uint64_t fnd = 0;
             while (jj < ee && nd) {
-                // two windows of 32 entries: loads of both first
-                const int64_t i0 = jj + lane, i1 = jj + 32 + lane;
-                const uint32_t u0 = i0 < ee ? __ldg(d.col + i0) : 0xFFFFFFFFu;
-                const uint32_t u1 = i1 < ee ? __ldg(d.col + i1) : 0xFFFFFFFFu;
-                const uint64_t h0 = u0 != 0xFFFFFFFFu ? a.front[d.vbase + u0] : 0ull;
-                const uint64_t h1 = u1 != 0xFFFFFFFFu ? a.front[d.vbase + u1] : 0ull;
+                uint32_t uw[4];
+                uint64_t hw[4];
 #pragma unroll
-                for (int half = 0; half < 2; ++half) {
+                for (int q = 0; q < 4; ++q) {
+                    const int64_t i = jj + 32 * q + lane;
+                    uw[q] = i < ee ? __ldg(d.col + i) : 0xFFFFFFFFu;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) hw[q] = uw[q] != 0xFFFFFFFFu ? a.front[d.vbase + uw[q]] : 0ull;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
                     if (!nd) break;
-                    const uint64_t hit = (half ? h1 : h0) & nd;
-                    const uint32_t uu = half ? u1 : u0;
+                    const uint64_t hit = hw[q] & nd;
                     // first lane of each root: exclusive prefix OR over the lanes
                     uint64_t incl = hit;
 #pragma unroll
@@ -283,10 +389,13 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
                     uint64_t excl = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
                     if (lane == 0) excl = 0;
                     uint64_t x = hit & ~excl;
-                    while (x) {
-                        const int r = __ffsll((long long)x) - 1;
-                        x &= x - 1;
-                        pv[r] = uu;
+                    if (x) {
+                        const uint32_t uo = __ldg(d.orig + uw[q]);
+                        while (x) {
+                            const int rr = __ffsll((long long)x) - 1;
+                            x &= x - 1;
+                            pv[rr] = uo;
+                        }
                     }
                     const uint64_t all = __shfl_sync(0xFFFFFFFFu, incl, 31);
                     const unsigned cov = __ballot_sync(0xFFFFFFFFu, (incl & nd) == nd);
@@ -309,7 +418,7 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
             const int vi = __ffs(vm) - 1;
             vm &= vm - 1;
             const uint64_t sf = __shfl_sync(0xFFFFFFFFu, sfound, vi);
-            uint32_t *pv = a.pred + d.pred_base + (v - lane + vi - d.vbase) * R;
+            uint32_t *pv = a.pred + d.pred_base + (uint64_t)__shfl_sync(0xFFFFFFFFu, vo, vi) * R;
             for (uint32_t r = lane; r < R; r += 32) {
                 if (!((sf >> r) & 1ull)) continue;
                 uint32_t p = 0;
@@ -593,7 +702,7 @@ __global__ void k_sadmit(BArgs a, const Admit *adm, int nadm)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nadm; i += gridDim.x * blockDim.x) {
         const Admit x = adm[i];
         const GraphDesc &d = a.gd[x.graph];
-        atomicOr((unsigned long long *)&a.next[d.vbase + x.root], 1ull << x.slot);
+        atomicOr((unsigned long long *)&a.next[d.vbase + d.perm[x.root]], 1ull << x.slot);
         a.pred[d.pred_base + (uint64_t)x.root * d.nroots + x.slot] = (uint32_t)x.root;
     }
 }
@@ -611,7 +720,7 @@ __global__ void k_sclear(BArgs a, const uint64_t *clear_mask)
             if (x & m) {
                 a.vis[v] = x & ~m;
                 const GraphDesc &d = a.gd[g];
-                uint32_t *p = a.pred + d.pred_base + (v - d.vbase) * d.nroots;
+                uint32_t *p = a.pred + d.pred_base + (uint64_t)d.orig[v - d.vbase] * d.nroots;
                 uint64_t y = x & m;
                 while (y) {
                     const int r = __ffsll((long long)y) - 1;
@@ -648,6 +757,56 @@ __global__ void k_bdeg(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t
     }
 }
 
+// iso0: degree-0 bits in original-id order (padding vertices count as isolated)
+__global__ void k_biso0(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t ntot, const uint32_t *deg,
+                        uint32_t *iso0)
+{
+    for (uint64_t go = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; go < ntot;
+         go += (uint64_t)gridDim.x * blockDim.x) {
+        const GraphDesc &d = gd[chunk_graph[go / kChunk]];
+        const int64_t ol = (int64_t)(go - d.vbase);
+        const bool z = ol >= d.n || deg[d.vbase + d.perm[ol]] == 0u;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, z);
+        if ((threadIdx.x & 31) == 0) iso0[go >> 5] = m;
+    }
+}
+
+// ---- degree-ordered copy of a graph ----------------------------------------------------
+
+__global__ void k_rl_deg(const int64_t *row_off, int64_t n, uint32_t *deg, uint32_t *ids)
+{
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        deg[v] = (uint32_t)(row_off[v + 1] - row_off[v]);
+        ids[v] = (uint32_t)v;
+    }
+}
+
+// perm[orig[p]] = p; row2[p] = degree of new vertex p (scanned into offsets)
+__global__ void k_rl_perm(const uint32_t *orig, const uint32_t *deg_sorted, int64_t n, uint32_t *perm, int64_t *row2)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p <= n; p += (int64_t)gridDim.x * blockDim.x) {
+        if (p < n) {
+            perm[orig[p]] = (uint32_t)p;
+            row2[p] = deg_sorted[p];
+        } else {
+            row2[n] = 0;
+        }
+    }
+}
+
+// one warp per new row: the original row, neighbours renamed, order kept
+__global__ void k_rl_cols(const int64_t *row_off, const uint32_t *col, const uint32_t *orig, const uint32_t *perm,
+                          const int64_t *row2, int64_t n, uint32_t *col2)
+{
+    const int lane = g5_lane();
+    for (int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < n;
+         p += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const uint32_t o = orig[p];
+        const int64_t s = row_off[o], len = row_off[o + 1] - s, d0 = row2[p];
+        for (int64_t k = lane; k < len; k += 32) col2[d0 + k] = perm[col[s + k]];
+    }
+}
+
 }  // namespace
 
 struct g5_batch {
@@ -660,6 +819,7 @@ struct g5_batch {
     uint32_t *deg = nullptr;
     uint32_t *heavy = nullptr;
     uint32_t *iso = nullptr;
+    uint32_t *iso0 = nullptr;
     uint64_t *words = nullptr;  // vis | front | next
     uint32_t *queue = nullptr;
     uint64_t *qoff = nullptr;
@@ -679,6 +839,7 @@ struct g5_batch {
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<void *> owned;        // degree-ordered graph copies
 };
 
 namespace {
@@ -758,6 +919,7 @@ void free_batch(g5_batch *b)
     cudaFree(b->deg);
     cudaFree(b->heavy);
     cudaFree(b->iso);
+    cudaFree(b->iso0);
     cudaFree(b->words);
     cudaFree(b->queue);
     cudaFree(b->qoff);
@@ -775,7 +937,51 @@ void free_batch(g5_batch *b)
     cudaFreeHost(b->h_st);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
+    for (void *p : b->owned) cudaFree(p);
+    b->owned.clear();
     if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+// Degree-ordered copy of g on b's stream: new ids by descending degree (ties
+// by original id), rows in new-id order, each row's neighbours renamed but in
+// their original order.
+g5_status build_relabel(g5_batch *b, const g5_graph *g, GraphDesc &d)
+{
+    const int64_t n = g->n, nnz = g->nnz;
+    cudaStream_t s = b->stream;
+    auto alloc = [&](void **p, size_t bytes) -> bool {
+        if (cudaMalloc(p, bytes ? bytes : 16) != cudaSuccess) return false;
+        b->owned.push_back(*p);
+        return true;
+    };
+    uint32_t *orig = nullptr, *perm = nullptr, *col2 = nullptr;
+    int64_t *row2 = nullptr;
+    if (!alloc((void **)&orig, sizeof(uint32_t) * n) || !alloc((void **)&perm, sizeof(uint32_t) * n) ||
+        !alloc((void **)&row2, sizeof(int64_t) * (n + 1)) || !alloc((void **)&col2, sizeof(uint32_t) * nnz))
+        return G5_ERR_OOM;
+    d.orig = orig;
+    d.perm = perm;
+    d.row_off = row2;
+    d.col = col2;
+    if (n == 0) {
+        G5_CUDA(cudaMemsetAsync(row2, 0, sizeof(int64_t), s));
+        return G5_OK;
+    }
+    g5::DevBuf<uint32_t> deg, ids, deg_sorted;
+    if (deg.alloc(n) != G5_OK || ids.alloc(n) != G5_OK || deg_sorted.alloc(n) != G5_OK) return G5_ERR_OOM;
+    const int blocks = g5::grid_for(8);
+    k_rl_deg<<<blocks, 256, 0, s>>>(g->row_off, n, deg.p, ids.p);
+    size_t t1 = 0, t2 = 0;
+    G5_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, t1, deg.p, deg_sorted.p, ids.p, orig, n, 0, 32, s));
+    G5_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t2, row2, row2, n + 1, s));
+    g5::DevBuf<uint8_t> tmp;
+    if (tmp.alloc(std::max(t1, t2)) != G5_OK) return G5_ERR_OOM;
+    G5_CUDA(cub::DeviceRadixSort::SortPairsDescending(tmp.p, t1, deg.p, deg_sorted.p, ids.p, orig, n, 0, 32, s));
+    k_rl_perm<<<blocks, 256, 0, s>>>(orig, deg_sorted.p, n, perm, row2);
+    G5_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, t2, row2, row2, n + 1, s));
+    k_rl_cols<<<blocks, 256, 0, s>>>(g->row_off, g->col, orig, perm, row2, n, col2);
+    G5_CUDA(cudaStreamSynchronize(s));
+    return G5_OK;
 }
 
 }  // namespace
@@ -799,8 +1005,6 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
         b->graphs.push_back(graphs[i]);
         GraphDesc d;
         memset(&d, 0, sizeof d);
-        d.row_off = graphs[i]->row_off;
-        d.col = graphs[i]->col;
         d.n = graphs[i]->n;
         d.nnz = graphs[i]->nnz;
         d.vbase = vb;
@@ -822,6 +1026,10 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(G5_ERR_CUDA);
     cudaEventCreate(&b->ev0);
     cudaEventCreate(&b->ev1);
+    for (int i = 0; i < ngraphs; ++i) {
+        const g5_status rs = build_relabel(b, graphs[i], b->hgd[i]);
+        if (rs != G5_OK) return fail(rs);
+    }
 #define B_ALLOC(ptr, bytes) \
     if (cudaMalloc(&(ptr), (bytes)) != cudaSuccess) return fail(G5_ERR_OOM)
     B_ALLOC(b->gd, sizeof(GraphDesc) * ngraphs);
@@ -829,6 +1037,7 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     B_ALLOC(b->deg, sizeof(uint32_t) * vb);
     B_ALLOC(b->heavy, sizeof(uint32_t) * (vb / 32));
     B_ALLOC(b->iso, sizeof(uint32_t) * (vb / 32));
+    B_ALLOC(b->iso0, sizeof(uint32_t) * (vb / 32));
     B_ALLOC(b->words, sizeof(uint64_t) * 3 * vb);
     B_ALLOC(b->queue, sizeof(uint32_t) * vb);
     B_ALLOC(b->qoff, sizeof(uint64_t) * (vb + 1));
@@ -852,6 +1061,7 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     a.deg = b->deg;
     a.heavy = b->heavy;
     a.iso = b->iso;
+    a.iso0 = b->iso0;
     a.vis = b->words;
     a.front = b->words + vb;
     a.next = b->words + 2 * vb;
@@ -866,6 +1076,7 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     a.root_off = b->root_off;
     a.level_log = b->level_log;
     k_bdeg<<<g5::grid_for(8), kB, 0, b->stream>>>(b->gd, b->chunk_graph, vb, b->deg, b->heavy, b->iso);
+    k_biso0<<<g5::grid_for(8), kB, 0, b->stream>>>(b->gd, b->chunk_graph, vb, b->deg, b->iso0);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
     *out = b;
     return G5_OK;

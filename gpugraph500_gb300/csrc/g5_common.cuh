@@ -47,6 +47,27 @@ bool is_device_ptr(const void *p);
 // Grid of `per_sm` blocks per SM.
 inline int grid_for(int per_sm) { return num_sms() * per_sm; }
 
+// Owning device buffer (freed on scope exit unless released).
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+    g5_status alloc(size_t count)
+    {
+        G5_CUDA(cudaMalloc(&p, sizeof(T) * (count ? count : 1)));
+        return G5_OK;
+    }
+    T *release()
+    {
+        T *r = p;
+        p = nullptr;
+        return r;
+    }
+};
+
 }  // namespace g5
 
 // Device-side error flags (bit set in a status word).

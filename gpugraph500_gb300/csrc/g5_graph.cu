@@ -323,25 +323,7 @@ struct DevSkip {
     }
 };
 
-template <class T>
-struct DevBuf {
-    T *p = nullptr;
-    ~DevBuf()
-    {
-        if (p) cudaFree(p);
-    }
-    g5_status alloc(size_t count)
-    {
-        G5_CUDA(cudaMalloc(&p, sizeof(T) * (count ? count : 1)));
-        return G5_OK;
-    }
-    T *release()
-    {
-        T *r = p;
-        p = nullptr;
-        return r;
-    }
-};
+using g5::DevBuf;
 
 }  // namespace
 
