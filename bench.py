@@ -280,7 +280,7 @@ def main():
         print(json.dumps({"profile_batch": prof, "scale": args.scale, "roots": nr}))
         return 0
     # Graph500 edge counts (untimed)
-    probe = g5.CudaBFS(g)
+    probe = g5.CudaBFS(g, use_graph=not args.host_loop)
     nedges = []
     for r in roots:
         probe.runBFS(int(r))
@@ -335,6 +335,10 @@ def main():
     achieved = sum(alg) / (sum(dev_ms) * 1e-3) / 1e9
     peak, peak_kind = peaks()
 
+    # dominant kernel: one untimed pass in profile mode (host-driven, CUDA
+    # events around every launch) over the same roots
+    kern = kernel_roofline(g5, g, roots, alpha, beta, peak)
+
     # end to end through the C ABI with host (pinned) output buffers
     pinned = torch.empty(g.n, dtype=torch.int64, pin_memory=True)
     e2e = []
@@ -388,9 +392,11 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * nr,
                     "d2h_bytes_per_step": 8 * g.n * nr},
             "gpu_launches": None,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                         "scope": "whole search (all kernels of the level loop), algorithmic bytes"},
+            "roofline": {"bound": "hbm", "achieved": kern["achieved"], "peak": peak, "unit": "GB/s",
+                         "frac": kern["achieved"] / peak, "traffic": kern["traffic"],
+                         "peak_kind": peak_kind + " (copy, burst)", "kernel": kern,
+                         "search": {"achieved": achieved, "frac": achieved / peak,
+                                    "scope": "whole search (every kernel of the level loop), algorithmic bytes"}},
             "clocks": clocks,
             "validation": {"all_valid": all_valid, "all_min_parent": all_minpar},
             "plain": {"hmean_gteps": value_rank, "mean_ms": statistics.mean(dev_ms),
@@ -415,6 +421,71 @@ def main():
     return 0
 
 
+BU_KERNEL = "k_bu"
+TD_KERNEL = "k_td"
+
+
+def ncu_traffic(kernel, scale):
+    """DRAM bytes per launch of `kernel` at `scale` from the committed ncu
+    summary (profiles/<kernel>_scale<scale>.txt, line 'dram_bytes_per_launch:'),
+    or None."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_scale{scale}.txt")
+    try:
+        with open(path) as f:
+            for ln in f:
+                if ln.startswith("dram_bytes_per_launch:"):
+                    return float(ln.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def kernel_roofline(g5, g, roots, alpha, beta, peak):
+    """Per-kernel times of the plain search (profile mode) and the
+    algorithmic-bytes roofline of the dominant expansion kernel.  Per launch:
+    bottom-up 8(N+1) + 4 E_bu + 3N/8 (offset stream, adjacency read until the
+    first hit, frontier/visited/next bitmaps); top-down 20|F| + 4 E_td + N/8
+    (queue and row-offset pair, adjacency, visited bitmap)."""
+    pb = g5.CudaBFS(g, alpha=alpha, beta=beta, use_graph=False, profile=True)
+    n = g.n
+    tot = {}
+    acc = {"bu": [0.0, 0.0, 0], "td": [0.0, 0.0, 0]}  # bytes, ms, launches
+    for r in roots:
+        code = pb.run(int(r), None, None, stats=True)
+        if code != 0:
+            raise g5.G5Error(code, "g5_bfs_run (profile)")
+        log = pb.profile_log()
+        for k, ms in log:
+            tot[k] = tot.get(k, 0.0) + ms
+        exp = [ms for k, ms in log if k == "expand"]
+        for lvl, row in enumerate(pb.level_log()):
+            if lvl >= len(exp):
+                break
+            d, nf, _, read = (int(x) for x in row)
+            if d == 1:
+                b = 8 * (n + 1) + 4 * read + 3 * n / 8
+                key = "bu"
+            else:
+                b = 20 * nf + 4 * read + n / 8
+                key = "td"
+            acc[key][0] += b
+            acc[key][1] += exp[lvl]
+            acc[key][2] += 1
+    pb.close()
+    total_ms = sum(tot.values())
+    key = "bu" if acc["bu"][1] >= acc["td"][1] else "td"
+    b, ms, cnt = acc[key]
+    name = BU_KERNEL if key == "bu" else TD_KERNEL
+    ach = b / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+    return {"name": name, "launches": cnt, "ms_per_launch": ms / max(cnt, 1),
+            "bytes_per_launch": b / max(cnt, 1), "achieved": ach,
+            "share_of_search": ms / total_ms if total_ms else None,
+            "traffic": ncu_traffic(name, g.scale),
+            "kernel_ms_per_search": {k: v / len(roots) for k, v in tot.items()},
+            "other_expand": {"name": TD_KERNEL if key == "bu" else BU_KERNEL, "launches": acc["td" if key == "bu" else "bu"][2],
+                             "ms_total": acc["td" if key == "bu" else "bu"][1]}}
+
+
 class _DevArray:
     """A device array handed to torch through __cuda_array_interface__."""
 
@@ -429,11 +500,17 @@ def bench_batched(g5, torch, g, roots, nedges, args, tune=None, bfs=None):
     if tuned:
         bt.set_direction(tuned["alpha"], tuned["beta"])
     out = torch.empty(nr * g.n, dtype=torch.int32, device="cuda")
+
+    def one():
+        if args.host_loop:  # host-driven loop, same kernels (profilable by ncu)
+            return sum(bt.profile(roots, [nr], out)["kernel_ms"].values())
+        return bt.run(roots, [nr], out)
+
     for _ in range(args.warmup):
-        bt.run(roots, [nr], out)
+        one()
     ms = []
     for _ in range(args.steps):
-        ms.append(bt.run(roots, [nr], out))
+        ms.append(one())
     total = sum(nedges)
     agg = [total / (m * 1e-3) / 1e9 for m in ms]
     bt.close()
