@@ -21,10 +21,11 @@
 //
 // Parent choice: a vertex discovered at level L+1 gets the smallest adjacent
 // vertex of level L: the first frontier hit of its ascending adjacency, found
-// by the bottom-up sweep itself or, after a top-down level (which only sets
-// next-frontier bits for vertices of degree <= 64), by a fix-up sweep over the
-// new vertices; vertices of higher degree get it from a 64-bit atomicMin in
-// the top-down kernel instead of a long scan.  This is the parent
+// by the bottom-up sweep itself, or on a top-down level by a 64-bit atomicMin
+// per discovered edge (parent_mode 0, the default).  parent_mode 1 and 2 keep
+// the atomicMin for vertices of degree > 64 only (1) or not at all (2) and
+// find the other parents with a fix-up sweep of the new vertices' adjacency;
+// all three give the same parents.  This is the parent
 // CPUBFS_bin's ascending first-writer sweep picks (cpu_2d/cpubfs_bin.cpp:
 // 143-180), so parents equal the reference CPU path's, not only valid ones.
 #include <algorithm>
