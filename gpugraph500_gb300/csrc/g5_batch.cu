@@ -375,10 +375,23 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
                 }
 #pragma unroll
                 for (int q = 0; q < 4; ++q) hw[q] = uw[q] != 0xFFFFFFFFu ? a.front[d.vbase + uw[q]] : 0ull;
+                // one OR over the four windows; the first hits are located
+                // only when the step holds a root not found before
+                uint64_t lo = (hw[0] | hw[1] | hw[2] | hw[3]) & nd;
+#pragma unroll
+                for (int o = 16; o; o >>= 1) lo |= __shfl_xor_sync(0xFFFFFFFFu, lo, o);
+                if (!lo) {
+                    jj += 128;
+                    continue;
+                }
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     if (!nd) break;
                     const uint64_t hit = hw[q] & nd;
+                    if (!__ballot_sync(0xFFFFFFFFu, hit != 0)) {
+                        jj += 32;
+                        continue;
+                    }
                     // first lane of each root: exclusive prefix OR over the lanes
                     uint64_t incl = hit;
 #pragma unroll
