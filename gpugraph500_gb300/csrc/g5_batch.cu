@@ -425,21 +425,25 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
             }
         }
         __syncwarp();
-        // serial hits: lane r takes root r (and r + 32) of each vertex
+        // serial hits: lane k takes roots k and k + 32 of each vertex; the
+        // events' root sets are disjoint, so each root has one event
         unsigned vm = __ballot_sync(0xFFFFFFFFu, sfound != 0);
         while (vm) {
             const int vi = __ffs(vm) - 1;
             vm &= vm - 1;
             const uint64_t sf = __shfl_sync(0xFFFFFFFFu, sfound, vi);
             uint32_t *pv = a.pred + d.pred_base + (uint64_t)__shfl_sync(0xFFFFFFFFu, vo, vi) * R;
-            for (uint32_t r = lane; r < R; r += 32) {
-                if (!((sf >> r) & 1ull)) continue;
-                uint32_t p = 0;
+            uint32_t p0 = 0, p1 = 0;
 #pragma unroll
-                for (int k = kSerial - 1; k >= 0; --k)
-                    if ((s_evm[wib][k][vi] >> r) & 1ull) p = s_evu[wib][k][vi];
-                pv[r] = p;
+            for (int k = 0; k < kSerial; ++k) {
+                const uint64_t m = s_evm[wib][k][vi];
+                if (!m) continue;
+                const uint32_t u = s_evu[wib][k][vi];
+                if ((m >> lane) & 1ull) p0 = u;
+                if ((m >> (lane + 32)) & 1ull) p1 = u;
             }
+            if ((sf >> lane) & 1ull) pv[lane] = p0;
+            if ((sf >> (lane + 32)) & 1ull) pv[lane + 32] = p1;
         }
         __syncwarp();
         if (found) a.next[v] |= found;  // only this lane writes v in a bottom-up level
