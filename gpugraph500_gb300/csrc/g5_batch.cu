@@ -102,6 +102,7 @@ struct BArgs {
     uint32_t *tile_start;
     uint64_t max_tiles;
     uint64_t *chunk_n, *chunk_m;
+    uint8_t *chunk_live;    // per chunk: bit 0 next frontier not empty, bit 1 nothing for k_bwrite
     BState *st;
     const int64_t *roots;   // device copy of the roots (graph-major)
     const int32_t *root_off;
@@ -500,6 +501,10 @@ __global__ void __launch_bounds__(kB) k_bcount(BArgs a)
         }
         a.chunk_n[c] = tn;
         a.chunk_m[c] = tm;
+        // no frontier this level nor the last: visited, front and next of
+        // the chunk stay as they are, so the write pass skips it
+        const bool prev = a.chunk_live[c] & 1u, cur = tn != 0;
+        a.chunk_live[c] = (uint8_t)(cur ? 1u : (prev ? 0u : 2u));
     }
 }
 
@@ -509,7 +514,6 @@ __global__ void __launch_bounds__(1024) k_bscan(BArgs a)
 {
     __shared__ uint64_t s_gn[kMaxGraphs], s_gm[kMaxGraphs];
     __shared__ int s_gdir[kMaxGraphs];
-    __shared__ uint64_t s_w[33];
     for (int g = threadIdx.x; g < a.ngraphs; g += blockDim.x) {
         s_gn[g] = 0;
         s_gm[g] = 0;
@@ -517,29 +521,41 @@ __global__ void __launch_bounds__(1024) k_bscan(BArgs a)
     if (threadIdx.x == 0) a.st->dirs = 0;
     __syncthreads();
     const uint32_t C = a.nchunks;
+    // each warp owns a contiguous range of chunks and reads it 32 chunks at a
+    // time (coalesced); a step inside one graph is summed with a warp
+    // reduction and kept in registers until the graph changes
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t per_w = (C + 31) / 32;
+    const uint32_t w0 = min(C, wid * per_w), w1 = min(C, w0 + per_w);
     {
-        // each thread sums a contiguous run of chunks (mostly one graph) and
-        // flushes once per graph change: few shared atomics per thread
-        const uint32_t per0 = (C + blockDim.x - 1) / blockDim.x;
-        const uint32_t c0 = threadIdx.x * per0, c1 = min(C, c0 + per0);
-        int g = -1;
-        uint64_t sn = 0, sm = 0;
-        for (uint32_t c = c0; c < c1; ++c) {
-            const int gc = a.chunk_graph[c];
-            if (gc != g) {
-                if (g >= 0 && sn) {
-                    atomicAdd((unsigned long long *)&s_gn[g], (unsigned long long)sn);
-                    atomicAdd((unsigned long long *)&s_gm[g], (unsigned long long)sm);
+        int cur = -1;
+        uint64_t an = 0, am = 0;
+        for (uint32_t c0 = w0; c0 < w1; c0 += 32) {
+            const uint32_t c = c0 + lane;
+            const bool ok = c < w1;
+            const uint64_t xn = ok ? a.chunk_n[c] : 0, xm = ok ? a.chunk_m[c] : 0;
+            const int g = ok ? a.chunk_graph[c] : -1;
+            const int g0 = __shfl_sync(0xFFFFFFFFu, g, 0);
+            if (__all_sync(0xFFFFFFFFu, !ok || g == g0)) {
+                const uint64_t sn = wsum(xn), sm = wsum(xm);
+                if (g0 != cur) {
+                    if (lane == 0 && cur >= 0 && (an | am)) {
+                        atomicAdd((unsigned long long *)&s_gn[cur], (unsigned long long)an);
+                        atomicAdd((unsigned long long *)&s_gm[cur], (unsigned long long)am);
+                    }
+                    cur = g0;
+                    an = am = 0;
                 }
-                g = gc;
-                sn = sm = 0;
+                an += sn;
+                am += sm;
+            } else if (ok && (xn | xm)) {  // a graph boundary inside the step
+                atomicAdd((unsigned long long *)&s_gn[g], (unsigned long long)xn);
+                atomicAdd((unsigned long long *)&s_gm[g], (unsigned long long)xm);
             }
-            sn += a.chunk_n[c];
-            sm += a.chunk_m[c];
         }
-        if (g >= 0 && sn) {
-            atomicAdd((unsigned long long *)&s_gn[g], (unsigned long long)sn);
-            atomicAdd((unsigned long long *)&s_gm[g], (unsigned long long)sm);
+        if (lane == 0 && cur >= 0 && (an | am)) {
+            atomicAdd((unsigned long long *)&s_gn[cur], (unsigned long long)an);
+            atomicAdd((unsigned long long *)&s_gm[cur], (unsigned long long)am);
         }
     }
     __syncthreads();
@@ -567,59 +583,53 @@ __global__ void __launch_bounds__(1024) k_bscan(BArgs a)
         if (tn) atomicOr(&a.st->dirs, nd == TD ? 1u : 2u);
     }
     __syncthreads();
-    // exclusive prefix over chunks of top-down graphs
-    const uint32_t per = (C + 1023) / 1024;
-    const uint32_t b0 = threadIdx.x * per;
-    uint64_t ln = 0, lm = 0;
-    for (uint32_t i = 0; i < per && b0 + i < C; ++i) {
-        if (s_gdir[a.chunk_graph[b0 + i]] == TD) {
-            ln += a.chunk_n[b0 + i];
-            lm += a.chunk_m[b0 + i];
+    // exclusive prefix over the chunks of top-down graphs: warp totals, a
+    // scan of the 32 totals, then each warp writes its range's offsets
+    uint64_t tn_w = 0, tm_w = 0;
+    for (uint32_t c0 = w0; c0 < w1; c0 += 32) {
+        const uint32_t c = c0 + lane;
+        if (c < w1 && s_gdir[a.chunk_graph[c]] == TD) {
+            tn_w += a.chunk_n[c];
+            tm_w += a.chunk_m[c];
         }
     }
-    // block scan (two passes over s_w)
-    uint64_t tot_n, tot_m, on, om;
-    {
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-        for (int pass = 0; pass < 2; ++pass) {
-            uint64_t v = pass ? lm : ln, x = v;
+    tn_w = wsum(tn_w);
+    tm_w = wsum(tm_w);
+    __shared__ uint64_t s_wn[32], s_wm[32];
+    if (lane == 0) {
+        s_wn[wid] = tn_w;
+        s_wm[wid] = tm_w;
+    }
+    __syncthreads();
+    uint64_t tot_n = 0, tot_m = 0, on = 0, om = 0;
+    for (int i = 0; i < 32; ++i) {
+        if (i == wid) {
+            on = tot_n;
+            om = tot_m;
+        }
+        tot_n += s_wn[i];
+        tot_m += s_wm[i];
+    }
+    for (uint32_t c0 = w0; c0 < w1; c0 += 32) {
+        const uint32_t c = c0 + lane;
+        const bool ok = c < w1;
+        const bool td = ok && s_gdir[a.chunk_graph[c]] == TD;
+        const uint64_t xn = td ? a.chunk_n[c] : 0, xm = td ? a.chunk_m[c] : 0;
+        uint64_t in = xn, im = xm;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint64_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-                if (lane >= o) x += y;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t yn = __shfl_up_sync(0xFFFFFFFFu, in, o), ym = __shfl_up_sync(0xFFFFFFFFu, im, o);
+            if (lane >= o) {
+                in += yn;
+                im += ym;
             }
-            if (lane == 31) s_w[wid] = x;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                uint64_t acc = 0;
-                for (int i = 0; i < 32; ++i) {
-                    uint64_t t = s_w[i];
-                    s_w[i] = acc;
-                    acc += t;
-                }
-                s_w[32] = acc;
-            }
-            __syncthreads();
-            const uint64_t r = x - v + s_w[wid];
-            if (pass) {
-                om = r;
-                tot_m = s_w[32];
-            } else {
-                on = r;
-                tot_n = s_w[32];
-            }
-            __syncthreads();
         }
-    }
-    for (uint32_t i = 0; i < per && b0 + i < C; ++i) {
-        const uint64_t xn = a.chunk_n[b0 + i], xm = a.chunk_m[b0 + i];
-        const bool td = s_gdir[a.chunk_graph[b0 + i]] == TD;
-        a.chunk_n[b0 + i] = td ? on : ~0ull;  // ~0: chunk not queued
-        a.chunk_m[b0 + i] = om;
-        if (td) {
-            on += xn;
-            om += xm;
+        if (ok) {
+            a.chunk_n[c] = td ? on + in - xn : ~0ull;  // ~0: chunk not queued
+            a.chunk_m[c] = om + im - xm;
         }
+        on += __shfl_sync(0xFFFFFFFFu, in, 31);
+        om += __shfl_sync(0xFFFFFFFFu, im, 31);
     }
     if (threadIdx.x == 0) {
         uint64_t act = 0;
@@ -643,6 +653,7 @@ __global__ void __launch_bounds__(1024) k_bscan(BArgs a)
 __global__ void __launch_bounds__(kB) k_bwrite(BArgs a)
 {
     const uint32_t c = blockIdx.x;
+    if (a.chunk_live[c] & 2u) return;
     const uint64_t v0 = (uint64_t)c * kChunk + (uint64_t)threadIdx.x * kPerThread;
     uint64_t nx[kPerThread];
     uint64_t cn = 0, cm = 0;
@@ -873,6 +884,7 @@ void enqueue_batch(g5_batch *b, const BArgs &a, cudaStream_t s, bool body, std::
     };
     if (!body) {
         cudaMemsetAsync(b->words, 0, sizeof(uint64_t) * 3 * a.ntot, s);
+        cudaMemsetAsync(a.chunk_live, 0, a.nchunks, s);
         k_binit<<<std::max(1, a.ngraphs), kB, 0, s>>>(a);
         return;
     }
@@ -1060,7 +1072,7 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     B_ALLOC(b->qoff, sizeof(uint64_t) * (vb + 1));
     B_ALLOC(b->qbase, sizeof(int64_t) * vb);
     B_ALLOC(b->tile_start, sizeof(uint32_t) * a.max_tiles);
-    B_ALLOC(b->chunks, sizeof(uint64_t) * 2 * a.nchunks);
+    B_ALLOC(b->chunks, sizeof(uint64_t) * 2 * a.nchunks + a.nchunks);
     B_ALLOC(b->st, sizeof(BState));
     B_ALLOC(b->roots, sizeof(int64_t) * 64 * ngraphs);
     B_ALLOC(b->root_off, sizeof(int32_t) * (ngraphs + 1));
@@ -1088,6 +1100,7 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     a.tile_start = b->tile_start;
     a.chunk_n = b->chunks;
     a.chunk_m = b->chunks + a.nchunks;
+    a.chunk_live = reinterpret_cast<uint8_t *>(b->chunks + 2 * (uint64_t)a.nchunks);
     a.st = b->st;
     a.roots = b->roots;
     a.root_off = b->root_off;
@@ -1190,6 +1203,7 @@ g5_status g5_batch_serve_begin(g5_batch *b, uint32_t *pred_dev, const int *slots
     if (!b->adm_host) G5_CUDA(cudaMallocHost(&b->adm_host, sizeof(Admit) * 64 * ng + sizeof(uint64_t) * ng));
     G5_CUDA(cudaMemcpyAsync(b->gd, b->hgd.data(), sizeof(GraphDesc) * ng, cudaMemcpyHostToDevice, s));
     G5_CUDA(cudaMemsetAsync(b->words, 0, sizeof(uint64_t) * 3 * b->args.ntot, s));
+    G5_CUDA(cudaMemsetAsync(b->args.chunk_live, 0, b->args.nchunks, s));
     // every entry starts unvisited; a retired slot's entries are reset by
     // k_sclear, so an admitted root always starts from a clean column
     if (pb) G5_CUDA(cudaMemsetAsync(pred_dev, 0xFF, sizeof(uint32_t) * pb, s));
