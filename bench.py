@@ -148,28 +148,18 @@ def dist_init(args):
 
 
 def barrier_sync(dist):
-    import torch
-    if dist is not None:
-        dist.barrier()
-    torch.cuda.synchronize()
+    from gpugraph500_gb300 import replicas
+    replicas.barrier(dist)
 
 
 def max_over_ranks(x, dist):
-    if dist is None:
-        return x
-    import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from gpugraph500_gb300 import replicas
+    return replicas.reduce_max(x, dist)
 
 
 def sum_over_ranks(x, dist):
-    if dist is None:
-        return x
-    import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    from gpugraph500_gb300 import replicas
+    return replicas.reduce_sum(x, dist)
 
 
 # ---------------------------------------------------------------------------
@@ -270,7 +260,9 @@ def main():
     t0 = time.time()
     g = g5.Graph.kronecker(args.scale)
     gen_s = time.time() - t0
-    roots = g5.select_roots(g, args.roots)
+    # every rank holds the graph and searches its own block of roots
+    from gpugraph500_gb300 import replicas
+    roots = replicas.shard_roots(g5.select_roots(g, args.roots * ws), args.roots, rank, ws)
     nr = len(roots)
     if args.profile_batch:
         bt = g5.Batch([g])
