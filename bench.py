@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-codec", action="store_true")
+    ap.add_argument("--big-scale", type=int, default=0,
+                    help="also compare plain and batched search on a second, larger graph (e.g. 28)")
     ap.add_argument("--serve-rates", default="1000,5000,20000")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--profile-batch", action="store_true",
@@ -369,6 +371,14 @@ def main():
                          f"(cpu_2d/cpubfs_bin.cpp:147,168), ~{args.cpu_seconds:.0f} s budget"}
         del ro, col
 
+    big = None
+    if rank == 0 and args.big_scale:
+        # the main graph and workspace go first: the larger graph needs the room
+        bfs.close()
+        g.close()
+        torch.cuda.empty_cache()
+        big = bench_big(g5, torch, args, tune if not args.no_tune else None, (alpha, beta))
+
     value = sum_over_ranks(value_rank, dist) if ws > 1 else value_rank
     if rank == 0:
         line = {
@@ -397,6 +407,7 @@ def main():
             "serve": serve,
             "mixed_batch": mixed,
             "codec": codec,
+            "big_scale": big,
             "cpu_baseline": cpu,
         }
         if batched and "aggregate_gteps" in batched:
@@ -573,6 +584,32 @@ def bench_serve(g5, big, args):
         gr.close()
     return {"graphs_scales": scales, "slots": slots, "mem_budget_bytes": budget, "mode": "streams",
             "rates": out}
+
+
+def bench_big(g5, torch, args, tune, ab):
+    """Plain vs batched search, 64 roots, on a second graph of scale
+    args.big_scale (built after the main graph is released)."""
+    t0 = time.time()
+    g = g5.Graph.kronecker(args.big_scale)
+    build_s = time.time() - t0
+    roots = g5.select_roots(g, 64)
+    bfs = g5.CudaBFS(g, alpha=ab[0], beta=ab[1], use_graph=not args.host_loop)
+    nedges, ms = [], []
+    for r in roots:  # warm-up pass, also the TEPS edge counts
+        bfs.runBFS(int(r))
+        nedges.append(bfs.teps_edges())
+    for r in roots:
+        code = bfs.run(int(r), None, None, stats=True)
+        if code != 0:
+            raise g5.G5Error(code, "g5_bfs_run")
+        ms.append(bfs.stats.device_ms)
+    plain = hmean([ne / (t * 1e-3) / 1e9 for ne, t in zip(nedges, ms)])
+    batched = bench_batched(g5, torch, g, roots, nedges, args, tune, bfs)
+    bfs.close()
+    g.close()
+    return {"scale": args.big_scale, "graph_build_s": round(build_s, 2), "plain_hmean_gteps": plain,
+            "plain_mean_ms": statistics.mean(ms), "batched": batched,
+            "batched_over_plain": batched["aggregate_gteps"] / plain if plain else None}
 
 
 def bench_mixed(g5, torch, args):

@@ -34,6 +34,7 @@ STATUS = {
 }
 G5_OK, G5_ERR_OOM, G5_ERR_CAPACITY, G5_ERR_INVALID_ARG = 0, 1, 2, 3
 G5_ERR_TIMEOUT, G5_ERR_CORRUPT_STREAM, G5_ERR_CUDA, G5_ERR_NO_DEVICE, G5_ERR_MISMATCH = 4, 5, 6, 7, 8
+G5_ERR_IO = 9
 
 CODEC_NONE, CODEC_D4, CODEC_DM = 0, 1, 2
 CODEC_NAMES = {"s4-bp128-d4": CODEC_D4, "s4-bp128-dm": CODEC_DM}
@@ -80,6 +81,9 @@ SIGNATURES = {
     "g5_graph_copy_csr": (_I, [_P, _P, _P]),
     "g5_graph_device_csr": (_I, [_P, C.POINTER(_P), C.POINTER(_P)]),
     "g5_graph_destroy": (_I, [_P]),
+    "g5_graph_save": (_I, [_P, C.c_char_p]),
+    "g5_graph_load": (_I, [C.c_char_p, C.POINTER(_P)]),
+    "g5_graph_kronecker_info": (_I, [_P, C.POINTER(C.c_int), C.POINTER(_I64)]),
     "g5_select_roots": (_I, [_P, _I, _I64, _P, C.POINTER(_I)]),
     "g5_bfs_config_default": (None, [C.POINTER(BfsConfig)]),
     "g5_bfs_create": (_I, [_P, C.POINTER(BfsConfig), C.POINTER(_P)]),
@@ -177,6 +181,19 @@ class Graph:
         _check(lib().g5_graph_generate_kronecker(scale, edgefactor, seed1, seed2, C.byref(h)),
                "g5_graph_generate_kronecker")
         return cls(h.value, scale)
+
+    @classmethod
+    def load(cls, path: str) -> "Graph":
+        """A graph saved with save(), uploaded to the current device."""
+        h = C.c_void_p()
+        _check(lib().g5_graph_load(os.fsencode(path), C.byref(h)), "g5_graph_load")
+        sc = C.c_int()
+        _check(lib().g5_graph_kronecker_info(h, C.byref(sc), None), "g5_graph_kronecker_info")
+        return cls(h.value, sc.value if sc.value >= 0 else None)
+
+    def save(self, path: str) -> None:
+        """Binary CSR cache on disk (header, offsets, columns, generated endpoint counts)."""
+        _check(lib().g5_graph_save(self._h, os.fsencode(path)), "g5_graph_save")
 
     def csr(self) -> tuple[np.ndarray, np.ndarray]:
         ro = np.empty(self.n + 1, np.int64)

@@ -8,6 +8,8 @@
 // append reversed edges, sort by (v0, v1), drop self loops and duplicates.
 #include <cub/cub.cuh>
 
+#include <algorithm>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -339,6 +341,59 @@ g5_status graph_degree(const g5_graph *g, int64_t v, int64_t *deg)
 
 }  // namespace g5
 
+namespace {
+
+// On-disk header of the binary CSR cache (64 bytes, little-endian).
+constexpr char kFileMagic[8] = {'G', '5', 'C', 'S', 'R', 0, 0, 1};  // format version 1
+struct FileHeader {
+    char magic[8];
+    int64_t n;
+    int64_t nnz;
+    int32_t scale;      // Kronecker scale, -1 if not generated
+    uint32_t flags;     // bit 0: generated endpoint counts follow the columns
+    int64_t gen_edges;  // generated (undirected) edges, 0 if not generated
+    uint8_t pad[24];
+};
+static_assert(sizeof(FileHeader) == 64, "graph file header is 64 bytes");
+
+constexpr size_t kIoChunk = size_t(64) << 20;  // bytes per staged copy
+
+// Device array -> file, through a pinned staging buffer.
+g5_status stream_out(FILE *f, const void *dev, size_t bytes)
+{
+    void *stage = nullptr;
+    if (cudaMallocHost(&stage, std::min(bytes, kIoChunk) + 1) != cudaSuccess) return G5_ERR_OOM;
+    g5_status st = G5_OK;
+    for (size_t off = 0; off < bytes && st == G5_OK; off += kIoChunk) {
+        const size_t len = std::min(kIoChunk, bytes - off);
+        if (cudaMemcpy(stage, (const char *)dev + off, len, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = G5_ERR_CUDA;
+        else if (fwrite(stage, 1, len, f) != len)
+            st = G5_ERR_IO;
+    }
+    cudaFreeHost(stage);
+    return st;
+}
+
+// File -> device array, through a pinned staging buffer.
+g5_status stream_in(FILE *f, void *dev, size_t bytes)
+{
+    void *stage = nullptr;
+    if (cudaMallocHost(&stage, std::min(bytes, kIoChunk) + 1) != cudaSuccess) return G5_ERR_OOM;
+    g5_status st = G5_OK;
+    for (size_t off = 0; off < bytes && st == G5_OK; off += kIoChunk) {
+        const size_t len = std::min(kIoChunk, bytes - off);
+        if (fread(stage, 1, len, f) != len)
+            st = G5_ERR_IO;
+        else if (cudaMemcpy((char *)dev + off, stage, len, cudaMemcpyHostToDevice) != cudaSuccess)
+            st = G5_ERR_CUDA;
+    }
+    cudaFreeHost(stage);
+    return st;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *g5_status_str(g5_status s)
@@ -353,6 +408,7 @@ const char *g5_status_str(g5_status s)
     case G5_ERR_CUDA: return "CUDA error";
     case G5_ERR_NO_DEVICE: return "no CUDA device";
     case G5_ERR_MISMATCH: return "round-trip mismatch";
+    case G5_ERR_IO: return "graph file I/O error or not a graph file";
     }
     return "unknown status";
 }
@@ -534,6 +590,98 @@ g5_status g5_graph_device_csr(const g5_graph *g, const int64_t **row_off, const 
     if (!g) return G5_ERR_INVALID_ARG;
     if (row_off) *row_off = g->row_off;
     if (col) *col = g->col;
+    return G5_OK;
+}
+
+g5_status g5_graph_kronecker_info(const g5_graph *g, int *scale, int64_t *gen_edges)
+{
+    if (!g) return G5_ERR_INVALID_ARG;
+    if (scale) *scale = g->end_deg ? g->scale : -1;
+    if (gen_edges) *gen_edges = g->end_deg ? g->gen_edges : 0;
+    return G5_OK;
+}
+
+g5_status g5_graph_save(const g5_graph *g, const char *path)
+{
+    if (!g || !path) return G5_ERR_INVALID_ARG;
+    FileHeader h;
+    memset(&h, 0, sizeof h);
+    memcpy(h.magic, kFileMagic, sizeof h.magic);
+    h.n = g->n;
+    h.nnz = g->nnz;
+    h.scale = g->end_deg ? g->scale : -1;
+    h.flags = g->end_deg ? 1u : 0u;
+    h.gen_edges = g->end_deg ? g->gen_edges : 0;
+    FILE *f = fopen(path, "wb");
+    if (!f) return G5_ERR_IO;
+    g5_status st = G5_OK;
+    if (fwrite(&h, sizeof h, 1, f) != 1) st = G5_ERR_IO;
+    if (st == G5_OK) st = stream_out(f, g->row_off, sizeof(int64_t) * (size_t)(g->n + 1));
+    if (st == G5_OK) st = stream_out(f, g->col, sizeof(uint32_t) * (size_t)g->nnz);
+    if (st == G5_OK && g->end_deg) st = stream_out(f, g->end_deg, sizeof(uint32_t) * (size_t)g->n);
+    if (fclose(f) != 0 && st == G5_OK) st = G5_ERR_IO;
+    return st;
+}
+
+g5_status g5_graph_load(const char *path, g5_graph **out)
+{
+    if (!path || !out) return G5_ERR_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return G5_ERR_NO_DEVICE;
+    }
+    FILE *f = fopen(path, "rb");
+    if (!f) return G5_ERR_IO;
+    struct Closer {
+        FILE *f;
+        ~Closer() { fclose(f); }
+    } closer{f};
+    FileHeader h;
+    if (fread(&h, sizeof h, 1, f) != 1 || memcmp(h.magic, kFileMagic, sizeof h.magic) != 0) return G5_ERR_IO;
+    if (h.n <= 0 || h.n > ((int64_t)1 << 32) || h.nnz < 0 || (h.flags & ~1u)) return G5_ERR_IO;
+    // the file must hold exactly the arrays the header announces
+    const uint64_t body = sizeof(int64_t) * (uint64_t)(h.n + 1) + sizeof(uint32_t) * (uint64_t)h.nnz +
+                          ((h.flags & 1u) ? sizeof(uint32_t) * (uint64_t)h.n : 0);
+    if (fseeko(f, 0, SEEK_END) != 0) return G5_ERR_IO;
+    const off_t size = ftello(f);
+    if (size < 0 || (uint64_t)size != sizeof h + body || fseeko(f, (off_t)sizeof h, SEEK_SET) != 0)
+        return G5_ERR_IO;
+    DevBuf<int64_t> ro;
+    DevBuf<uint32_t> cl, ed;
+    G5_TRY(ro.alloc((size_t)h.n + 1));
+    G5_TRY(cl.alloc((size_t)h.nnz));
+    G5_TRY(stream_in(f, ro.p, sizeof(int64_t) * (size_t)(h.n + 1)));
+    G5_TRY(stream_in(f, cl.p, sizeof(uint32_t) * (size_t)h.nnz));
+    if (h.flags & 1u) {
+        G5_TRY(ed.alloc((size_t)h.n));
+        G5_TRY(stream_in(f, ed.p, sizeof(uint32_t) * (size_t)h.n));
+    }
+    int64_t first = -1, last = -1;
+    G5_CUDA(cudaMemcpy(&first, ro.p, sizeof(int64_t), cudaMemcpyDeviceToHost));
+    G5_CUDA(cudaMemcpy(&last, ro.p + h.n, sizeof(int64_t), cudaMemcpyDeviceToHost));
+    if (first != 0 || last != h.nnz) return G5_ERR_INVALID_ARG;
+    DevBuf<unsigned> bad;
+    G5_TRY(bad.alloc(1));
+    G5_CUDA(cudaMemset(bad.p, 0, sizeof(unsigned)));
+    k_check_csr<<<g5::grid_for(4), 256>>>(ro.p, cl.p, h.n, h.nnz, bad.p);
+    G5_CUDA(cudaGetLastError());
+    unsigned hbad = 0;
+    G5_CUDA(cudaMemcpy(&hbad, bad.p, sizeof hbad, cudaMemcpyDeviceToHost));
+    if (hbad & 1u) return G5_ERR_INVALID_ARG;
+    g5_graph *g = new g5_graph();
+    cudaGetDevice(&g->device);
+    g->n = h.n;
+    g->nnz = h.nnz;
+    g->row_off = ro.release();
+    g->col = cl.release();
+    if (h.flags & 1u) {
+        g->end_deg = ed.release();
+        g->scale = h.scale;
+        g->gen_edges = h.gen_edges;
+    }
+    *out = g;
     return G5_OK;
 }
 

@@ -34,7 +34,9 @@ typedef enum g5_status {
     G5_ERR_CORRUPT_STREAM = 5, /* codec stream fails validation            */
     G5_ERR_CUDA = 6,           /* any other CUDA runtime error             */
     G5_ERR_NO_DEVICE = 7,      /* no CUDA device visible                   */
-    G5_ERR_MISMATCH = 8        /* an in-loop round-trip check failed       */
+    G5_ERR_MISMATCH = 8,       /* an in-loop round-trip check failed       */
+    G5_ERR_IO = 9              /* a graph file cannot be read or written, or
+                                  is not a well-formed graph file          */
 } g5_status;
 
 /* Human-readable name of a status code (static storage). */
@@ -88,6 +90,23 @@ g5_status g5_graph_device_csr(const g5_graph *g, const int64_t **row_off,
                               const uint32_t **col);
 
 g5_status g5_graph_destroy(g5_graph *g);
+
+/* Binary CSR cache on disk, so a large graph is built once: the reference
+ * rebuilds the graph on every run (generator + setupMatrix2,
+ * cpu_2d/main.cpp:221-260, cpu_2d/distmatrix2d.hh:745-1166).  The file holds
+ * a 64-byte header (magic "G5CSR", format version, n, nnz, Kronecker scale and
+ * generated edge count when known), the int64 row offsets, the uint32
+ * columns and, for generated graphs, the per-vertex generated endpoint counts
+ * (little-endian).  g5_graph_load uploads it to the current device and checks
+ * its structure like g5_graph_create (offsets from 0 to nnz, columns < n,
+ * rows sorted without duplicates); a short, truncated or foreign file gives
+ * G5_ERR_IO, a malformed CSR G5_ERR_INVALID_ARG. */
+g5_status g5_graph_save(const g5_graph *g, const char *path);
+g5_status g5_graph_load(const char *path, g5_graph **out);
+
+/* Kronecker scale and generated edge count of a generated (or loaded
+ * generated) graph; scale -1 and 0 edges for a CSR built from arrays. */
+g5_status g5_graph_kronecker_info(const g5_graph *g, int *scale, int64_t *gen_edges);
 
 /* Root selection of the reference driver (cpu_2d/main.cpp:351-392):
  * default-seeded std::knuth_b, uniform_int_distribution<int64_t>(0, n-1),
