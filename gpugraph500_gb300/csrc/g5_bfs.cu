@@ -405,9 +405,58 @@ __device__ void sweep(const BfsArgs &a, uint64_t &examined)
     }
 }
 
+// First bottom-up level: one warp per 32-vertex word, software-pipelined so
+// that a word's visited bits are loaded two steps and its candidates' row
+// offsets one step before the word is scanned; the scan of one word then
+// overlaps the loads of the next two instead of waiting on each in turn.
+template <typename Off>
+__device__ void sweep_bu(const BfsArgs &a, uint64_t &examined)
+{
+    const int lane = g5_lane();
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t nwords = a.nwords;
+    // stage 2: candidates of the word after next; stage 1: next word's offsets
+    uint32_t c1 = gw < nwords ? ~a.visited[gw] : 0u;
+    uint32_t c2 = gw + nw < nwords ? ~a.visited[gw + nw] : 0u;
+    Off s1 = 0, e1 = 0;
+    if ((c1 >> lane) & 1u) load_offsets(a, gw * 32 + lane, s1, e1);
+    for (uint64_t w = gw; w < nwords; w += nw) {
+        const uint32_t cw = c1;
+        const Off s = s1, e = e1;
+        c1 = c2;
+        const uint64_t w2 = w + 2 * nw;
+        c2 = w2 < nwords ? ~a.visited[w2] : 0u;
+        s1 = e1 = 0;
+        if ((c1 >> lane) & 1u) load_offsets(a, (w + nw) * 32 + lane, s1, e1);
+        if (!cw) continue;
+        const uint64_t v = w * 32 + lane;
+        const bool mine = (cw >> lane) & 1u;
+        bool found;
+        uint32_t par;
+        uint64_t ex;
+        first_hit<Off>(a, mine, s, e, found, par, ex);
+        if (found) a.pred[v] = (int64_t)par;
+        const unsigned fm = __ballot_sync(0xFFFFFFFFu, found);
+        if (fm) {
+            // degree sum of the added vertices: the counting pass after a
+            // bottom-up level then reads one word per 32 vertices
+            uint32_t dsum = found ? (uint32_t)(e - s) : 0u;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) dsum += __shfl_xor_sync(0xFFFFFFFFu, dsum, o);
+            if (lane == 0) {
+                a.next[w] = fm;
+                a.wdeg[w] = dsum;
+            }
+        }
+        examined += ex;
+    }
+}
+
 // Bottom-up level over the sorted list of unvisited vertices (written by the
 // previous level's compaction): 32 candidates per warp step, every lane
-// busy, instead of sweeping all words of which many hold no candidate.
+// busy, instead of sweeping all words of which many hold no candidate.  The
+// list entries are loaded two steps and their row offsets one step ahead.
 template <typename Off>
 __device__ void bottom_up_list(const BfsArgs &a, uint64_t &examined)
 {
@@ -416,11 +465,22 @@ __device__ void bottom_up_list(const BfsArgs &a, uint64_t &examined)
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const uint64_t len = a.st->ulen;
     const uint32_t *__restrict__ list = a.ulist;
-    for (uint64_t b0 = gw * 32; b0 < len; b0 += nw * 32) {
+    const uint64_t stride = nw * 32;
+    uint64_t p1 = gw * 32 + lane, p2 = p1 + stride;
+    uint32_t v1 = p1 < len ? list[p1] : 0u;
+    uint32_t v2 = p2 < len ? list[p2] : 0u;
+    Off s1 = 0, e1 = 0;
+    if (p1 < len) load_offsets(a, v1, s1, e1);
+    for (uint64_t b0 = gw * 32; b0 < len; b0 += stride) {
         const bool mine = b0 + lane < len;
-        const uint32_t v = mine ? list[b0 + lane] : 0u;
-        Off s = 0, e = 0;
-        if (mine) load_offsets(a, v, s, e);
+        const uint32_t v = v1;
+        const Off s = s1, e = e1;
+        v1 = v2;
+        p1 = p2;
+        p2 += stride;
+        v2 = p2 < len ? list[p2] : 0u;
+        s1 = e1 = 0;
+        if (p1 < len) load_offsets(a, v1, s1, e1);
         bool found;
         uint32_t par;
         uint64_t ex;
@@ -463,7 +523,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_bu(BfsArgs a)
     if (a.st->err || a.st->dir != DIR_BU) return;
     uint64_t examined = 0;
     if (a.st->list_mode) bottom_up_list<Off>(a, examined);
-    else sweep<false, Off>(a, examined);
+    else sweep_bu<Off>(a, examined);
     add_examined(a, examined);
 }
 
