@@ -292,7 +292,14 @@ def main():
         k = min(8, nr)
         tuned = tune.tune_plain(g5, g, roots[:k], nedges[:k])
         alpha, beta = tuned["alpha"], tuned["beta"]
-    bfs = g5.CudaBFS(g, alpha=alpha, beta=beta, use_graph=not args.host_loop)
+    sizes = {}
+    if not args.no_tune:
+        st = tune.tune_sizes(g5, g, roots[:min(8, nr)], nedges[:min(8, nr)], alpha, beta)
+        sizes = {"tile_edges": st["tile_edges"], "bu_serial": st["bu_serial"]}
+        tuned_sizes = st["grid"][:6]
+    else:
+        tuned_sizes = None
+    bfs = g5.CudaBFS(g, alpha=alpha, beta=beta, use_graph=not args.host_loop, **sizes)
 
     # Graph500 validation of every root on the device (untimed)
     all_valid, all_minpar = True, True
@@ -331,7 +338,7 @@ def main():
 
     # dominant kernel: one untimed pass in profile mode (host-driven, CUDA
     # events around every launch) over the same roots
-    kern = kernel_roofline(g5, g, roots, alpha, beta, peak)
+    kern = kernel_roofline(g5, g, roots, alpha, beta, peak, sizes)
 
     # end to end through the C ABI with host (pinned) output buffers
     pinned = torch.empty(g.n, dtype=torch.int64, pin_memory=True)
@@ -390,7 +397,8 @@ def main():
                        "n": g.n, "nnz": g.nnz, "roots": nr, "parallelism": "replicas" if ws > 1 else "1 GPU",
                        "l2": "inputs larger than L2 (CSR %.1f GB)" % ((g.nnz * 4 + g.n * 8) / 1e9),
                        "graph_build_s": round(gen_s, 2), "alpha": alpha, "beta": beta,
-                       "tuner": tuned["grid"][:6] if tuned else None},
+                       "tuner": tuned["grid"][:6] if tuned else None, "sizes": sizes or "defaults (256, 8)",
+                       "sizes_tuner": tuned_sizes},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * nr,
                     "d2h_bytes_per_step": 8 * g.n * nr},
             "gpu_launches": None,
@@ -443,13 +451,13 @@ def ncu_traffic(kernel, scale):
     return None
 
 
-def kernel_roofline(g5, g, roots, alpha, beta, peak):
+def kernel_roofline(g5, g, roots, alpha, beta, peak, sizes=None):
     """Per-kernel times of the plain search (profile mode) and the
     algorithmic-bytes roofline of the dominant expansion kernel.  Per launch:
     bottom-up 8(N+1) + 4 E_bu + 3N/8 (offset stream, adjacency read until the
     first hit, frontier/visited/next bitmaps); top-down 20|F| + 4 E_td + N/8
     (queue and row-offset pair, adjacency, visited bitmap)."""
-    pb = g5.CudaBFS(g, alpha=alpha, beta=beta, use_graph=False, profile=True)
+    pb = g5.CudaBFS(g, alpha=alpha, beta=beta, use_graph=False, profile=True, **(sizes or {}))
     n = g.n
     tot = {}
     acc = {"bu": [0.0, 0.0, 0], "td": [0.0, 0.0, 0]}  # bytes, ms, launches

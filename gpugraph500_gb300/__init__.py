@@ -50,7 +50,7 @@ class BfsConfig(C.Structure):
     _fields_ = [("alpha", C.c_double), ("beta", C.c_double), ("codec", C.c_int),
                 ("codec_threshold", C.c_uint32), ("use_graph", C.c_int),
                 ("max_levels", C.c_int), ("want_levels", C.c_int), ("profile", C.c_int),
-                ("parent_mode", C.c_int)]
+                ("parent_mode", C.c_int), ("tile_edges", C.c_uint32), ("bu_serial", C.c_int)]
 
 
 class BfsStats(C.Structure):
@@ -254,7 +254,8 @@ class CudaBFS:
     def __init__(self, graph: Graph, codec: int = CODEC_NONE, codec_threshold: int = 64,
                  alpha: float = 14.0, beta: float = 24.0, use_graph: bool = True,
                  want_levels: bool = False, max_levels: int = 4096, profile: bool = False,
-                 parent_mode: Optional[int] = None):
+                 parent_mode: Optional[int] = None, tile_edges: Optional[int] = None,
+                 bu_serial: Optional[int] = None):
         self.graph = graph
         cfg = default_config()
         cfg.alpha, cfg.beta, cfg.codec, cfg.codec_threshold = alpha, beta, codec, codec_threshold
@@ -262,6 +263,10 @@ class CudaBFS:
         cfg.profile = int(profile)
         if parent_mode is not None:
             cfg.parent_mode = parent_mode
+        if tile_edges is not None:
+            cfg.tile_edges = tile_edges
+        if bu_serial is not None:
+            cfg.bu_serial = bu_serial
         self.cfg = cfg
         h = C.c_void_p()
         _check(lib().g5_bfs_create(graph._h, C.byref(cfg), C.byref(h)), "g5_bfs_create")

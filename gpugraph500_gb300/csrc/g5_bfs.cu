@@ -43,8 +43,8 @@ constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
 constexpr int kChunkWords = 2048;  // bitmap words per compaction chunk
 constexpr int kWordsPerThread = kChunkWords / kBlock;
-constexpr uint64_t kTile = 256;    // frontier edges per top-down warp tile
-constexpr int kBuSerial = 8;       // entries a lane scans alone before the warp helps
+constexpr uint32_t kTileDefault = 256;  // frontier edges per top-down warp tile
+constexpr int kBuSerialDefault = 8;     // entries a lane scans alone before the warp helps
 constexpr uint32_t kHeavy = 64;    // degree above which top-down sets the parent itself
 
 enum : int32_t { DIR_TD = 0, DIR_BU = 1 };
@@ -98,6 +98,9 @@ struct BfsArgs {
     uint32_t *ulist;       // sorted unvisited vertices for a bottom-up level
     uint64_t *chunk_u;     // per chunk: unvisited vertices after the level
     int parent_mode;       // 0 atomicMin, 1 heavy atomicMin + fix-up, 2 first writer + fix-up
+    uint64_t tile;         // frontier edges per top-down warp tile (a power of two >= 32)
+    int tile_shift;        // log2(tile)
+    int bu_serial;         // entries a bottom-up lane scans alone before the warp helps
     uint64_t max_tiles;
     uint64_t *chunk_n;
     uint64_t *chunk_m;
@@ -167,7 +170,7 @@ __global__ void k_init(BfsArgs a)
     }
     __syncthreads();
     if (!s_ok) return;
-    const uint64_t tiles = ((uint64_t)s_deg + kTile - 1) / kTile;
+    const uint64_t tiles = ((uint64_t)s_deg + a.tile - 1) >> a.tile_shift;
     for (uint64_t t = threadIdx.x; t < tiles; t += blockDim.x) a.tile_start[t] = 0;
 }
 
@@ -181,14 +184,14 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
     const uint64_t gw = (uint64_t)blockIdx.x * kWarps + wib;
     const uint64_t nw = (uint64_t)gridDim.x * kWarps;
     const uint64_t mf = a.st->mf, nf = a.st->nf;
-    const uint64_t ntiles = (mf + kTile - 1) / kTile;
+    const uint64_t ntiles = (mf + a.tile - 1) >> a.tile_shift;
     if (ntiles > a.max_tiles) {
         if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(&a.st->err, G5_DEVERR_CAPACITY);
         return;
     }
     for (uint64_t t = gw; t < ntiles; t += nw) {
-        const uint64_t e0 = t * kTile;
-        const uint64_t e1 = min(e0 + kTile, mf);
+        const uint64_t e0 = t << a.tile_shift;
+        const uint64_t e1 = min(e0 + a.tile, mf);
         uint64_t cur = a.tile_start[t];
         for (uint64_t gb = e0; gb < e1; gb += 32) {
             const uint64_t idx = cur + 1 + lane;
@@ -252,7 +255,7 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
 // just discovered; each takes the first frontier neighbour of its adjacency.
 // Either way the parent is the smallest neighbour in the frontier.
 // Warp-collective search of each active lane's adjacency [s, e) for its
-// first vertex in the frontier: every lane scans its first kBuSerial entries
+// first vertex in the frontier: every lane scans its first bu_serial entries
 // alone (four independent loads at a time), then the warp finishes the longer
 // lists one at a time, 32 entries per step (the first set ballot bit is the
 // smallest index).  Returns found / par per lane and the entries read.
@@ -266,7 +269,7 @@ __device__ __forceinline__ void first_hit(const BfsArgs &a, bool mine, Off s, Of
     found = false;
     par = 0;
     Off j = s;
-    const Off lim = min(e, (Off)(s + kBuSerial));
+    const Off lim = min(e, (Off)(s + a.bu_serial));
     while (j < lim && !found) {
         uint32_t u[4];
         bool h[4];
@@ -817,8 +820,8 @@ __global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
                     a.queue[p] = (uint32_t)v;
                     a.qoff[p] = mp;
                     a.qbase[p] = a.row_off[v] - (int64_t)mp;
-                    uint64_t t = (mp + kTile - 1) / kTile;
-                    const uint64_t tend = (mp + d + kTile - 1) / kTile;
+                    uint64_t t = (mp + a.tile - 1) >> a.tile_shift;
+                    const uint64_t tend = (mp + d + a.tile - 1) >> a.tile_shift;
                     for (; t < tend && t < a.max_tiles; ++t) a.tile_start[t] = (uint32_t)p;
                 }
             }
@@ -1093,7 +1096,10 @@ g5_status alloc_ws(g5_bfs *b)
     a.nnz = g->nnz;
     a.nwords = (uint64_t)((n + 31) / 32);
     a.nchunks = (uint32_t)((a.nwords + kChunkWords - 1) / kChunkWords);
-    a.max_tiles = (uint64_t)g->nnz / kTile + 2;
+    a.tile = b->cfg.tile_edges;
+    a.tile_shift = __builtin_ctz(b->cfg.tile_edges);
+    a.bu_serial = b->cfg.bu_serial;
+    a.max_tiles = (uint64_t)g->nnz / a.tile + 2;
     a.max_levels = b->cfg.max_levels;
     G5_CUDA(cudaMalloc(&b->deg, sizeof(uint32_t) * (size_t)n));
     G5_CUDA(cudaMalloc(&b->bitmaps, sizeof(uint32_t) * 3 * a.nwords));
@@ -1246,6 +1252,8 @@ void g5_bfs_config_default(g5_bfs_config *cfg)
     cfg->want_levels = 0;
     cfg->profile = 0;
     cfg->parent_mode = 0;
+    cfg->tile_edges = kTileDefault;
+    cfg->bu_serial = kBuSerialDefault;
 }
 
 g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
@@ -1258,7 +1266,8 @@ g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
     else g5_bfs_config_default(&b->cfg);
     if (b->cfg.max_levels < 2) b->cfg.max_levels = 2;
     if (b->cfg.codec < 0 || b->cfg.codec > 2 || b->cfg.alpha <= 0 || b->cfg.beta <= 0 ||
-        b->cfg.parent_mode < 0 || b->cfg.parent_mode > 2) {
+        b->cfg.parent_mode < 0 || b->cfg.parent_mode > 2 || b->cfg.tile_edges < 32 ||
+        b->cfg.tile_edges > 4096 || (b->cfg.tile_edges & (b->cfg.tile_edges - 1)) != 0 || b->cfg.bu_serial < 1 || b->cfg.bu_serial > 64) {
         delete b;
         return G5_ERR_INVALID_ARG;
     }

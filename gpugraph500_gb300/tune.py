@@ -1,11 +1,14 @@
-"""Autotuner for the direction-switch thresholds.
+"""Autotuner for the direction-switch thresholds and the load-balancing sizes.
 
 Beamer's alpha/beta (SC'12) were tuned for CPUs; on a GPU the cost of a
 top-down edge and of a bottom-up probe differ, so the thresholds are picked by
 measurement: every (alpha, beta) pair of a small grid runs a sample of roots,
-and the pair with the best harmonic-mean TEPS wins.  Searches are timed with
-the library's CUDA events.  The result is cached per (graph size, edge count)
-in memory for the process.
+and the pair with the best harmonic-mean TEPS wins.  A second stage then picks,
+with those thresholds, the top-down tile size (frontier edges per warp tile)
+and the bottom-up serial length (entries a lane scans alone before its warp
+takes over the row: the cut-off between the lane and warp degree bins).
+Searches are timed with the library's CUDA events.  Results are cached per
+(graph size, edge count) in memory for the process.
 """
 from __future__ import annotations
 
@@ -14,6 +17,8 @@ from typing import Sequence
 
 ALPHAS = (4.0, 14.0, 40.0, 120.0, 400.0)
 BETAS = (12.0, 24.0, 64.0, 200.0)
+TILES = (128, 256, 512, 1024)
+SERIALS = (4, 8, 16)
 
 _cache: dict = {}
 
@@ -70,3 +75,31 @@ def tune_batch(g5, torch, graphs, roots_per_graph, alphas=ALPHAS, betas=BETAS) -
     results.sort()
     return {"alpha": results[0][1], "beta": results[0][2], "ms": results[0][0],
             "grid": [{"alpha": a, "beta": b, "ms": round(m, 3)} for m, a, b in results]}
+
+
+def tune_sizes(g5, graph, roots: Sequence[int], nedges: Sequence[int], alpha: float, beta: float,
+               tiles=TILES, serials=SERIALS, reps: int = 2) -> dict:
+    """Best (tile_edges, bu_serial) for the one-root search with fixed thresholds."""
+    key = ("sizes", graph.n, graph.nnz, alpha, beta, tuple(tiles), tuple(serials))
+    if key in _cache:
+        return _cache[key]
+    results = []
+    for t, sr in itertools.product(tiles, serials):
+        bfs = g5.CudaBFS(graph, alpha=alpha, beta=beta, tile_edges=t, bu_serial=sr)
+        best = None
+        for _ in range(reps):
+            ts = []
+            for r in roots:
+                code = bfs.run(int(r), None, None, stats=True)
+                if code != 0:
+                    raise g5.G5Error(code, "tune")
+                ts.append(bfs.stats.device_ms)
+            v = _hmean_teps(ts, nedges)
+            best = v if best is None else max(best, v)
+        bfs.close()
+        results.append((best, t, sr))
+    results.sort(reverse=True)
+    out = {"tile_edges": results[0][1], "bu_serial": results[0][2], "gteps": results[0][0],
+           "grid": [{"tile_edges": t, "bu_serial": sr, "gteps": round(v, 2)} for v, t, sr in results]}
+    _cache[key] = out
+    return out

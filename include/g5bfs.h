@@ -147,6 +147,11 @@ typedef struct g5_bfs_config {
                             degree > 64, a scan of the adjacency for the rest;
                             2 as 1, but the first discoverer's atomicMin stands
                             unless the vertex is reached twice               */
+    uint32_t tile_edges; /* frontier edges per top-down warp tile: a power of
+                            two from 32 to 4096 (default 256)                  */
+    int bu_serial;       /* adjacency entries a bottom-up lane scans alone
+                            before its warp scans the rest together: 1..64
+                            (default 8)                                        */
 } g5_bfs_config;
 
 /* Fills the defaults: alpha 14, beta 24, no codec, threshold 64, CUDA graph,

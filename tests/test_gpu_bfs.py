@@ -71,6 +71,26 @@ def test_direction_extremes():
         run_all_roots(ro, col, roots, alpha=alpha, beta=beta)
 
 
+@pytest.mark.parametrize("tile,serial", [(32, 1), (128, 4), (1024, 16), (4096, 64)])
+def test_tile_and_serial_sizes(tile, serial):
+    """Every top-down tile size and bottom-up serial length gives the same parents."""
+    e = orc.kronecker(12)
+    ro, col = orc.build_csr(1 << 12, e)
+    roots = orc.select_roots(ro, 4)
+    for alpha, beta in ((14.0, 24.0), (1e-6, 1e-6)):
+        run_all_roots(ro, col, roots, alpha=alpha, beta=beta, tile_edges=tile, bu_serial=serial)
+
+
+def test_bad_sizes_rejected():
+    e = orc.kronecker(8)
+    ro, col = orc.build_csr(1 << 8, e)
+    g = g5.Graph.from_csr(ro, col)
+    for kw in ({"tile_edges": 48}, {"tile_edges": 96}, {"tile_edges": 8192}, {"bu_serial": 0}, {"bu_serial": 65}):
+        with pytest.raises(g5.G5Error):
+            g5.CudaBFS(g, **kw)
+    g.close()
+
+
 @pytest.mark.parametrize("mode", [0, 1, 2])
 def test_parent_modes_agree(mode):
     """The three top-down parent strategies give the same (reference) parents."""
