@@ -670,9 +670,17 @@ def bench_codec(g5, torch, args):
     dout = torch.empty(g5.Codec.bound(maxn) + 64, dtype=torch.int32, device="cuda")
     back = torch.empty(maxn + 256, dtype=torch.int32, device="cuda")
     stats = {}
+    # all queues concatenated, for the batched calls
+    cat = np.concatenate(queues)
+    in_off = np.zeros(len(queues) + 1, np.uint64)
+    in_off[1:] = np.cumsum([len(q) for q in queues])
+    bin_ = torch.from_numpy(cat.view(np.int32)).cuda()
+    bout = torch.empty(g5.Codec.batch_bound(in_off) + 64, dtype=torch.int32, device="cuda")
+    bback = torch.empty(len(cat) + 256, dtype=torch.int32, device="cuda")
     for mode, name in ((g5.CODEC_D4, "d4"), (g5.CODEC_DM, "dm")):
         enc_s = dec_s = 0.0
         words = vals = 0
+        singles = []
         for q in queues:
             din[: len(q)] = torch.from_numpy(q.view(np.int32)).cuda()
             torch.cuda.synchronize()
@@ -686,10 +694,29 @@ def bench_codec(g5, torch, args):
             e1.record(); torch.cuda.synchronize()
             dec_s += e0.elapsed_time(e1) * 1e-3
             assert m == len(q)
+            singles.append(dout[:w].cpu().numpy())
             words += w
             vals += len(q)
         stats[name] = {"encode_GBps": 4 * vals / enc_s / 1e9, "decode_GBps": 4 * vals / dec_s / 1e9,
                        "ratio_words_per_value": words / vals}
+        # the same queues in one batched call each way (host set-up included)
+        cs = torch.cuda.current_stream().cuda_stream
+        times = {"enc": [], "dec": []}
+        for rep in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out_off, bw = c.encode_batch(bin_, in_off, bout, mode=mode, stream=cs)
+            times["enc"].append(time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            c.decode_batch(bout, out_off[:-1], bw, np.diff(in_off), bback, mode=mode, stream=cs)
+            times["dec"].append(time.perf_counter() - t0)
+        hb = bout.cpu().numpy()
+        same = all(np.array_equal(hb[int(o):int(o) + int(w)], sg) for o, w, sg in zip(out_off[:-1], bw, singles))
+        same &= bool(torch.equal(bback[:len(cat)].cpu(), torch.from_numpy(cat.view(np.int32))))
+        stats[name]["batched"] = {"encode_GBps": 4 * vals / min(times["enc"]) / 1e9,
+                                  "decode_GBps": 4 * vals / min(times["dec"]) / 1e9,
+                                  "streams_equal_single_calls": bool(same),
+                                  "timing": "one call for all queues, wall time incl. host set-up, best of 3"}
     c.close()
     gr.close()
     # bitmap OR: 8 sources of 2^24 bits, densities 1..60 %, 12 independent sets

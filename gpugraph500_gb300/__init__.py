@@ -114,6 +114,9 @@ SIGNATURES = {
     "g5_codec_bound": (_SZ, [_SZ]),
     "g5_codec_create": (_I, [_SZ, C.POINTER(_P)]),
     "g5_codec_destroy": (_I, [_P]),
+    "g5_codec_batch_bound": (_SZ, [_P, _I]),
+    "g5_codec_encode_batch": (_I, [_P, _P, _P, _I, _P, _P, _P, _U32, _I, _P]),
+    "g5_codec_decode_batch": (_I, [_P, _P, _P, _P, _P, _I, _P, _P, _P, _U32, _I, _P]),
     "g5_codec_encode": (_I, [_P, _P, _SZ, _P, C.POINTER(_SZ), _I, _P]),
     "g5_codec_decode": (_I, [_P, _P, _SZ, _P, _SZ, C.POINTER(_SZ), _I, _P]),
     "g5_codec_encode_noalloc": (_I, [_P, _SZ, _P, C.POINTER(_SZ), _I, _P]),
@@ -361,6 +364,41 @@ class Codec:
         _check(lib().g5_codec_decode(self._h, _ptr(in_dev), words, _ptr(out_dev), out_cap, C.byref(n),
                                      mode, stream), "g5_codec_decode")
         return n.value
+
+    @staticmethod
+    def batch_bound(in_off: np.ndarray) -> int:
+        """Output words encode_batch needs for queues with these offsets (k+1 entries)."""
+        in_off = np.ascontiguousarray(in_off, dtype=np.uint64)
+        return lib().g5_codec_batch_bound(_ptr(in_off), len(in_off) - 1)
+
+    def encode_batch(self, in_dev, in_off: np.ndarray, out_dev, raw_threshold: int = 0, mode: int = CODEC_D4,
+                     stream=None) -> tuple[np.ndarray, np.ndarray]:
+        """Encodes k concatenated queues in one launch set; returns (out_off, out_words)."""
+        in_off = np.ascontiguousarray(in_off, dtype=np.uint64)
+        k = len(in_off) - 1
+        out_off = np.zeros(k + 1, np.uint64)
+        words = np.zeros(max(k, 1), np.uint64)
+        _check(lib().g5_codec_encode_batch(self._h, _ptr(in_dev), _ptr(in_off), k, _ptr(out_dev), _ptr(out_off),
+                                           _ptr(words), raw_threshold, mode, stream), "g5_codec_encode_batch")
+        return out_off, words[:k]
+
+    def decode_batch(self, in_dev, in_off: np.ndarray, words: np.ndarray, n: np.ndarray, out_dev,
+                     raw_threshold: int = 0, mode: int = CODEC_D4, stream=None) -> tuple[np.ndarray, np.ndarray]:
+        """Decodes k streams in one launch set; returns (out_off, per-stream ok flags).
+        Raises G5Error if a stream is malformed (the flags say which)."""
+        in_off = np.ascontiguousarray(in_off, dtype=np.uint64)
+        words = np.ascontiguousarray(words, dtype=np.uint64)
+        n = np.ascontiguousarray(n, dtype=np.uint64)
+        k = len(n)
+        out_off = np.zeros(k + 1, np.uint64)
+        ok = np.zeros(max(k, 1), np.int32)
+        code = lib().g5_codec_decode_batch(self._h, _ptr(in_dev), _ptr(in_off), _ptr(words), _ptr(n), k,
+                                           _ptr(out_dev), _ptr(out_off), _ptr(ok), raw_threshold, mode, stream)
+        if code != 0:
+            err = G5Error(code, "g5_codec_decode_batch")
+            err.stream_ok = ok[:k].copy()
+            raise err
+        return out_off, ok[:k]
 
     def close(self) -> None:
         if self._h:

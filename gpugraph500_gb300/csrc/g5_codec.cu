@@ -31,6 +31,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "g5_codec_dev.cuh"
 #include "g5_common.cuh"
@@ -682,6 +683,433 @@ __global__ void k_dec_tail(const uint32_t *in, uint64_t *scal, uint64_t cap, uin
     }
 }
 
+// ---- many streams in one launch set -------------------------------------------------------
+//
+// k queues (or k streams) are concatenated; each kernel below walks the global
+// index space of all streams' miniblocks, groups or vectors and finds the
+// stream of an index by a binary search over the per-stream first indices, so
+// the k streams cost one launch set instead of k.  Each stream's bytes are
+// exactly those of a single-stream call.
+
+struct BStream {
+    uint64_t in_off;   // encode: first input value; decode: first stream word (multiple of 4)
+    uint64_t out_off;  // encode: first output word (multiple of 4); decode: first output value
+    uint64_t n;        // values
+    uint64_t words;    // decode: stream length; encode: written by k_benc_tail
+    uint64_t nmb;      // miniblocks of the block part (0 for a raw stream)
+    uint64_t nv;       // decode: whole 16-byte vectors of the stream
+    uint64_t blkend;   // decode: word after the block part
+    uint32_t raw;      // raw copy (plugin threshold semantics)
+    uint32_t err;      // G5_DEVERR_* bits
+};
+
+// The last stream s < k with first[s] <= x (empty streams share a first
+// index with the next one, so x always lands in a stream that holds it).
+__device__ __forceinline__ int find_stream(const uint64_t *first, int k, uint64_t x)
+{
+    int lo = 0, hi = k - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (first[mid] <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// load_vectors for an input of any alignment (queues start anywhere).
+__device__ __forceinline__ void load_vectors_any(const uint32_t *in, uint64_t k, uint4 &cur, uint4 &prev)
+{
+    const int lane = g5_lane();
+    const uint32_t *p = in + k * 128 + 4 * (uint64_t)lane;
+    cur = make_uint4(p[0], p[1], p[2], p[3]);
+    uint4 q;
+    q.x = __shfl_up_sync(0xFFFFFFFFu, cur.x, 1);
+    q.y = __shfl_up_sync(0xFFFFFFFFu, cur.y, 1);
+    q.z = __shfl_up_sync(0xFFFFFFFFu, cur.z, 1);
+    q.w = __shfl_up_sync(0xFFFFFFFFu, cur.w, 1);
+    if (lane == 0) q = k ? make_uint4(p[-4], p[-3], p[-2], p[-1]) : make_uint4(0, 0, 0, 0);
+    prev = q;
+}
+
+__global__ void __launch_bounds__(kB) k_benc_bits(const uint32_t *in, const BStream *bs, const uint64_t *mb0,
+                                                  int k, uint64_t total_mb, uint8_t *mb_bits, uint32_t *mb_len,
+                                                  int mode)
+{
+    const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
+    for (uint64_t kg = gw; kg < total_mb; kg += nw) {
+        const int s = find_stream(mb0, k, kg);
+        uint4 cur, prev;
+        load_vectors_any(in + bs[s].in_off, kg - mb0[s], cur, prev);
+        const uint4 d = deltas(cur, prev, mode);
+        uint32_t acc = d.x | d.y | d.z | d.w;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) acc |= __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+        if (g5_lane() == 0) {
+            const uint32_t b = bits_of(acc);
+            mb_bits[kg] = (uint8_t)b;
+            mb_len[kg] = 4 * b;
+        }
+    }
+}
+
+// mb_off: exclusive prefix of the payload words over all miniblocks.
+__global__ void __launch_bounds__(kB) k_benc_pack(const uint32_t *in, const BStream *bs, const uint64_t *mb0,
+                                                  int k, uint64_t total_mb, const uint8_t *mb_bits,
+                                                  const uint32_t *mb_off, uint32_t *out, int mode)
+{
+    __shared__ uint4 s_d[kB / 32][32];
+    const int lane = g5_lane(), wib = threadIdx.x >> 5;
+    const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
+    for (uint64_t kg = gw; kg < total_mb; kg += nw) {
+        const int s = find_stream(mb0, k, kg);
+        const BStream &st = bs[s];
+        const uint64_t kl = kg - mb0[s];
+        const uint32_t base = mb_off[mb0[s]];
+        uint32_t *o = out + st.out_off;
+        const uint32_t b = mb_bits[kg];
+        const uint64_t off = 4 + 4 * (kl / 16 + 1) + (uint64_t)(mb_off[kg] - base);
+        if ((kl & 15) == 0 && lane < 4) {
+            uint32_t h = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint64_t kk = kl + 4 * lane + q;
+                const uint32_t bb = kk < st.nmb ? mb_bits[mb0[s] + kk] : 0u;
+                h |= bb << (24 - 8 * q);
+            }
+            o[4 + 4 * (kl / 16) + (uint64_t)(mb_off[kg] - base) + lane] = h;
+        }
+        uint4 cur, prev;
+        load_vectors_any(in + st.in_off, kl, cur, prev);
+        if (b == 32) {
+            reinterpret_cast<uint4 *>(o + off)[lane] = cur;
+            continue;
+        }
+        if (b == 0) continue;
+        s_d[wib][lane] = deltas(cur, prev, mode);
+        __syncwarp();
+        for (uint32_t idx = lane; idx < 4 * b; idx += 32) {
+            const uint32_t w = idx >> 2, l = idx & 3;
+            const uint32_t bit0 = 32 * w;
+            const uint32_t j0 = bit0 / b, j1 = (bit0 + 31) / b;
+            uint32_t word = 0;
+            for (uint32_t j = j0; j <= j1 && j < 32; ++j) {
+                const uint32_t dd = comp(s_d[wib][j], l);
+                const int sh = (int)(j * b) - (int)bit0;
+                word |= sh >= 0 ? (dd << sh) : (dd >> (-sh));
+            }
+            o[off + idx] = word;
+        }
+        __syncwarp();
+    }
+}
+
+// One warp per stream: raw copies, header words and the VariableByte tail;
+// the stream's length -> bs[s].words.  payload_total: sum of all payloads.
+__global__ void k_benc_tail(const uint32_t *in, BStream *bs, const uint64_t *mb0, int k, uint64_t total_mb,
+                            const uint32_t *mb_off, const uint32_t *payload_total, uint32_t *out)
+{
+    __shared__ uint32_t s_val[128];
+    __shared__ uint32_t s_bytes[(128 * 5 + 3) / 4 + 1];
+    const int lane = threadIdx.x;
+    for (int s = blockIdx.x; s < k; s += gridDim.x) {
+        BStream &st = bs[s];
+        const uint32_t *x = in + st.in_off;
+        uint32_t *o = out + st.out_off;
+        if (st.raw) {
+            for (uint64_t i = lane; i < st.n; i += 32) o[i] = x[i];
+            if (lane == 0) st.words = st.n;
+            continue;
+        }
+        const uint64_t nmb = st.nmb, n1 = nmb * 128, ngroups = (nmb + 15) / 16;
+        uint64_t payload = 0;
+        if (nmb) {
+            const uint64_t e = mb0[s] + nmb;
+            payload = (uint64_t)((e < total_mb ? mb_off[e] : *payload_total) - mb_off[mb0[s]]);
+        }
+        const uint64_t blkend = 4 + 4 * ngroups + payload;
+        const uint32_t nt = (uint32_t)(st.n - n1);
+        __syncwarp();
+        for (uint32_t i = lane; i < nt; i += 32) s_val[i] = x[n1 + i];
+        for (uint32_t i = lane; i < sizeof(s_bytes) / 4; i += 32) s_bytes[i] = 0;
+        __syncwarp();
+        if (lane == 0) {
+            o[0] = (uint32_t)n1;
+            o[1] = kCookie;
+            o[2] = kCookie;
+            o[3] = kCookie;
+            uint8_t *bb = reinterpret_cast<uint8_t *>(s_bytes);
+            uint32_t p = 0, prevv = 0;
+            for (uint32_t i = 0; i < nt; ++i) {
+                uint32_t v = s_val[i] - prevv;
+                prevv = s_val[i];
+                while (v >= 128u) {
+                    bb[p++] = (uint8_t)(v & 127u);
+                    v >>= 7;
+                }
+                bb[p++] = (uint8_t)(v | 128u);
+            }
+            const uint32_t tw = (p + 3) / 4;
+            s_val[0] = tw;
+            st.words = blkend + tw;
+        }
+        __syncwarp();
+        const uint32_t tw = s_val[0];
+        for (uint32_t i = lane; i < tw; i += 32) o[blkend + i] = s_bytes[i];
+    }
+}
+
+// Stream headers (one thread per stream): cookies and the block-part length.
+__global__ void k_bdec_prep(const uint32_t *in, BStream *bs, int k)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < k; s += gridDim.x * blockDim.x) {
+        BStream &st = bs[s];
+        st.err = 0;
+        st.blkend = 4;
+        if (st.raw) {
+            if (st.words != st.n) st.err |= G5_DEVERR_CORRUPT;
+            continue;
+        }
+        const uint32_t *x = in + st.in_off;
+        if (st.words < 4 || x[0] != st.nmb * 128 || x[1] != kCookie || x[2] != kCookie || x[3] != kCookie)
+            st.err |= G5_DEVERR_CORRUPT;
+    }
+}
+
+// jump[vg] = global vector after the group whose header is global vector vg,
+// or the sink (total_v) when that leaves the stream.
+__global__ void __launch_bounds__(kB) k_bdec_jump(const uint32_t *in, const BStream *bs, const uint64_t *v0,
+                                                  int k, uint64_t total_v, uint32_t *jump)
+{
+    for (uint64_t vg = (uint64_t)blockIdx.x * kB + threadIdx.x; vg <= total_v; vg += (uint64_t)gridDim.x * kB) {
+        uint32_t j = (uint32_t)total_v;
+        if (vg < total_v) {
+            const int s = find_stream(v0, k, vg);
+            const BStream &st = bs[s];
+            const uint64_t lv = vg - v0[s];
+            const uint4 h = reinterpret_cast<const uint4 *>(in + st.in_off)[lv];
+            const uint32_t hw[4] = {h.x, h.y, h.z, h.w};
+            uint32_t sum = 0;
+            bool ok = true;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int by = 0; by < 4; ++by) {
+                    const uint32_t b = (hw[q] >> (8 * by)) & 0xFF;
+                    ok &= b <= 32;
+                    sum += b;
+                }
+            if (ok && lv + 1 + sum < st.nv) j = (uint32_t)(vg + 1 + sum);
+        }
+        jump[vg] = j;
+    }
+}
+
+__global__ void __launch_bounds__(kB) k_bdec_lift(uint32_t *jump, uint64_t total_v, uint64_t stride, int r)
+{
+    const uint32_t *t = jump + stride * r;
+    uint32_t *t1 = jump + stride * (r + 1);
+    for (uint64_t i = (uint64_t)blockIdx.x * kB + threadIdx.x; i <= total_v; i += (uint64_t)gridDim.x * kB)
+        t1[i] = t[t[i]];
+}
+
+// Group positions (local vector index of each group header); the last group
+// of a stream gives the end of its block part.
+__global__ void __launch_bounds__(kB) k_bdec_pos(const uint32_t *in, BStream *bs, const uint64_t *g0,
+                                                 const uint64_t *v0, int k, uint64_t total_g, uint64_t total_v,
+                                                 const uint32_t *jump, uint64_t stride, int R, uint32_t *gpos)
+{
+    for (uint64_t gg = (uint64_t)blockIdx.x * kB + threadIdx.x; gg < total_g; gg += (uint64_t)gridDim.x * kB) {
+        const int s = find_stream(g0, k, gg);
+        BStream &st = bs[s];
+        const uint64_t g = gg - g0[s], ng = (st.nmb + 15) / 16;
+        uint64_t pos = v0[s] + 1;
+        for (int r = 0; r < R && pos < total_v; ++r)
+            if ((g >> r) & 1) pos = jump[stride * r + pos];
+        uint64_t lp = 0;
+        if (st.err || pos >= v0[s] + st.nv) {
+            atomicOr(&st.err, (uint32_t)G5_DEVERR_CORRUPT);
+        } else {
+            lp = pos - v0[s];
+            if (g == ng - 1) {
+                const uint64_t howmany = st.nmb - 16 * g;
+                const uint4 h = reinterpret_cast<const uint4 *>(in + st.in_off)[lp];
+                const uint32_t hw[4] = {h.x, h.y, h.z, h.w};
+                uint64_t sum = 0;
+                bool ok = true;
+                for (uint64_t i = 0; i < howmany; ++i) {
+                    const uint32_t b = (hw[i / 4] >> (24 - 8 * (i % 4))) & 0xFF;
+                    ok &= b <= 32;
+                    sum += b;
+                }
+                const uint64_t end = lp + 1 + sum;
+                if (!ok || end > st.nv) atomicOr(&st.err, (uint32_t)G5_DEVERR_CORRUPT);
+                else st.blkend = 4 * end;
+            }
+        }
+        gpos[gg] = (uint32_t)lp;
+    }
+}
+
+// Per miniblock lane sums (the first miniblock of a stream starts from zero,
+// so its sums are absolute and reset the scan).
+__global__ void __launch_bounds__(kB) k_bdec_sum(const uint32_t *in, const BStream *bs, const uint64_t *mb0,
+                                                 const uint64_t *g0, int k, uint64_t total_mb,
+                                                 const uint32_t *gpos, VecFlag *mb_sf, int mode)
+{
+    const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
+    for (uint64_t kg = gw; kg < total_mb; kg += nw) {
+        const int s = find_stream(mb0, k, kg);
+        const BStream &st = bs[s];
+        const uint64_t kl = kg - mb0[s];
+        VecFlag r;
+        r.v = make_uint4(0, 0, 0, 0);
+        r.f = 1;
+        if (!st.err) {
+            const uint32_t *x = in + st.in_off;
+            uint64_t off;
+            uint32_t b;
+            mb_locate(x, gpos + g0[s], kl, off, b);
+            const uint4 d = unpack_vec(x, off, b);
+            if (b == 32) {
+                r.v.x = __shfl_sync(0xFFFFFFFFu, d.x, 31);
+                r.v.y = __shfl_sync(0xFFFFFFFFu, d.y, 31);
+                r.v.z = __shfl_sync(0xFFFFFFFFu, d.z, 31);
+                r.v.w = __shfl_sync(0xFFFFFFFFu, d.w, 31);
+            } else {
+                uint32_t sx = d.x, sy = d.y, sz = d.z, sw = d.w;
+#pragma unroll
+                for (int o = 16; o; o >>= 1) {
+                    sx += __shfl_xor_sync(0xFFFFFFFFu, sx, o);
+                    sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
+                    sz += __shfl_xor_sync(0xFFFFFFFFu, sz, o);
+                    sw += __shfl_xor_sync(0xFFFFFFFFu, sw, o);
+                }
+                if (mode == G5_CODEC_DM) r.v = make_uint4(sw, sw, sw, sw);
+                else r.v = make_uint4(sx, sy, sz, sw);
+                r.f = kl == 0 ? 1u : 0u;
+            }
+        }
+        if (g5_lane() == 0) mb_sf[kg] = r;
+    }
+}
+
+__global__ void __launch_bounds__(kB) k_bdec_out(const uint32_t *in, const BStream *bs, const uint64_t *mb0,
+                                                 const uint64_t *g0, int k, uint64_t total_mb,
+                                                 const uint32_t *gpos, const VecFlag *mb_base, uint32_t *out,
+                                                 int mode)
+{
+    const int lane = g5_lane();
+    const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
+    for (uint64_t kg = gw; kg < total_mb; kg += nw) {
+        const int s = find_stream(mb0, k, kg);
+        const BStream &st = bs[s];
+        if (st.err) continue;
+        const uint64_t kl = kg - mb0[s];
+        const uint32_t *x = in + st.in_off;
+        uint64_t off;
+        uint32_t b;
+        mb_locate(x, gpos + g0[s], kl, off, b);
+        const uint4 d = unpack_vec(x, off, b);
+        const uint4 base = kl == 0 ? make_uint4(0, 0, 0, 0) : mb_base[kg].v;
+        uint4 v;
+        if (b == 32) {
+            v = d;
+        } else if (mode == G5_CODEC_DM) {
+            uint32_t c = d.w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, c, o);
+                if (lane >= o) c += y;
+            }
+            c += base.w;
+            uint32_t pc = __shfl_up_sync(0xFFFFFFFFu, c, 1);
+            if (lane == 0) pc = base.w;
+            v = make_uint4(d.x + pc, d.y + pc, d.z + pc, c);
+        } else {
+            uint32_t cx = d.x, cy = d.y, cz = d.z, cw = d.w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t yx = __shfl_up_sync(0xFFFFFFFFu, cx, o);
+                const uint32_t yy = __shfl_up_sync(0xFFFFFFFFu, cy, o);
+                const uint32_t yz = __shfl_up_sync(0xFFFFFFFFu, cz, o);
+                const uint32_t yw = __shfl_up_sync(0xFFFFFFFFu, cw, o);
+                if (lane >= o) {
+                    cx += yx;
+                    cy += yy;
+                    cz += yz;
+                    cw += yw;
+                }
+            }
+            v = make_uint4(cx + base.x, cy + base.y, cz + base.z, cw + base.w);
+        }
+        uint32_t *o = out + st.out_off + kl * 128 + 4 * (uint64_t)lane;  // any alignment
+        o[0] = v.x;
+        o[1] = v.y;
+        o[2] = v.z;
+        o[3] = v.w;
+    }
+}
+
+// One warp per stream: raw copies and the VariableByte tail; every stream
+// must decode to exactly its n values.
+__global__ void k_bdec_tail(const uint32_t *in, BStream *bs, int k, uint32_t *out)
+{
+    __shared__ uint32_t s_b[kTailMaxBytes / 4];
+    const int lane = threadIdx.x;
+    for (int s = blockIdx.x; s < k; s += gridDim.x) {
+        BStream &st = bs[s];
+        const uint32_t *x = in + st.in_off;
+        uint32_t *o = out + st.out_off;
+        if (st.err) continue;
+        if (st.raw) {
+            for (uint64_t i = lane; i < st.n; i += 32) o[i] = x[i];
+            continue;
+        }
+        const uint64_t n1 = st.nmb * 128;
+        const uint64_t tw = st.words > st.blkend ? st.words - st.blkend : 0;
+        if (tw * 4 > kTailMaxBytes) {
+            if (lane == 0) st.err |= G5_DEVERR_CORRUPT;
+            continue;
+        }
+        __syncwarp();
+        for (uint64_t i = lane; i < tw; i += 32) s_b[i] = x[st.blkend + i];
+        __syncwarp();
+        if (lane == 0) {
+            const uint8_t *bb = reinterpret_cast<const uint8_t *>(s_b);
+            uint64_t c = n1;
+            uint32_t prevv = 0, v = 0;
+            int shift = 0;
+            uint32_t err = 0;
+            for (uint64_t p = 0; p < tw * 4; ++p) {
+                const uint32_t ch = bb[p];
+                v |= (ch & 127u) << shift;
+                if (ch & 128u) {
+                    if (c >= st.n) {
+                        err |= G5_DEVERR_CORRUPT;
+                        break;
+                    }
+                    prevv += v;
+                    o[c++] = prevv;
+                    v = 0;
+                    shift = 0;
+                } else {
+                    shift += 7;
+                    if (shift > 28) {
+                        err |= G5_DEVERR_CORRUPT;
+                        break;
+                    }
+                }
+            }
+            if (c != st.n) err |= G5_DEVERR_CORRUPT;
+            st.err |= err;
+        }
+    }
+}
+
 int lift_levels_for(size_t max_n)
 {
     const size_t ng = (max_n / 128 + 15) / 16;
@@ -776,10 +1204,39 @@ void decode_launch_acc(CodecWork &w, const uint32_t *in, const uint64_t *words_d
 
 // ---- C ABI ----------------------------------------------------------------------------
 
+namespace {
+
+// Device buffers of the batched calls, grown on demand (contents not kept).
+struct BatchWs {
+    void *p[10] = {nullptr};
+    size_t cap[10] = {0};
+    enum { BS, IDX, BITS, LEN, JUMP, GPOS, SF, BASE, PART, CNT };
+    g5_status grow(int i, size_t bytes)
+    {
+        if (p[i] && cap[i] >= bytes) return G5_OK;
+        cudaFree(p[i]);
+        p[i] = nullptr;
+        cap[i] = 0;
+        if (cudaMalloc(&p[i], bytes ? bytes : 16) != cudaSuccess) return G5_ERR_OOM;
+        cap[i] = bytes;
+        return G5_OK;
+    }
+    void release()
+    {
+        for (int i = 0; i < 10; ++i) cudaFree(p[i]);
+        *this = BatchWs();
+    }
+};
+
+size_t round4(size_t w) { return (w + 3) & ~(size_t)3; }
+
+}  // namespace
+
 struct g5_codec {
     g5::CodecWork w;
     uint64_t *n_dev = nullptr;
     uint64_t *h_scal = nullptr;  // pinned
+    BatchWs bw;
 };
 
 extern "C" {
@@ -816,6 +1273,7 @@ g5_status g5_codec_destroy(g5_codec *c)
     g5::codec_work_free(c->w);
     cudaFree(c->n_dev);
     cudaFreeHost(c->h_scal);
+    c->bw.release();
     delete c;
     return G5_OK;
 }
@@ -854,6 +1312,170 @@ g5_status g5_codec_decode(g5_codec *c, const uint32_t *in_dev, size_t words, uin
     if (c->h_scal[g5::CS_ERR]) return G5_ERR_CORRUPT_STREAM;
     *out_n = (size_t)c->h_scal[g5::CS_N];
     return G5_OK;
+}
+
+size_t g5_codec_batch_bound(const uint64_t *in_off, int k)
+{
+    if (!in_off || k < 0) return 0;
+    size_t w = 0;
+    for (int q = 0; q < k; ++q) w += round4(g5::codec_bound((size_t)(in_off[q + 1] - in_off[q])));
+    return w;
+}
+
+g5_status g5_codec_encode_batch(g5_codec *c, const uint32_t *in_dev, const uint64_t *in_off, int k,
+                                uint32_t *out_dev, uint64_t *out_off, uint64_t *out_words,
+                                uint32_t raw_threshold, int mode, void *stream)
+{
+    if (!c || !in_off || !out_off || !out_words || k < 0 || !out_dev) return G5_ERR_INVALID_ARG;
+    if (mode != G5_CODEC_D4 && mode != G5_CODEC_DM) return G5_ERR_INVALID_ARG;
+    if ((uintptr_t)out_dev & 15) return G5_ERR_INVALID_ARG;
+    out_off[0] = 0;
+    if (k == 0) return G5_OK;
+    if (!in_dev || in_off[0] != 0) return G5_ERR_INVALID_ARG;
+    for (int q = 0; q < k; ++q)
+        if (in_off[q + 1] < in_off[q]) return G5_ERR_INVALID_ARG;
+    if (in_off[k] > ((uint64_t)1 << 31)) return G5_ERR_CAPACITY;  // payload offsets are 32-bit
+    std::vector<g5::BStream> hb((size_t)k);
+    std::vector<uint64_t> mb0((size_t)k + 1);
+    uint64_t total_mb = 0;
+    for (int q = 0; q < k; ++q) {
+        g5::BStream &b = hb[q];
+        memset(&b, 0, sizeof b);
+        b.in_off = in_off[q];
+        b.out_off = out_off[q];
+        b.n = in_off[q + 1] - in_off[q];
+        b.raw = raw_threshold && b.n <= raw_threshold;
+        b.nmb = b.raw ? 0 : b.n / 128;
+        out_off[q + 1] = out_off[q] + round4(g5::codec_bound((size_t)b.n));
+        mb0[q] = total_mb;
+        total_mb += b.nmb;
+    }
+    mb0[k] = total_mb;
+    BatchWs &w = c->bw;
+    const int grid = c->w.grid;
+    G5_TRY(w.grow(BatchWs::BS, sizeof(g5::BStream) * (size_t)k));
+    G5_TRY(w.grow(BatchWs::IDX, sizeof(uint64_t) * ((size_t)k + 1)));
+    G5_TRY(w.grow(BatchWs::BITS, total_mb + 1));
+    G5_TRY(w.grow(BatchWs::LEN, sizeof(uint32_t) * (total_mb + 1)));
+    G5_TRY(w.grow(BatchWs::PART, sizeof(uint32_t) * ((size_t)grid + 1)));
+    G5_TRY(w.grow(BatchWs::CNT, sizeof(uint64_t)));
+    g5::BStream *bs = (g5::BStream *)w.p[BatchWs::BS];
+    uint64_t *idx = (uint64_t *)w.p[BatchWs::IDX], *cnt = (uint64_t *)w.p[BatchWs::CNT];
+    uint8_t *bits = (uint8_t *)w.p[BatchWs::BITS];
+    uint32_t *len = (uint32_t *)w.p[BatchWs::LEN], *part = (uint32_t *)w.p[BatchWs::PART];
+    cudaStream_t s = (cudaStream_t)stream;
+    G5_CUDA(cudaMemcpyAsync(bs, hb.data(), sizeof(g5::BStream) * (size_t)k, cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaMemcpyAsync(idx, mb0.data(), sizeof(uint64_t) * ((size_t)k + 1), cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaMemcpyAsync(cnt, &mb0[k], sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaMemsetAsync(part + grid, 0, sizeof(uint32_t), s));
+    if (total_mb) {
+        g5::k_benc_bits<<<grid, g5::kB, 0, s>>>(in_dev, bs, idx, k, total_mb, bits, len, mode);
+        g5::k_scan_red<g5::AddU32><<<grid, g5::kB, 0, s>>>(len, cnt, part);
+        g5::k_scan_top<g5::AddU32><<<1, g5::kB, 0, s>>>(part, grid, part + grid);
+        g5::k_scan_down<g5::AddU32><<<grid, g5::kB, 0, s>>>(len, len, cnt, part);
+        g5::k_benc_pack<<<grid, g5::kB, 0, s>>>(in_dev, bs, idx, k, total_mb, bits, len, out_dev, mode);
+    }
+    g5::k_benc_tail<<<std::min(k, 65535), 32, 0, s>>>(in_dev, bs, idx, k, total_mb, len, part + grid, out_dev);
+    G5_CUDA(cudaGetLastError());
+    G5_CUDA(cudaMemcpyAsync(hb.data(), bs, sizeof(g5::BStream) * (size_t)k, cudaMemcpyDeviceToHost, s));
+    G5_CUDA(cudaStreamSynchronize(s));
+    for (int q = 0; q < k; ++q) out_words[q] = hb[q].words;
+    return G5_OK;
+}
+
+g5_status g5_codec_decode_batch(g5_codec *c, const uint32_t *in_dev, const uint64_t *in_off,
+                                const uint64_t *words, const uint64_t *n, int k, uint32_t *out_dev,
+                                uint64_t *out_off, int *stream_ok, uint32_t raw_threshold, int mode,
+                                void *stream)
+{
+    if (!c || !in_off || !words || !n || !out_off || k < 0) return G5_ERR_INVALID_ARG;
+    if (mode != G5_CODEC_D4 && mode != G5_CODEC_DM) return G5_ERR_INVALID_ARG;
+    out_off[0] = 0;
+    if (k == 0) return G5_OK;
+    if (!in_dev || !out_dev || ((uintptr_t)in_dev & 15)) return G5_ERR_INVALID_ARG;
+    std::vector<g5::BStream> hb((size_t)k);
+    std::vector<uint64_t> mb0((size_t)k + 1), g0((size_t)k + 1), v0((size_t)k + 1);
+    uint64_t total_mb = 0, total_g = 0, total_v = 0;
+    int max_ng = 0;
+    for (int q = 0; q < k; ++q) {
+        if (in_off[q] % 4) return G5_ERR_INVALID_ARG;  // streams start 16-byte aligned
+        g5::BStream &b = hb[q];
+        memset(&b, 0, sizeof b);
+        b.in_off = in_off[q];
+        b.out_off = out_off[q];
+        b.n = n[q];
+        b.words = words[q];
+        // plugin semantics: raw when n <= thr or the stream is as long as n
+        b.raw = raw_threshold && (b.n <= raw_threshold || b.words == b.n);
+        b.nmb = b.raw ? 0 : b.n / 128;
+        b.nv = b.raw ? 0 : b.words / 4;
+        out_off[q + 1] = out_off[q] + b.n;
+        mb0[q] = total_mb;
+        g0[q] = total_g;
+        v0[q] = total_v;
+        const uint64_t ng = (b.nmb + 15) / 16;
+        total_mb += b.nmb;
+        total_g += ng;
+        total_v += b.nv;
+        max_ng = std::max<int>(max_ng, (int)std::min<uint64_t>(ng, 1u << 30));
+    }
+    mb0[k] = total_mb;
+    g0[k] = total_g;
+    v0[k] = total_v;
+    if (total_v >= ((uint64_t)1 << 32) - 2 || out_off[k] > ((uint64_t)1 << 40)) return G5_ERR_CAPACITY;
+    int R = 1;
+    while (((uint64_t)1 << R) < (uint64_t)max_ng + 1) ++R;
+    const uint64_t stride = total_v + 1;
+    BatchWs &w = c->bw;
+    const int grid = c->w.grid;
+    G5_TRY(w.grow(BatchWs::BS, sizeof(g5::BStream) * (size_t)k));
+    G5_TRY(w.grow(BatchWs::IDX, sizeof(uint64_t) * 3 * ((size_t)k + 1)));
+    G5_TRY(w.grow(BatchWs::JUMP, sizeof(uint32_t) * stride * (size_t)R));
+    G5_TRY(w.grow(BatchWs::GPOS, sizeof(uint32_t) * (total_g + 1)));
+    G5_TRY(w.grow(BatchWs::SF, sizeof(g5::VecFlag) * (total_mb + 1)));
+    G5_TRY(w.grow(BatchWs::BASE, sizeof(g5::VecFlag) * (total_mb + 1)));
+    G5_TRY(w.grow(BatchWs::PART, sizeof(g5::VecFlag) * ((size_t)grid + 1)));
+    G5_TRY(w.grow(BatchWs::CNT, sizeof(uint64_t)));
+    g5::BStream *bs = (g5::BStream *)w.p[BatchWs::BS];
+    uint64_t *idx = (uint64_t *)w.p[BatchWs::IDX], *cnt = (uint64_t *)w.p[BatchWs::CNT];
+    uint64_t *dmb0 = idx, *dg0 = idx + (k + 1), *dv0 = idx + 2 * (k + 1);
+    uint32_t *jump = (uint32_t *)w.p[BatchWs::JUMP], *gpos = (uint32_t *)w.p[BatchWs::GPOS];
+    g5::VecFlag *sf = (g5::VecFlag *)w.p[BatchWs::SF], *base = (g5::VecFlag *)w.p[BatchWs::BASE];
+    g5::VecFlag *part = (g5::VecFlag *)w.p[BatchWs::PART];
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<uint64_t> allidx;
+    allidx.reserve(3 * ((size_t)k + 1));
+    allidx.insert(allidx.end(), mb0.begin(), mb0.end());
+    allidx.insert(allidx.end(), g0.begin(), g0.end());
+    allidx.insert(allidx.end(), v0.begin(), v0.end());
+    G5_CUDA(cudaMemcpyAsync(bs, hb.data(), sizeof(g5::BStream) * (size_t)k, cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaMemcpyAsync(idx, allidx.data(), sizeof(uint64_t) * allidx.size(), cudaMemcpyHostToDevice, s));
+    G5_CUDA(cudaMemcpyAsync(cnt, &mb0[k], sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    const int pgrid = std::max(1, std::min(grid, (k + g5::kB - 1) / g5::kB));
+    g5::k_bdec_prep<<<pgrid, g5::kB, 0, s>>>(in_dev, bs, k);
+    if (total_g) {
+        g5::k_bdec_jump<<<grid, g5::kB, 0, s>>>(in_dev, bs, dv0, k, total_v, jump);
+        for (int r = 0; r + 1 < R; ++r) g5::k_bdec_lift<<<grid, g5::kB, 0, s>>>(jump, total_v, stride, r);
+        g5::k_bdec_pos<<<grid, g5::kB, 0, s>>>(in_dev, bs, dg0, dv0, k, total_g, total_v, jump, stride, R, gpos);
+    }
+    if (total_mb) {
+        g5::k_bdec_sum<<<grid, g5::kB, 0, s>>>(in_dev, bs, dmb0, dg0, k, total_mb, gpos, sf, mode);
+        g5::k_scan_red<g5::ResetAdd><<<grid, g5::kB, 0, s>>>(sf, cnt, part);
+        g5::k_scan_top<g5::ResetAdd><<<1, g5::kB, 0, s>>>(part, grid, nullptr);
+        g5::k_scan_down<g5::ResetAdd><<<grid, g5::kB, 0, s>>>(sf, base, cnt, part);
+        g5::k_bdec_out<<<grid, g5::kB, 0, s>>>(in_dev, bs, dmb0, dg0, k, total_mb, gpos, base, out_dev, mode);
+    }
+    g5::k_bdec_tail<<<std::min(k, 65535), 32, 0, s>>>(in_dev, bs, k, out_dev);
+    G5_CUDA(cudaGetLastError());
+    G5_CUDA(cudaMemcpyAsync(hb.data(), bs, sizeof(g5::BStream) * (size_t)k, cudaMemcpyDeviceToHost, s));
+    G5_CUDA(cudaStreamSynchronize(s));
+    bool all = true;
+    for (int q = 0; q < k; ++q) {
+        const bool ok = hb[q].err == 0;
+        if (stream_ok) stream_ok[q] = ok ? 1 : 0;
+        all &= ok;
+    }
+    return all ? G5_OK : G5_ERR_CORRUPT_STREAM;
 }
 
 }  // extern "C"

@@ -346,6 +346,35 @@ g5_status g5_codec_encode(g5_codec *c, const uint32_t *in_dev, size_t n, uint32_
 g5_status g5_codec_decode(g5_codec *c, const uint32_t *in_dev, size_t words, uint32_t *out_dev,
                           size_t out_cap, size_t *out_n, int mode, void *stream);
 
+/* Many queues per call, one launch set for all of them (the reference's
+ * compress/decompress run once per queue, vreduce.hpp:192-528,
+ * globalbfs.hh:853-938; a level's queues or a microbench's queue set go
+ * through the GPU together).  The streams are byte for byte those of
+ * g5_codec_encode / g5_plugin_compress on each queue.
+ *
+ * encode_batch: queue q is in_dev[in_off[q] .. in_off[q+1]) (in_off on the
+ * host, k+1 entries, in_off[0] = 0, total at most 2^31 values); stream q is
+ * written at out_dev + out_off[q] (out_off filled by the call, k+1 entries:
+ * the exclusive prefix of g5_codec_bound rounded up to 4 words, so every
+ * stream starts 16-byte aligned; out_dev needs g5_codec_batch_bound words);
+ * out_words[q] receives its length.  raw_threshold > 0 gives the plugin's
+ * raw copy for queues of at most that many values (cpusimd.hh:102-117).
+ *
+ * decode_batch: stream q is in_dev[in_off[q] .. + words[q]) (in_off multiples
+ * of 4) and holds n[q] values (the caller passes n out of band, as the
+ * reference plugin does); value i of queue q goes to out_dev[out_off[q] + i]
+ * (out_off filled: the exclusive prefix of n).  stream_ok (nullable, k
+ * entries) gets 1 per stream that decoded to exactly n[q] values, 0 per
+ * malformed stream; the call returns G5_ERR_CORRUPT_STREAM if any failed. */
+size_t g5_codec_batch_bound(const uint64_t *in_off, int k);
+g5_status g5_codec_encode_batch(g5_codec *c, const uint32_t *in_dev, const uint64_t *in_off, int k,
+                                uint32_t *out_dev, uint64_t *out_off, uint64_t *out_words,
+                                uint32_t raw_threshold, int mode, void *stream);
+g5_status g5_codec_decode_batch(g5_codec *c, const uint32_t *in_dev, const uint64_t *in_off,
+                                const uint64_t *words, const uint64_t *n, int k, uint32_t *out_dev,
+                                uint64_t *out_off, int *stream_ok, uint32_t raw_threshold, int mode,
+                                void *stream);
+
 /* Same stream as g5_codec_encode, for callers that cannot allocate device
  * memory: a serving loop that must never block on or fragment the CUDA
  * allocator between requests, or a process whose device memory belongs to
