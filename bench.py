@@ -600,6 +600,15 @@ def bench_big(g5, torch, args, tune, ab):
     t0 = time.time()
     g = g5.Graph.kronecker(args.big_scale)
     build_s = time.time() - t0
+    res = plain_vs_batched(g5, torch, g, args, tune, ab)
+    g.close()
+    res.update({"scale": args.big_scale, "graph_build_s": round(build_s, 2)})
+    return res
+
+
+def plain_vs_batched(g5, torch, g, args, tune, ab):
+    """64 roots on graph g: harmonic-mean GTEPS of the plain search, then the
+    batched search over the same roots (parents checked against plain)."""
     roots = g5.select_roots(g, 64)
     bfs = g5.CudaBFS(g, alpha=ab[0], beta=ab[1], use_graph=not args.host_loop)
     nedges, ms = [], []
@@ -614,9 +623,7 @@ def bench_big(g5, torch, args, tune, ab):
     plain = hmean([ne / (t * 1e-3) / 1e9 for ne, t in zip(nedges, ms)])
     batched = bench_batched(g5, torch, g, roots, nedges, args, tune, bfs)
     bfs.close()
-    g.close()
-    return {"scale": args.big_scale, "graph_build_s": round(build_s, 2), "plain_hmean_gteps": plain,
-            "plain_mean_ms": statistics.mean(ms), "batched": batched,
+    return {"plain_hmean_gteps": plain, "plain_mean_ms": statistics.mean(ms), "batched": batched,
             "batched_over_plain": batched["aggregate_gteps"] / plain if plain else None}
 
 
@@ -640,10 +647,15 @@ def bench_mixed(g5, torch, args):
         bt.run(allroots, counts, out)
     ms = [bt.run(allroots, counts, out) for _ in range(3)]
     bt.close()
+    del out
+    # the single-graph batched case: 64 roots on the largest graph of the set
+    single = plain_vs_batched(g5, torch, graphs[-1], args, None, (14.0, 200.0))
+    single["scale"] = scales[-1]
     for gr in graphs:
         gr.close()
     return {"scales": scales, "roots_per_graph": 16, "ms": float(np.median(ms)),
-            "aggregate_gteps": total_edges / (np.median(ms) * 1e-3) / 1e9}
+            "aggregate_gteps": total_edges / (np.median(ms) * 1e-3) / 1e9,
+            "single_graph_64_roots": single}
 
 
 def bench_codec(g5, torch, args):
