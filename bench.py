@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--big-scale", type=int, default=0,
                     help="also compare plain and batched search on a second, larger graph (e.g. 28)")
     ap.add_argument("--serve-rates", default="1000,5000,20000")
+    ap.add_argument("--serve-modes", default="streams",
+                    help="comma list of server slot kinds to measure: streams, levels, auto")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--profile-batch", action="store_true",
                     help="only the batched search, host-driven with per-kernel CUDA events (for ncu)")
@@ -421,9 +423,12 @@ def main():
         if batched and "aggregate_gteps" in batched:
             line["batched_over_plain"] = batched["aggregate_gteps"] / value_rank if value_rank else None
         if serve:
-            # headline: the lowest offered rate (the others saturate the scale-26 graph)
-            line["p99_query_ms"] = serve["rates"][0]["p99_ms"]
-            line["p50_query_ms"] = serve["rates"][0]["p50_ms"]
+            # headline: the lowest offered rate, from the serving mode with the lower p99 there
+            modes = [m for m in ("streams", "levels", "auto") if m in serve]
+            best = min(modes, key=lambda m: serve[m]["rates"][0]["p99_ms"])
+            line["p99_query_ms"] = serve[best]["rates"][0]["p99_ms"]
+            line["p50_query_ms"] = serve[best]["rates"][0]["p50_ms"]
+            line["serve_mode"] = best
         # per search: k_init + (k_td, k_bu, k_count, k_write) per level
         line["gpu_launches"] = sum(1 + 4 * rec[3] for rec in recs)
         print(json.dumps(line))
@@ -558,14 +563,28 @@ def bench_serve(g5, big, args):
         pools.append(roots)
         nedge.append(ne)
     budget = 64 << 30
-    sv = g5.Server(graphs, mem_budget=budget, keep_results=False, mode=g5.Server.STREAMS)
-    slots = sv.slots()
+    res = {"graphs_scales": scales, "mem_budget_bytes": budget}
+    kinds = {"streams": g5.Server.STREAMS, "levels": g5.Server.LEVELS, "auto": g5.Server.AUTO}
+    for name in args.serve_modes.split(","):
+        sv = g5.Server(graphs, mem_budget=budget, keep_results=False, mode=kinds[name])
+        res[name] = {"slots": sv.slots(), "rates": serve_rates(sv, args, pools, nedge, len(graphs))}
+        sv.close()
+    for gr in graphs[:-1]:
+        gr.close()
+    res["mode_note"] = ("streams: one-root workspaces for every graph; levels: root slots of the bit-sliced "
+                        "batch; auto: level slots for graphs of >= 2^25 vertices, workspaces for the rest")
+    return res
+
+
+def serve_rates(sv, args, pools, nedge, ngraphs):
+    """Seeded Poisson arrivals at each rate (graph chosen uniformly); p50/p99
+    latency from submission to completion, and GTEPS over the run."""
     rng = np.random.default_rng(12345)
     out = []
     for rate in [float(x) for x in args.serve_rates.split(",")]:
         n = int(rate * args.serve_seconds)
         gaps = rng.exponential(1.0 / rate, n)
-        which = rng.integers(0, len(graphs), n)
+        which = rng.integers(0, ngraphs, n)
         picks = [int(pools[w][rng.integers(0, len(pools[w]))]) for w in which]
         st0 = sv.stats()
         t0 = time.perf_counter()
@@ -587,11 +606,7 @@ def bench_serve(g5, big, args):
         out.append({"rate_qps": rate, "queries": n, "p50_ms": float(np.percentile(lat, 50)),
                     "p99_ms": float(np.percentile(lat, 99)), "gteps": edges / wall / 1e9,
                     "wall_s": wall, "level_steps": st1["steps"] - st0["steps"]})
-    sv.close()
-    for gr in graphs[:-1]:
-        gr.close()
-    return {"graphs_scales": scales, "slots": slots, "mem_budget_bytes": budget, "mode": "streams",
-            "rates": out}
+    return out
 
 
 def bench_big(g5, torch, args, tune, ab):

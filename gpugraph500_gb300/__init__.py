@@ -105,6 +105,7 @@ SIGNATURES = {
     "g5_bfs_launch": (_I, [_P, _I64]),
     "g5_bfs_poll": (_I, [_P, C.POINTER(_I), C.POINTER(C.c_double)]),
     "g5_server_create": (_I, [_P, _I, _SZ, _I, _I, C.POINTER(_P)]),
+    "g5_server_create_modes": (_I, [_P, _I, _SZ, _I, _P, C.POINTER(_P)]),
     "g5_server_slots": (_I, [_P, _P]),
     "g5_server_submit": (_I, [_P, _I, _I64, C.POINTER(_U64)]),
     "g5_server_wait": (_I, [_P, _U64, C.c_double, C.POINTER(_I)]),
@@ -534,14 +535,21 @@ class Batch:
 class Server:
     """Resident graphs answering single-root queries with continuous batching (g5_server)."""
 
-    STREAMS, LEVELS = 0, 1
+    STREAMS, LEVELS, AUTO = 0, 1, 2
 
-    def __init__(self, graphs: Sequence[Graph], mem_budget: int, keep_results: bool = True, mode: int = 0):
+    def __init__(self, graphs: Sequence[Graph], mem_budget: int, keep_results: bool = True, mode: int = 0,
+                 modes: Optional[Sequence[int]] = None):
+        """mode: one slot kind for all graphs (or AUTO); modes: a kind per graph."""
         self.graphs = list(graphs)
         arr = (C.c_void_p * len(self.graphs))(*[g._h.value for g in self.graphs])
         h = C.c_void_p()
-        _check(lib().g5_server_create(arr, len(self.graphs), int(mem_budget), int(keep_results), int(mode),
-                                      C.byref(h)), "g5_server_create")
+        if modes is not None:
+            m = np.ascontiguousarray(modes, dtype=np.int32)
+            _check(lib().g5_server_create_modes(arr, len(self.graphs), int(mem_budget), int(keep_results), _ptr(m),
+                                                C.byref(h)), "g5_server_create_modes")
+        else:
+            _check(lib().g5_server_create(arr, len(self.graphs), int(mem_budget), int(keep_results), int(mode),
+                                          C.byref(h)), "g5_server_create")
         self._h = h
 
     def slots(self) -> list:

@@ -12,7 +12,10 @@
 // Two slot kinds: one-root search workspaces on their own streams (queries
 // start as soon as a workspace is free and run concurrently), or root bits
 // of the bit-sliced level loop (queries join at the next level boundary and
-// share every adjacency read with the other roots of their graph).
+// share every adjacency read with the other roots of their graph).  The
+// automatic mode gives the large graphs, whose one-root searches would
+// saturate the GPU first, the level slots and the small ones the stream
+// workspaces, each kind with its own worker thread.
 // Admission is by device memory: a graph gets as many slots (at most 64) as
 // its share of the budget holds.
 #include <cuda_runtime.h>
@@ -36,6 +39,9 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// Automatic mode: graphs of at least this many vertices get level slots.
+constexpr int64_t kAutoLevelsVertices = int64_t(1) << 25;
+
 struct Query {
     int graph = 0;
     int64_t root = 0;
@@ -49,6 +55,9 @@ struct Query {
 struct g5_server {
     std::vector<g5_graph *> graphs;
     int mode = G5_SERVE_STREAMS;
+    std::vector<int> kind;                  // per graph: G5_SERVE_STREAMS or G5_SERVE_LEVELS
+    std::vector<int> levels_graphs;         // graphs in the batch, in batch order
+    std::vector<int> bidx;                  // per graph: index in the batch (-1 if none)
     std::vector<std::vector<g5_bfs *>> ws;  // streams mode: workspaces per graph
     g5_batch *bt = nullptr;
     uint32_t *pred = nullptr;             // parents of every slot (device)
@@ -62,7 +71,7 @@ struct g5_server {
     int keep_results = 1;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::thread worker;
+    std::thread worker, worker2;          // stream-workspace and level-slot workers
     std::atomic<bool> stop{false};
     g5_status error = G5_OK;
     // statistics
@@ -79,12 +88,13 @@ void worker_streams(g5_server *sv)
     cudaSetDevice(sv->graphs[0]->device);
     const int ng = (int)sv->graphs.size();
     std::vector<std::vector<int>> running(ng);
-    for (int g = 0; g < ng; ++g) running[g].assign(sv->slots[g], 0);
+    for (int g = 0; g < ng; ++g) running[g].assign(sv->kind[g] == G5_SERVE_STREAMS ? sv->slots[g] : 0, 0);
     int nrun = 0;
     while (!sv->stop.load()) {
         {
             std::unique_lock<std::mutex> lk(sv->mu);
             for (int g = 0; g < ng; ++g) {
+                if (sv->kind[g] != G5_SERVE_STREAMS) continue;
                 for (int s = 0; s < sv->slots[g] && !sv->queue[g].empty(); ++s) {
                     if (sv->slot_query[g][s] != 0) continue;
                     const uint64_t t = sv->queue[g].front();
@@ -112,6 +122,7 @@ void worker_streams(g5_server *sv)
         }
         bool any_done = false;
         for (int g = 0; g < ng; ++g) {
+            if (sv->kind[g] != G5_SERVE_STREAMS) continue;
             for (int s = 0; s < sv->slots[g]; ++s) {
                 if (!running[g][s]) continue;
                 int done = 0;
@@ -155,10 +166,11 @@ void worker_streams(g5_server *sv)
 void worker_loop(g5_server *sv)
 {
     cudaSetDevice(sv->graphs[0]->device);
-    const int ng = (int)sv->graphs.size();
+    const std::vector<int> &lg = sv->levels_graphs;  // batch index -> graph
+    const int nb = (int)lg.size();
     std::vector<int32_t> ag, as;
     std::vector<int64_t> ar;
-    std::vector<uint64_t> active(ng, 0), retire(ng, 0), inflight(ng, 0);
+    std::vector<uint64_t> active(nb, 0), retire(nb, 0), inflight(nb, 0);
     while (!sv->stop.load()) {
         ag.clear();
         as.clear();
@@ -167,7 +179,8 @@ void worker_loop(g5_server *sv)
             std::unique_lock<std::mutex> lk(sv->mu);
             // admit queued queries into free slots (a slot retired in the last
             // step is cleared by this step before its new root starts)
-            for (int g = 0; g < ng; ++g) {
+            for (int i = 0; i < nb; ++i) {
+                const int g = lg[i];
                 for (int s = 0; s < sv->slots[g] && !sv->queue[g].empty(); ++s) {
                     if (sv->slot_query[g][s] != 0 || (sv->retire[g] >> s) & 1ull) continue;
                     const uint64_t t = sv->queue[g].front();
@@ -177,18 +190,19 @@ void worker_loop(g5_server *sv)
                     q.state = 1;
                     q.t_start = Clock::now();
                     sv->slot_query[g][s] = t;
-                    ag.push_back(g);
+                    ag.push_back(i);
                     as.push_back(s);
                     ar.push_back(q.root);
-                    inflight[g] |= 1ull << s;
+                    inflight[i] |= 1ull << s;
                 }
-                retire[g] = sv->retire[g];
+                retire[i] = sv->retire[g];
                 sv->retire[g] = 0;
             }
-            bool any_inflight = false;
-            for (int g = 0; g < ng; ++g) any_inflight |= inflight[g] != 0;
-            bool any_retire = false;
-            for (int g = 0; g < ng; ++g) any_retire |= retire[g] != 0;
+            bool any_inflight = false, any_retire = false;
+            for (int i = 0; i < nb; ++i) {
+                any_inflight |= inflight[i] != 0;
+                any_retire |= retire[i] != 0;
+            }
             if (!any_inflight && ag.empty() && !any_retire) {
                 sv->cv_work.wait_for(lk, std::chrono::milliseconds(2));
                 continue;
@@ -207,10 +221,11 @@ void worker_loop(g5_server *sv)
             return;
         }
         const Clock::time_point now = Clock::now();
-        for (int g = 0; g < ng; ++g) {
-            const uint64_t fin = inflight[g] & ~active[g];
+        for (int i = 0; i < nb; ++i) {
+            const int g = lg[i];
+            const uint64_t fin = inflight[i] & ~active[i];
             if (!fin) continue;
-            inflight[g] &= ~fin;
+            inflight[i] &= ~fin;
             for (int s = 0; s < sv->slots[g]; ++s) {
                 if (!((fin >> s) & 1ull)) continue;
                 const uint64_t t = sv->slot_query[g][s];
@@ -234,93 +249,100 @@ void worker_loop(g5_server *sv)
 
 extern "C" {
 
-g5_status g5_server_create(g5_graph *const *graphs, int ngraphs, size_t mem_budget, int keep_results, int mode,
-                           g5_server **out)
+g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t mem_budget, int keep_results,
+                                 const int *modes, g5_server **out)
 {
-    if (!graphs || ngraphs < 1 || ngraphs > 64 || !out) return G5_ERR_INVALID_ARG;
-    if (mode != G5_SERVE_STREAMS && mode != G5_SERVE_LEVELS) return G5_ERR_INVALID_ARG;
+    if (!graphs || ngraphs < 1 || ngraphs > 64 || !out || !modes) return G5_ERR_INVALID_ARG;
     *out = nullptr;
+    for (int i = 0; i < ngraphs; ++i)
+        if (!graphs[i] || (modes[i] != G5_SERVE_STREAMS && modes[i] != G5_SERVE_LEVELS)) return G5_ERR_INVALID_ARG;
     g5_server *sv = new g5_server();
     sv->keep_results = keep_results ? 1 : 0;
-    sv->mode = mode;
-    uint64_t total_n = 0;
+    sv->mode = G5_SERVE_AUTO;
     for (int i = 0; i < ngraphs; ++i) {
-        if (!graphs[i]) {
-            delete sv;
-            return G5_ERR_INVALID_ARG;
-        }
         sv->graphs.push_back(graphs[i]);
-        total_n += (uint64_t)graphs[i]->n;
+        sv->kind.push_back(modes[i]);
     }
-    if (mode == G5_SERVE_STREAMS) {
-        // memory-based admission: workspaces per graph from an equal share
-        g5_bfs_config cfg;
-        g5_bfs_config_default(&cfg);
-        cfg.alpha = 40.0;
-        cfg.beta = 200.0;
-        for (int i = 0; i < ngraphs; ++i) {
-            const uint64_t per = 48ull * (uint64_t)graphs[i]->n + (uint64_t)graphs[i]->nnz / 64 + (1u << 20);
-            uint64_t k = std::min<uint64_t>(64, (mem_budget / (uint64_t)ngraphs) / per);
-            if (k == 0) {
-                for (auto &v : sv->ws)
-                    for (g5_bfs *b : v) g5_bfs_destroy(b);
-                delete sv;
-                return G5_ERR_OOM;
-            }
-            sv->ws.emplace_back();
-            for (uint64_t j = 0; j < k; ++j) {
-                g5_bfs *b = nullptr;
-                const g5_status st = g5_bfs_create(graphs[i], &cfg, &b);
-                if (st != G5_OK) {
-                    for (auto &v : sv->ws)
-                        for (g5_bfs *x : v) g5_bfs_destroy(x);
-                    delete sv;
-                    return st;
-                }
-                sv->ws.back().push_back(b);
-            }
-            sv->slots.push_back((int)k);
-            sv->slot_query.emplace_back(k, 0);
-        }
-        sv->retire.assign(ngraphs, 0);
-        sv->queue.resize(ngraphs);
-        sv->worker = std::thread(worker_streams, sv);
-        *out = sv;
-        return G5_OK;
-    }
-    // memory-based admission: slots per graph from an equal share of the budget
-    uint64_t pb = 0;
-    for (int i = 0; i < ngraphs; ++i) {
-        const uint64_t share = mem_budget / (uint64_t)ngraphs;
-        uint64_t s = share / (4ull * (uint64_t)graphs[i]->n);
-        s = std::min<uint64_t>(64, s);
-        if (s == 0) {
-            delete sv;
-            return G5_ERR_OOM;
-        }
-        sv->slots.push_back((int)s);
-        sv->pred_base.push_back(pb);
-        pb += s * (uint64_t)graphs[i]->n;
-        sv->slot_query.emplace_back(s, 0);
-    }
-    sv->retire.assign(ngraphs, 0);
-    sv->queue.resize(ngraphs);
-    if (cudaMalloc(&sv->pred, sizeof(uint32_t) * pb) != cudaSuccess) {
-        cudaGetLastError();
-        delete sv;
-        return G5_ERR_OOM;
-    }
-    g5_status st = g5_batch_create(graphs, ngraphs, &sv->bt);
-    if (st == G5_OK) st = g5_batch_serve_begin(sv->bt, sv->pred, sv->slots.data());
-    if (st != G5_OK) {
+    auto fail = [&](g5_status st) {
+        for (auto &v : sv->ws)
+            for (g5_bfs *b : v) g5_bfs_destroy(b);
         if (sv->bt) g5_batch_destroy(sv->bt);
         cudaFree(sv->pred);
         delete sv;
         return st;
+    };
+    // memory-based admission from an equal share of the budget per graph:
+    // one-root workspaces (their footprint estimated per vertex and edge), or
+    // root slots of 4 bytes per vertex
+    g5_bfs_config cfg;
+    g5_bfs_config_default(&cfg);
+    cfg.alpha = 40.0;
+    cfg.beta = 200.0;
+    const uint64_t share = mem_budget / (uint64_t)ngraphs;
+    sv->ws.resize(ngraphs);
+    sv->pred_base.assign(ngraphs, 0);
+    sv->bidx.assign(ngraphs, -1);
+    std::vector<g5_graph *> bgraphs;
+    std::vector<int> bslots;
+    uint64_t pb = 0;
+    for (int i = 0; i < ngraphs; ++i) {
+        const uint64_t n = (uint64_t)graphs[i]->n;
+        uint64_t k;
+        if (sv->kind[i] == G5_SERVE_STREAMS) {
+            const uint64_t per = 48ull * n + (uint64_t)graphs[i]->nnz / 64 + (1u << 20);
+            k = std::min<uint64_t>(64, share / per);
+            if (k == 0) return fail(G5_ERR_OOM);
+            for (uint64_t j = 0; j < k; ++j) {
+                g5_bfs *b = nullptr;
+                const g5_status st = g5_bfs_create(graphs[i], &cfg, &b);
+                if (st != G5_OK) return fail(st);
+                sv->ws[i].push_back(b);
+            }
+        } else {
+            k = std::min<uint64_t>(64, share / (4ull * n));
+            if (k == 0) return fail(G5_ERR_OOM);
+            sv->bidx[i] = (int)bgraphs.size();
+            sv->levels_graphs.push_back(i);
+            bgraphs.push_back(graphs[i]);
+            bslots.push_back((int)k);
+            sv->pred_base[i] = pb;  // batch order: the layout g5_batch_serve_begin uses
+            pb += k * n;
+        }
+        sv->slots.push_back((int)k);
+        sv->slot_query.emplace_back(k, 0);
     }
-    sv->worker = std::thread(worker_loop, sv);
+    sv->retire.assign(ngraphs, 0);
+    sv->queue.resize(ngraphs);
+    if (!bgraphs.empty()) {
+        if (cudaMalloc(&sv->pred, sizeof(uint32_t) * pb) != cudaSuccess) {
+            cudaGetLastError();
+            sv->pred = nullptr;
+            return fail(G5_ERR_OOM);
+        }
+        g5_status st = g5_batch_create(bgraphs.data(), (int)bgraphs.size(), &sv->bt);
+        if (st == G5_OK) st = g5_batch_serve_begin(sv->bt, sv->pred, bslots.data());
+        if (st != G5_OK) return fail(st);
+        sv->worker2 = std::thread(worker_loop, sv);
+    }
+    if (bgraphs.size() < (size_t)ngraphs) sv->worker = std::thread(worker_streams, sv);
     *out = sv;
     return G5_OK;
+}
+
+g5_status g5_server_create(g5_graph *const *graphs, int ngraphs, size_t mem_budget, int keep_results, int mode,
+                           g5_server **out)
+{
+    if (!graphs || ngraphs < 1 || ngraphs > 64 || !out) return G5_ERR_INVALID_ARG;
+    if (mode != G5_SERVE_STREAMS && mode != G5_SERVE_LEVELS && mode != G5_SERVE_AUTO) return G5_ERR_INVALID_ARG;
+    std::vector<int> modes(ngraphs, mode);
+    for (int i = 0; i < ngraphs; ++i) {
+        if (!graphs[i]) return G5_ERR_INVALID_ARG;
+        if (mode == G5_SERVE_AUTO)
+            modes[i] = graphs[i]->n >= kAutoLevelsVertices ? G5_SERVE_LEVELS : G5_SERVE_STREAMS;
+    }
+    g5_status st = g5_server_create_modes(graphs, ngraphs, mem_budget, keep_results, modes.data(), out);
+    if (st == G5_OK) (*out)->mode = mode;
+    return st;
 }
 
 g5_status g5_server_slots(g5_server *sv, int *slots)
@@ -344,7 +366,7 @@ g5_status g5_server_submit(g5_server *sv, int graph, int64_t root, uint64_t *tic
     sv->queries[t] = q;
     sv->queue[graph].push_back(t);
     *ticket = t;
-    sv->cv_work.notify_one();
+    sv->cv_work.notify_all();
     return G5_OK;
 }
 
@@ -374,7 +396,7 @@ g5_status g5_server_result(g5_server *sv, uint64_t ticket, int64_t *pred_host, d
     Query q = it->second;
     if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(q.t_done - q.t_submit).count();
     if (queue_ms) *queue_ms = std::chrono::duration<double, std::milli>(q.t_start - q.t_submit).count();
-    if (q.state == 2 && pred_host && sv->mode == G5_SERVE_STREAMS) {
+    if (q.state == 2 && pred_host && sv->kind[q.graph] == G5_SERVE_STREAMS) {
         const int64_t n = sv->graphs[q.graph]->n;
         const int64_t *src = nullptr;
         g5_bfs_device_pred(sv->ws[q.graph][q.slot], &src);
@@ -403,9 +425,9 @@ g5_status g5_server_result(g5_server *sv, uint64_t ticket, int64_t *pred_host, d
     Query &qq = sv->queries[ticket];
     if (qq.state == 2) {
         sv->slot_query[qq.graph][qq.slot] = 0;
-        if (sv->mode == G5_SERVE_LEVELS) sv->retire[qq.graph] |= 1ull << qq.slot;
+        if (sv->kind[qq.graph] == G5_SERVE_LEVELS) sv->retire[qq.graph] |= 1ull << qq.slot;
         qq.state = 3;
-        sv->cv_work.notify_one();
+        sv->cv_work.notify_all();
     }
     sv->queries.erase(ticket);
     return G5_OK;
@@ -427,6 +449,7 @@ g5_status g5_server_destroy(g5_server *sv)
     sv->stop.store(true);
     sv->cv_work.notify_all();
     if (sv->worker.joinable()) sv->worker.join();
+    if (sv->worker2.joinable()) sv->worker2.join();
     for (auto &v : sv->ws)
         for (g5_bfs *b : v) g5_bfs_destroy(b);
     if (sv->bt) g5_batch_destroy(sv->bt);

@@ -296,15 +296,23 @@ g5_status g5_batch_serve_step(g5_batch *bt, const int32_t *adm_graph, const int3
  *   mode G5_SERVE_LEVELS: a slot is a root bit of the graph's bit-sliced
  *     level loop, which is stepped one level at a time; queries join at the
  *     next level boundary; slots = share / (4 bytes x vertices), at most 64.
+ *   mode G5_SERVE_AUTO: graphs of 2^25 vertices or more are served by level
+ *     slots (their one-root searches would saturate the GPU first: a slot
+ *     there shares every adjacency read with up to 63 other queries), the
+ *     smaller ones by stream workspaces; each kind has its own worker.
  * Queries beyond the free slots wait in a FIFO per graph (memory-based
  * admission).  keep_results = 0 frees a slot as soon as its query finishes
  * (results are discarded). */
 typedef struct g5_server g5_server;
 
-enum { G5_SERVE_STREAMS = 0, G5_SERVE_LEVELS = 1 };
+enum { G5_SERVE_STREAMS = 0, G5_SERVE_LEVELS = 1, G5_SERVE_AUTO = 2 };
 
 g5_status g5_server_create(g5_graph *const *graphs, int ngraphs, size_t mem_budget,
                            int keep_results, int mode, g5_server **out);
+/* As g5_server_create with the slot kind given per graph (modes[i] =
+ * G5_SERVE_STREAMS or G5_SERVE_LEVELS). */
+g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t mem_budget,
+                                 int keep_results, const int *modes, g5_server **out);
 /* Slots per graph chosen by the admission rule. */
 g5_status g5_server_slots(g5_server *sv, int *slots);
 /* Thread safe: queues one query; *ticket identifies it. */

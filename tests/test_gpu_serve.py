@@ -36,7 +36,7 @@ def run_queries(sv, queries, concurrent):
     return out
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, (1, 0, 1), 2])
 def test_alone_and_mixed_agree_with_oracle(graphs, mode):
     csrs = [g.csr() for g in graphs]
     roots = [g5.select_roots(g, 20) for g in graphs]
@@ -44,7 +44,10 @@ def test_alone_and_mixed_agree_with_oracle(graphs, mode):
     queries = [(gi, int(r)) for gi in range(3) for r in roots[gi]]
     order = rng.permutation(len(queries))
     queries = [queries[i] for i in order]
-    sv = g5.Server(graphs, mem_budget=1 << 30, mode=mode)
+    if isinstance(mode, tuple):  # level slots for two graphs, stream workspaces for one
+        sv = g5.Server(graphs, mem_budget=1 << 30, modes=list(mode))
+    else:
+        sv = g5.Server(graphs, mem_budget=1 << 30, mode=mode)
     assert min(sv.slots()) >= 2
     alone = run_queries(sv, queries, concurrent=False)
     mixed = run_queries(sv, queries, concurrent=True)
