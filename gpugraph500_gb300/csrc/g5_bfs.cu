@@ -98,6 +98,7 @@ struct BfsArgs {
     uint32_t *ulist;       // sorted unvisited vertices for a bottom-up level
     uint64_t *chunk_u;     // per chunk: unvisited vertices after the level
     int parent_mode;       // 0 atomicMin, 1 heavy atomicMin + fix-up, 2 first writer + fix-up
+    const uint32_t *first; // first (smallest) neighbour of each vertex, 0 for isolated ones
     uint64_t tile;         // frontier edges per top-down warp tile (a power of two >= 32)
     int tile_shift;        // log2(tile)
     int bu_serial;         // entries a bottom-up lane scans alone before the warp helps
@@ -260,7 +261,7 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
 // lists one at a time, 32 entries per step (the first set ballot bit is the
 // smallest index).  Returns found / par per lane and the entries read.
 template <typename Off>
-__device__ __forceinline__ void first_hit(const BfsArgs &a, bool mine, Off s, Off e, bool &found,
+__device__ __forceinline__ void first_hit(const BfsArgs &a, bool mine, Off s, Off e, uint32_t u0, bool &found,
                                           uint32_t &par, uint64_t &ex)
 {
     const int lane = g5_lane();
@@ -269,6 +270,16 @@ __device__ __forceinline__ void first_hit(const BfsArgs &a, bool mine, Off s, Of
     found = false;
     par = 0;
     Off j = s;
+    // the first neighbour comes from the dense copy (loaded with the offsets,
+    // coalesced), so a vertex whose first neighbour is in the frontier never
+    // touches its row
+    if (mine && s < e) {
+        if ((__ldg(front + (u0 >> 5)) >> (u0 & 31)) & 1u) {
+            found = true;
+            par = u0;
+        }
+        j = s + 1;
+    }
     const Off lim = min(e, (Off)(s + a.bu_serial));
     while (j < lim && !found) {
         uint32_t u[4];
@@ -381,11 +392,15 @@ __device__ void sweep(const BfsArgs &a, uint64_t &examined)
         const uint64_t v = w * 32 + lane;
         const bool mine = (cand_word >> lane) & 1u;
         Off s = 0, e = 0;
-        if (mine) load_offsets(a, v, s, e);
+        uint32_t u0 = 0;
+        if (mine) {
+            load_offsets(a, v, s, e);
+            u0 = a.first[v];
+        }
         bool found;
         uint32_t par;
         uint64_t ex;
-        first_hit<Off>(a, mine, s, e, found, par, ex);
+        first_hit<Off>(a, mine, s, e, u0, found, par, ex);
         if (found) a.pred[v] = (int64_t)par;
         if (FIXUP) {
             if (mine && !found) atomicOr(&a.st->err, G5_DEVERR_CAPACITY);  // cannot happen on a symmetric CSR
@@ -423,22 +438,30 @@ __device__ void sweep_bu(const BfsArgs &a, uint64_t &examined)
     uint32_t c1 = gw < nwords ? ~a.visited[gw] : 0u;
     uint32_t c2 = gw + nw < nwords ? ~a.visited[gw + nw] : 0u;
     Off s1 = 0, e1 = 0;
-    if ((c1 >> lane) & 1u) load_offsets(a, gw * 32 + lane, s1, e1);
+    uint32_t f1 = 0;
+    if ((c1 >> lane) & 1u) {
+        load_offsets(a, gw * 32 + lane, s1, e1);
+        f1 = a.first[gw * 32 + lane];
+    }
     for (uint64_t w = gw; w < nwords; w += nw) {
         const uint32_t cw = c1;
         const Off s = s1, e = e1;
+        const uint32_t u0 = f1;
         c1 = c2;
         const uint64_t w2 = w + 2 * nw;
         c2 = w2 < nwords ? ~a.visited[w2] : 0u;
         s1 = e1 = 0;
-        if ((c1 >> lane) & 1u) load_offsets(a, (w + nw) * 32 + lane, s1, e1);
+        if ((c1 >> lane) & 1u) {
+            load_offsets(a, (w + nw) * 32 + lane, s1, e1);
+            f1 = a.first[(w + nw) * 32 + lane];
+        }
         if (!cw) continue;
         const uint64_t v = w * 32 + lane;
         const bool mine = (cw >> lane) & 1u;
         bool found;
         uint32_t par;
         uint64_t ex;
-        first_hit<Off>(a, mine, s, e, found, par, ex);
+        first_hit<Off>(a, mine, s, e, u0, found, par, ex);
         if (found) a.pred[v] = (int64_t)par;
         const unsigned fm = __ballot_sync(0xFFFFFFFFu, found);
         if (fm) {
@@ -473,21 +496,29 @@ __device__ void bottom_up_list(const BfsArgs &a, uint64_t &examined)
     uint32_t v1 = p1 < len ? list[p1] : 0u;
     uint32_t v2 = p2 < len ? list[p2] : 0u;
     Off s1 = 0, e1 = 0;
-    if (p1 < len) load_offsets(a, v1, s1, e1);
+    uint32_t f1 = 0;
+    if (p1 < len) {
+        load_offsets(a, v1, s1, e1);
+        f1 = a.first[v1];
+    }
     for (uint64_t b0 = gw * 32; b0 < len; b0 += stride) {
         const bool mine = b0 + lane < len;
         const uint32_t v = v1;
         const Off s = s1, e = e1;
+        const uint32_t u0 = f1;
         v1 = v2;
         p1 = p2;
         p2 += stride;
         v2 = p2 < len ? list[p2] : 0u;
         s1 = e1 = 0;
-        if (p1 < len) load_offsets(a, v1, s1, e1);
+        if (p1 < len) {
+            load_offsets(a, v1, s1, e1);
+            f1 = a.first[v1];
+        }
         bool found;
         uint32_t par;
         uint64_t ex;
-        first_hit<Off>(a, mine, s, e, found, par, ex);
+        first_hit<Off>(a, mine, s, e, u0, found, par, ex);
         if (found) {
             a.pred[v] = (int64_t)par;
             atomicOr(a.next + (v >> 5), 1u << (v & 31));
@@ -985,6 +1016,7 @@ struct g5_bfs {
     uint32_t *isolated = nullptr; // one bit per vertex of degree 0
     uint32_t *heavy = nullptr;    // one bit per vertex of degree > kHeavy
     uint32_t *ro32 = nullptr;     // uint32 copy of the row offsets (nnz < 2^32)
+    uint32_t *first = nullptr;    // first neighbour of each vertex (dense, coalesced)
     uint32_t *multi = nullptr;    // reached more than once in a top-down level
     uint32_t *wdeg = nullptr;     // per-word degree sums written by bottom-up
     uint32_t *ulist = nullptr;    // sorted unvisited vertices (n entries)
@@ -1106,6 +1138,7 @@ g5_status alloc_ws(g5_bfs *b)
     G5_CUDA(cudaMalloc(&b->isolated, sizeof(uint32_t) * a.nwords));
     G5_CUDA(cudaMalloc(&b->heavy, sizeof(uint32_t) * a.nwords));
     if (g->nnz < ((int64_t)1 << 32)) G5_CUDA(cudaMalloc(&b->ro32, sizeof(uint32_t) * (size_t)(n + 1)));
+    G5_CUDA(cudaMalloc(&b->first, sizeof(uint32_t) * (size_t)n));
     G5_CUDA(cudaMalloc(&b->multi, sizeof(uint32_t) * a.nwords));
     G5_CUDA(cudaMalloc(&b->wdeg, sizeof(uint32_t) * a.nwords));
     G5_CUDA(cudaMalloc(&b->ulist, sizeof(uint32_t) * (size_t)n + 16));
@@ -1145,6 +1178,7 @@ g5_status alloc_ws(g5_bfs *b)
     a.tile_start = b->tile_start;
     a.heavy = b->heavy;
     a.ro32 = b->ro32;
+    a.first = b->first;
     a.multi = b->multi;
     a.wdeg = b->wdeg;
     a.ulist = b->ulist;
@@ -1164,8 +1198,9 @@ g5_status alloc_ws(g5_bfs *b)
     return G5_OK;
 }
 
-__global__ void k_degrees(const int64_t *__restrict__ ro, int64_t n, uint32_t *__restrict__ d,
-                          uint32_t *__restrict__ iso, uint32_t *__restrict__ heavy, uint32_t *__restrict__ ro32)
+__global__ void k_degrees(const int64_t *__restrict__ ro, const uint32_t *__restrict__ col, int64_t n,
+                          uint32_t *__restrict__ d, uint32_t *__restrict__ iso, uint32_t *__restrict__ heavy,
+                          uint32_t *__restrict__ ro32, uint32_t *__restrict__ first)
 {
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < ((n + 31) & ~(int64_t)31);
          v += (int64_t)gridDim.x * blockDim.x) {
@@ -1174,7 +1209,10 @@ __global__ void k_degrees(const int64_t *__restrict__ ro, int64_t n, uint32_t *_
             if (v == 0) ro32[n] = (uint32_t)ro[n];
         }
         const uint32_t dv = v < n ? (uint32_t)(ro[v + 1] - ro[v]) : 0u;
-        if (v < n) d[v] = dv;
+        if (v < n) {
+            d[v] = dv;
+            first[v] = dv ? col[ro[v]] : 0u;
+        }
         const unsigned m = __ballot_sync(0xFFFFFFFFu, dv == 0 && v < n);
         const unsigned h = __ballot_sync(0xFFFFFFFFu, dv > kHeavy);
         if ((threadIdx.x & 31) == 0) {
@@ -1193,6 +1231,7 @@ void free_ws(g5_bfs *b)
     cudaFree(b->isolated);
     cudaFree(b->heavy);
     cudaFree(b->ro32);
+    cudaFree(b->first);
     cudaFree(b->multi);
     cudaFree(b->wdeg);
     cudaFree(b->ulist);
@@ -1281,8 +1320,8 @@ g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
     cudaEventCreate(&b->ev0);
     cudaEventCreate(&b->ev1);
     if ((st = alloc_ws(b)) != G5_OK) return fail(st);
-    k_degrees<<<g5::grid_for(8), kBlock, 0, b->stream>>>(g->row_off, g->n, b->deg, b->isolated, b->heavy,
-                                                          b->ro32);
+    k_degrees<<<g5::grid_for(8), kBlock, 0, b->stream>>>(g->row_off, g->col, g->n, b->deg, b->isolated,
+                                                          b->heavy, b->ro32, b->first);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
     if (b->cfg.use_graph && (st = build_graph(b)) != G5_OK) return fail(st);
     *out = b;
