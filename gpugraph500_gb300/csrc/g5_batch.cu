@@ -51,6 +51,7 @@ constexpr int kPerThread = kChunk / kB;
 constexpr uint64_t kTile = 256;        // edges per top-down warp tile
 constexpr int kSerial = 4;             // bottom-up entries scanned per lane first
 constexpr int kMaxGraphs = 64;
+constexpr uint64_t kBuMinFrac = 16;    // bottom-up only when frontier entries > n / kBuMinFrac
 constexpr int kMaxLevels = 1024;
 
 enum : int32_t { TD = 0, BU = 1 };
@@ -568,7 +569,9 @@ __global__ void __launch_bounds__(1024) k_bscan(BArgs a)
         const uint64_t mu_after = a.serving ? (uint64_t)d.nnz : (d.mu >= tm ? d.mu - tm : 0);
         if (a.st->level >= 0) {
             if (d.dir == TD) {
-                if ((double)tm > (double)mu_after / a.alpha) nd = BU;
+                // Beamer's test, and a frontier large enough to pay for a
+                // sweep over all of the graph's vertices
+                if ((double)tm > (double)mu_after / a.alpha && tm > (uint64_t)d.n / kBuMinFrac) nd = BU;
             } else if ((double)tn < (double)d.n / a.beta && tn < d.nf) {
                 nd = TD;
             }
