@@ -80,6 +80,21 @@ def test_root_parents_extraction():
     bt.close(); g.close()
 
 
+def test_degenerate_graphs_in_one_batch():
+    """A graph without edges, a single-vertex graph and a graph whose size
+    ends exactly on a chunk boundary, all in one launch with isolated roots."""
+    ro0, col0 = orc.build_csr(37, np.zeros((0, 2), np.int64))
+    ro1, col1 = orc.build_csr(1, np.zeros((0, 2), np.int64))
+    n2 = 4096
+    e2 = np.array([(i, (i * 5 + 1) % n2) for i in range(0, n2, 2)], np.int64)
+    ro2, col2 = orc.build_csr(n2, e2)
+    gs = [g5.Graph.from_csr(ro, col) for ro, col in ((ro0, col0), (ro1, col1), (ro2, col2))]
+    bt = check_batch(gs, [(ro0, col0), (ro1, col1), (ro2, col2)], [[0, 36, 5], [0], [0, 1, 3, 4095, 2048]])
+    bt.close()
+    for g in gs:
+        g.close()
+
+
 def test_invalid_roots_rejected():
     g = g5.Graph.kronecker(8)
     bt = g5.Batch([g])

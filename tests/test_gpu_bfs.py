@@ -39,6 +39,20 @@ def test_hand_graphs():
     run_all_roots(ro, col, [0, 5, 9, 10, 11, 30, 33, 40])
 
 
+def test_degenerate_graphs():
+    """One vertex, no edges at all, an isolated root, and sizes at word and
+    chunk boundaries: parents equal the oracle's (the root maps to itself,
+    everything else stays -1 when nothing is reachable)."""
+    ro, col = csr_from_edges(1, np.zeros((0, 2), np.int64))
+    run_all_roots(ro, col, [0])
+    ro, col = csr_from_edges(37, np.zeros((0, 2), np.int64))
+    run_all_roots(ro, col, [0, 36])
+    for n in (32, 64, 65536, 65537):
+        edges = [(i, (i * 7 + 3) % n) for i in range(0, n, 3)]
+        ro, col = csr_from_edges(n, edges)
+        run_all_roots(ro, col, [1, n - 1, n // 3])  # n // 3 ... may be isolated
+
+
 def test_long_path_many_levels():
     n = 3000
     edges = [(i, i + 1) for i in range(n - 1)]
