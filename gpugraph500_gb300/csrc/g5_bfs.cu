@@ -935,9 +935,20 @@ __global__ void k_val_jump(const int64_t *__restrict__ anc_in, const int32_t *__
     }
 }
 
+// lev[v] = BFS level of v if its parent chain reaches the root, else -1:
+// one 4-byte word per vertex, so the edge check below reads one random word
+// per adjacency entry instead of the parent, ancestor and depth arrays.
+__global__ void k_val_level(const int64_t *__restrict__ pred, const int64_t *__restrict__ anc,
+                            const int32_t *__restrict__ dist, int64_t n, int64_t root, int32_t *__restrict__ lev)
+{
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+         v += (int64_t)gridDim.x * blockDim.x)
+        lev[v] = (pred[v] == -1 || anc[v] != root || dist[v] < 0) ? -1 : dist[v];
+}
+
 __global__ void k_val_edges(const int64_t *__restrict__ row_off, const uint32_t *__restrict__ col,
-                            const int64_t *__restrict__ pred, const int64_t *__restrict__ anc,
-                            const int32_t *__restrict__ dist, int64_t n, int64_t root, unsigned *flags)
+                            const int64_t *__restrict__ pred, const int32_t *__restrict__ lev, int64_t n,
+                            int64_t root, unsigned *flags)
 {
     const int lane = g5_lane();
     const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -945,11 +956,12 @@ __global__ void k_val_edges(const int64_t *__restrict__ row_off, const uint32_t 
     for (int64_t v = gw; v < n; v += nw) {
         const int64_t p = pred[v];
         if (p == -1) continue;
-        if (anc[v] != root || dist[v] < 0) {
+        const int32_t d = lev[v];
+        if (d < 0) {
+            // visited but its parent chain does not reach the root
             if (lane == 0) atomicOr(flags, VAL_CYCLE);
             continue;
         }
-        const int32_t d = dist[v];
         const int64_t s = row_off[v], e = row_off[v + 1];
         bool tree = (v == root);
         int64_t first_prev = -1;  // smallest neighbour one level up
@@ -959,9 +971,8 @@ __global__ void k_val_edges(const int64_t *__restrict__ row_off, const uint32_t 
             bool is_par = false, is_prev = false;
             uint32_t u = 0;
             if (j < e) {
-                u = col[j];
-                const int64_t pu = pred[u];
-                const int32_t du = (pu == -1 || anc[u] != root) ? -1 : dist[u];
+                u = __ldg(col + j);
+                const int32_t du = __ldg(lev + u);
                 if (du < 0) bad |= VAL_COVER;
                 else if (du > d + 1 || du < d - 1) bad |= VAL_LEVEL;
                 is_par = ((int64_t)u == p);
@@ -974,7 +985,7 @@ __global__ void k_val_edges(const int64_t *__restrict__ row_off, const uint32_t 
         if (v != root) {
             if (!tree) bad |= VAL_TREE_EDGE;
             if (first_prev != p) bad |= VAL_MINPAR;
-            if (dist[v] != 0 && first_prev < 0) bad |= VAL_LEVEL;
+            if (d != 0 && first_prev < 0) bad |= VAL_LEVEL;
         }
         if (bad) atomicOr(flags, bad);
     }
@@ -1542,8 +1553,9 @@ g5_status g5_bfs_validate(g5_bfs *b, int64_t root, int *valid, int *min_parent_o
         if (!ch) break;
     }
     if (rc == G5_OK) {
-        k_val_edges<<<g5::grid_for(8), kBlock, 0, s>>>(b->g->row_off, b->g->col, b->pred, anc[cur], dist[cur], n,
-                                                        root, flags);
+        int32_t *lev = dist[1 - cur];  // free after the last jump round
+        k_val_level<<<g5::grid_for(8), kBlock, 0, s>>>(b->pred, anc[cur], dist[cur], n, root, lev);
+        k_val_edges<<<g5::grid_for(8), kBlock, 0, s>>>(b->g->row_off, b->g->col, b->pred, lev, n, root, flags);
         unsigned f = 0;
         cudaMemcpyAsync(&f, flags, sizeof f, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) rc = G5_ERR_CUDA;

@@ -148,6 +148,57 @@ def test_teps_edges_and_validation_match_oracle():
     g.close()
 
 
+class _Dev:
+    """A device array handed to torch through __cuda_array_interface__."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<i8", "data": (ptr, False), "version": 3}
+
+
+def test_device_validator_rejects_corrupt_trees():
+    torch = pytest.importorskip("torch")
+    e = orc.kronecker(10)
+    n = 1 << 10
+    ro, col = orc.build_csr(n, e)
+    g = g5.Graph.from_csr(ro, col)
+    b = g5.CudaBFS(g, want_levels=True)
+    root = int(orc.select_roots(ro, 1)[0])
+    b.runBFS(root)
+    good = b.getPredecessor().copy()
+    lev = b.getLevels().copy()
+    pred = torch.as_tensor(_Dev(b.device_pred_ptr(), n), device="cuda")
+    adj = [set(col[ro[v]:ro[v + 1]].tolist()) for v in range(n)]
+    # a vertex at level >= 2 with two neighbours one level up
+    v2 = next(v for v in range(n) if lev[v] >= 2 and sum(lev[u] == lev[v] - 1 for u in adj[v]) >= 2)
+    ups = sorted(u for u in adj[v2] if lev[u] == lev[v2] - 1)
+    far = next(u for u in range(n) if u not in adj[v2] and u != v2 and lev[u] >= 0)
+    leaf = next(v for v in range(n) if v != root and lev[v] > 0 and good[v] >= 0)
+
+    def check(mutate, want_valid, want_min):
+        p = good.copy()
+        mutate(p)
+        pred.copy_(torch.from_numpy(p))
+        torch.cuda.synchronize()
+        valid, minpar = b.validate(root)
+        assert valid == want_valid, mutate
+        if want_valid:  # the min-parent verdict is only meaningful for a valid tree
+            assert minpar == want_min, mutate
+
+    check(lambda p: None, True, True)
+    check(lambda p: p.__setitem__(v2, ups[-1]), True, False)   # valid parent, not the smallest
+    check(lambda p: p.__setitem__(v2, far), False, False)      # not an edge of the graph
+    check(lambda p: p.__setitem__(root, ups[0]), False, False)  # the root does not map to itself
+    check(lambda p: p.__setitem__(leaf, leaf), False, False)   # self parent
+    check(lambda p: p.__setitem__(leaf, -1), False, False)     # a reachable vertex left out
+
+    def cycle(p):
+        p[v2] = ups[0]
+        p[ups[0]] = v2
+    check(cycle, False, False)
+    b.close()
+    g.close()
+
+
 def test_codec_in_loop_round_trips():
     e = orc.kronecker(13)
     ro, col = orc.build_csr(1 << 13, e)
