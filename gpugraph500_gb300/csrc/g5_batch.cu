@@ -92,7 +92,6 @@ struct BArgs {
     uint32_t nchunks;
     uint64_t ntot;          // padded global vertex count
     const uint32_t *deg;    // per global vertex
-    const uint32_t *heavy;  // one bit per global vertex of degree > 64
     const uint32_t *iso;    // one bit per global vertex of degree 0
     const uint32_t *iso0;   // the same bits in original-id order
     uint64_t *vis, *front, *next;
@@ -771,7 +770,7 @@ __global__ void k_gather_root(const uint32_t *pred, uint32_t R, uint32_t r, int6
 }
 
 __global__ void k_bdeg(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t ntot, uint32_t *deg,
-                       uint32_t *heavy, uint32_t *iso)
+                       uint32_t *iso)
 {
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < ntot;
          v += (uint64_t)gridDim.x * blockDim.x) {
@@ -779,12 +778,8 @@ __global__ void k_bdeg(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t
         const int64_t vl = (int64_t)(v - d.vbase);
         const uint32_t dv = vl < d.n ? (uint32_t)(d.row_off[vl + 1] - d.row_off[vl]) : 0u;
         deg[v] = dv;
-        const unsigned h = __ballot_sync(0xFFFFFFFFu, dv > 64u);
         const unsigned z = __ballot_sync(0xFFFFFFFFu, dv == 0u);
-        if ((threadIdx.x & 31) == 0) {
-            heavy[v >> 5] = h;
-            iso[v >> 5] = z;
-        }
+        if ((threadIdx.x & 31) == 0) iso[v >> 5] = z;
     }
 }
 
@@ -848,7 +843,6 @@ struct g5_batch {
     GraphDesc *gd = nullptr;
     uint8_t *chunk_graph = nullptr;
     uint32_t *deg = nullptr;
-    uint32_t *heavy = nullptr;
     uint32_t *iso = nullptr;
     uint32_t *iso0 = nullptr;
     uint64_t *words = nullptr;  // vis | front | next
@@ -949,7 +943,6 @@ void free_batch(g5_batch *b)
     cudaFree(b->gd);
     cudaFree(b->chunk_graph);
     cudaFree(b->deg);
-    cudaFree(b->heavy);
     cudaFree(b->iso);
     cudaFree(b->iso0);
     cudaFree(b->words);
@@ -1067,7 +1060,6 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     B_ALLOC(b->gd, sizeof(GraphDesc) * ngraphs);
     B_ALLOC(b->chunk_graph, cg.size());
     B_ALLOC(b->deg, sizeof(uint32_t) * vb);
-    B_ALLOC(b->heavy, sizeof(uint32_t) * (vb / 32));
     B_ALLOC(b->iso, sizeof(uint32_t) * (vb / 32));
     B_ALLOC(b->iso0, sizeof(uint32_t) * (vb / 32));
     B_ALLOC(b->words, sizeof(uint64_t) * 3 * vb);
@@ -1091,7 +1083,6 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     a.gd = b->gd;
     a.chunk_graph = b->chunk_graph;
     a.deg = b->deg;
-    a.heavy = b->heavy;
     a.iso = b->iso;
     a.iso0 = b->iso0;
     a.vis = b->words;
@@ -1108,7 +1099,7 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     a.roots = b->roots;
     a.root_off = b->root_off;
     a.level_log = b->level_log;
-    k_bdeg<<<g5::grid_for(8), kB, 0, b->stream>>>(b->gd, b->chunk_graph, vb, b->deg, b->heavy, b->iso);
+    k_bdeg<<<g5::grid_for(8), kB, 0, b->stream>>>(b->gd, b->chunk_graph, vb, b->deg, b->iso);
     k_biso0<<<g5::grid_for(8), kB, 0, b->stream>>>(b->gd, b->chunk_graph, vb, b->deg, b->iso0);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
     *out = b;
