@@ -519,9 +519,33 @@ __device__ void bottom_up_list(const BfsArgs &a, uint64_t &examined)
         uint32_t par;
         uint64_t ex;
         first_hit<Off>(a, mine, s, e, u0, found, par, ex);
-        if (found) {
-            a.pred[v] = (int64_t)par;
-            atomicOr(a.next + (v >> 5), 1u << (v & 31));
+        if (found) a.pred[v] = (int64_t)par;
+        // the list is sorted, so lanes holding vertices of one bitmap word
+        // are adjacent: a segmented scan gives the last lane of each word
+        // the word's new bits and their degree sum, and that lane alone
+        // updates next and wdeg (one atomic pair per word, not per vertex)
+        const unsigned fm = __ballot_sync(0xFFFFFFFFu, found);
+        if (fm) {
+            const uint32_t wv = mine ? (v >> 5) : 0xFFFFFFFFu;
+            const uint32_t wprev = __shfl_up_sync(0xFFFFFFFFu, wv, 1);
+            const unsigned heads = __ballot_sync(0xFFFFFFFFu, lane == 0 || wprev != wv);
+            const int head = 31 - __clz(heads & (0xFFFFFFFFu >> (31 - lane)));
+            uint32_t bits = found ? 1u << (v & 31) : 0u;
+            uint32_t dsum = found ? (uint32_t)(e - s) : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t b2 = __shfl_up_sync(0xFFFFFFFFu, bits, o);
+                const uint32_t d2 = __shfl_up_sync(0xFFFFFFFFu, dsum, o);
+                if (lane - o >= head) {
+                    bits |= b2;
+                    dsum += d2;
+                }
+            }
+            const uint32_t wnext = __shfl_down_sync(0xFFFFFFFFu, wv, 1);
+            if (bits && (lane == 31 || wnext != wv)) {
+                atomicOr(a.next + wv, bits);
+                atomicAdd(a.wdeg + wv, dsum);
+            }
         }
         examined += ex;
     }
@@ -586,22 +610,24 @@ __global__ void __launch_bounds__(kBlock) k_fixup(BfsArgs a)
 // word l (coalesced), then for every non-empty word the lanes read the
 // degrees of its set vertices in one coalesced 128-byte load.
 constexpr int kWordsPerWarp = kChunkWords / kWarps;
+constexpr int kWordIters = kWordsPerWarp / 32;  // words per lane
 
-__device__ __forceinline__ void warp_chunk_counts(const BfsArgs &a, uint64_t wbeg, uint64_t &cn, uint64_t &cm)
+__device__ __forceinline__ void warp_chunk_counts(const BfsArgs &a, uint64_t wbeg, const uint32_t (&xs)[kWordIters],
+                                                  uint64_t &cn, uint64_t &cm)
 {
     const int lane = g5_lane();
     cn = 0;
     cm = 0;
-    for (int g = 0; g < kWordsPerWarp; g += 32) {
-        const uint64_t wl = wbeg + g + lane;
-        const uint32_t x = wl < a.nwords ? a.next[wl] : 0u;
+#pragma unroll
+    for (int i = 0; i < kWordIters; ++i) {
+        const uint32_t x = xs[i];
         cn += __popc(x);
         unsigned act = __ballot_sync(0xFFFFFFFFu, x != 0u);
         while (act) {
             const int j = __ffs(act) - 1;
             act &= act - 1;
             const uint32_t wj = __shfl_sync(0xFFFFFFFFu, x, j);
-            if ((wj >> lane) & 1u) cm += __ldg(a.deg + (wbeg + g + j) * 32 + lane);
+            if ((wj >> lane) & 1u) cm += __ldg(a.deg + (wbeg + i * 32 + j) * 32 + lane);
         }
     }
     cn = warp_sum_u64(cn);
@@ -618,7 +644,7 @@ __global__ void __launch_bounds__(kBlock) k_count(BfsArgs a)
 {
     const uint32_t c = blockIdx.x;
     const uint64_t w0 = (uint64_t)c * kChunkWords + (uint64_t)threadIdx.x * kWordsPerThread;
-    const bool bu = a.st->dir == DIR_BU && !a.st->list_mode;  // word sweep: degree sums present
+    const bool bu = a.st->dir == DIR_BU;  // bottom-up levels leave per-word degree sums
     uint64_t cn = 0, cm = 0, cu = 0;
 #pragma unroll
     for (int k = 0; k < kWordsPerThread; ++k) {
@@ -778,14 +804,23 @@ __global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
     const int32_t L = a.st->level;  // index of the new frontier
     const bool want_q = a.st->want_queue != 0;
     const bool want_u = a.st->list_mode != 0;  // next level is bottom-up
+    uint64_t pos = a.chunk_n[c], mpos = a.chunk_m[c], upos = a.chunk_u[c];
+    // every word of the warp's range up front (one load per lane and word,
+    // all in flight at once): xs = next, vs = visited | next (all ones past
+    // the end, so those words hold no unvisited vertex)
+    uint32_t xs[kWordIters], vs[kWordIters];
+#pragma unroll
+    for (int i = 0; i < kWordIters; ++i) {
+        const uint64_t wl = wbeg + i * 32 + lane;
+        xs[i] = wl < a.nwords ? a.next[wl] : 0u;
+        vs[i] = wl < a.nwords ? a.visited[wl] : ~0u;
+    }
     // per-warp totals, then the warp's offsets inside the chunk
     uint64_t cn = 0, cm = 0, cu = 0;
-    if (want_q || a.level) warp_chunk_counts(a, wbeg, cn, cm);
+    if (want_q || a.level) warp_chunk_counts(a, wbeg, xs, cn, cm);
     if (want_u) {
-        for (int g = 0; g < kWordsPerWarp; g += 32) {
-            const uint64_t wl = wbeg + g + lane;
-            if (wl < a.nwords) cu += __popc(~(a.visited[wl] | a.next[wl]));
-        }
+#pragma unroll
+        for (int i = 0; i < kWordIters; ++i) cu += __popc(~(vs[i] | xs[i]));
         cu = warp_sum_u64(cu);
     }
     __shared__ uint64_t s_n[kWarps], s_m[kWarps], s_u[kWarps];
@@ -795,24 +830,24 @@ __global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
         s_u[wid] = cu;
     }
     __syncthreads();
-    uint64_t pos = a.chunk_n[c], mpos = a.chunk_m[c], upos = a.chunk_u[c];
     for (int i = 0; i < wid; ++i) {
         pos += s_n[i];
         mpos += s_m[i];
         upos += s_u[i];
     }
-    for (int g = 0; g < kWordsPerWarp; g += 32) {
-        const uint64_t wl = wbeg + g + lane;
-        uint32_t x = 0, unv = 0;
+#pragma unroll
+    for (int i = 0; i < kWordIters; ++i) {
+        const uint64_t wl = wbeg + i * 32 + lane;
+        const uint32_t x = xs[i];
+        const uint32_t vis = vs[i] | x;
+        const uint32_t unv = ~vis;
         if (wl < a.nwords) {
-            x = a.next[wl];
-            const uint32_t vis = a.visited[wl] | x;
             if (x) {
                 a.visited[wl] = vis;
                 a.next[wl] = 0;
+                a.wdeg[wl] = 0;  // a bottom-up list sweep adds into it
             }
             a.front[wl] = x;
-            unv = ~vis;
         }
         if (want_u) {
             // unvisited vertices of these 32 words, in order: one word at a
@@ -823,7 +858,7 @@ __global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
                 uact &= uact - 1;
                 const uint32_t uj = __shfl_sync(0xFFFFFFFFu, unv, j);
                 if ((uj >> lane) & 1u)
-                    a.ulist[upos + __popc(uj & g5_lanemask_lt())] = (uint32_t)((wbeg + g + j) * 32 + lane);
+                    a.ulist[upos + __popc(uj & g5_lanemask_lt())] = (uint32_t)((wbeg + i * 32 + j) * 32 + lane);
                 upos += __popc(uj);
             }
         }
@@ -834,7 +869,7 @@ __global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
             act &= act - 1;
             const uint32_t wj = __shfl_sync(0xFFFFFFFFu, x, j);
             const bool mine = (wj >> lane) & 1u;
-            const uint64_t v = (wbeg + g + j) * 32 + lane;
+            const uint64_t v = (wbeg + i * 32 + j) * 32 + lane;
             uint64_t d = mine ? (uint64_t)__ldg(a.deg + v) : 0;
             // inclusive scan of the degrees of this word's vertices
             uint64_t incl = d;
@@ -1152,6 +1187,7 @@ g5_status alloc_ws(g5_bfs *b)
     G5_CUDA(cudaMalloc(&b->first, sizeof(uint32_t) * (size_t)n));
     G5_CUDA(cudaMalloc(&b->multi, sizeof(uint32_t) * a.nwords));
     G5_CUDA(cudaMalloc(&b->wdeg, sizeof(uint32_t) * a.nwords));
+    G5_CUDA(cudaMemset(b->wdeg, 0, sizeof(uint32_t) * a.nwords));
     G5_CUDA(cudaMalloc(&b->ulist, sizeof(uint32_t) * (size_t)n + 16));
     G5_CUDA(cudaMalloc(&b->done, sizeof(unsigned)));
     G5_CUDA(cudaMemset(b->done, 0, sizeof(unsigned)));

@@ -16,9 +16,9 @@ import itertools
 from typing import Sequence
 
 ALPHAS = (4.0, 14.0, 40.0, 120.0, 400.0)
-BETAS = (12.0, 24.0, 64.0, 200.0)
-TILES = (128, 256, 512, 1024)
-SERIALS = (4, 8, 16)
+BETAS = (64.0, 200.0, 600.0, 2000.0, 6000.0)
+TILES = (64, 128, 256, 512)
+SERIALS = (4, 8, 16, 32)
 
 _cache: dict = {}
 
