@@ -61,6 +61,8 @@ struct GraphDesc {
     const uint32_t *col;     // new ids, each row in original-id order
     const uint32_t *orig;    // new id -> original id
     const uint32_t *perm;    // original id -> new id
+    const int64_t *ostart;   // by original id: start of the vertex's row in col
+    const uint32_t *odeg;    // by original id: its degree
     int64_t n;
     int64_t nnz;
     uint64_t vbase;      // first global vertex id
@@ -93,7 +95,6 @@ struct BArgs {
     uint64_t ntot;          // padded global vertex count
     const uint32_t *deg;    // per global vertex
     const uint32_t *iso;    // one bit per global vertex of degree 0
-    const uint32_t *iso0;   // the same bits in original-id order
     uint64_t *vis, *front, *next;
     uint32_t *pred;         // output parents, vertex-major per graph: [v][nroots]
     uint32_t *queue;
@@ -228,7 +229,8 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
 {
     __shared__ uint64_t s_evm[kW][kSerial][32];
     __shared__ uint32_t s_evu[kW][kSerial][32];
-    if (a.st->err || a.st->level < 0 || a.st->active == 0) return;
+    // no graph expands bottom-up this level
+    if (a.st->err || a.st->level < 0 || a.st->active == 0 || !(a.st->dirs & 2u)) return;
     const int lane = g5_lane(), wib = threadIdx.x >> 5;
     const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
@@ -236,23 +238,23 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
     for (uint64_t w = gw; w < a.ntot / 32; w += nw) {
         // vertices in original-id order: high-degree vertices, which have
         // the lowest new ids, spread over the warps
-        const uint64_t go = w * 32 + lane;
         const GraphDesc &d = a.gd[graph_of(a, w * 32)];
         if (d.dir != BU || d.nf == 0) continue;
-        const uint64_t ol = go - d.vbase;
+        const uint64_t ol = w * 32 + lane - d.vbase;
         const uint32_t R = (uint32_t)d.nroots;
-        const bool iso = (__ldg(a.iso0 + (go >> 5)) >> lane) & 1u;
-        const bool real = (int64_t)ol < d.n && !iso;
-        const uint64_t vl = real ? __ldg(d.perm + ol) : 0;
-        const uint64_t v = d.vbase + vl;
-        // roots with an empty frontier cannot reach v this level; vertices
-        // without edges are never reached
-        uint64_t need = real ? (~a.vis[v] & d.amask) : 0;
-        int64_t s = 0, e = 0;
-        if (need) {
-            s = d.row_off[vl];
-            e = d.row_off[vl + 1];
+        // new id and row bounds, indexed by original id: three coalesced
+        // loads issued together
+        uint32_t vl = 0, dg = 0;
+        int64_t s = 0;
+        if ((int64_t)ol < d.n) {
+            vl = __ldg(d.perm + ol);
+            s = __ldg(d.ostart + ol);
+            dg = __ldg(d.odeg + ol);  // 0: no edges, never reached
         }
+        const int64_t e = s + dg;
+        const uint64_t v = d.vbase + vl;
+        // roots with an empty frontier cannot reach v
+        uint64_t need = dg ? (~a.vis[v] & d.amask) : 0;
         // serial probes: all loads first, then the hits in adjacency order
         uint32_t u[kSerial];
         uint64_t f[kSerial];
@@ -783,20 +785,6 @@ __global__ void k_bdeg(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t
     }
 }
 
-// iso0: degree-0 bits in original-id order (padding vertices count as isolated)
-__global__ void k_biso0(const GraphDesc *gd, const uint8_t *chunk_graph, uint64_t ntot, const uint32_t *deg,
-                        uint32_t *iso0)
-{
-    for (uint64_t go = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; go < ntot;
-         go += (uint64_t)gridDim.x * blockDim.x) {
-        const GraphDesc &d = gd[chunk_graph[go / kChunk]];
-        const int64_t ol = (int64_t)(go - d.vbase);
-        const bool z = ol >= d.n || deg[d.vbase + d.perm[ol]] == 0u;
-        const unsigned m = __ballot_sync(0xFFFFFFFFu, z);
-        if ((threadIdx.x & 31) == 0) iso0[go >> 5] = m;
-    }
-}
-
 // ---- degree-ordered copy of a graph ----------------------------------------------------
 
 __global__ void k_rl_deg(const int64_t *row_off, int64_t n, uint32_t *deg, uint32_t *ids)
@@ -817,6 +805,18 @@ __global__ void k_rl_perm(const uint32_t *orig, const uint32_t *deg_sorted, int6
         } else {
             row2[n] = 0;
         }
+    }
+}
+
+// by original id: where the vertex's row starts in the copy, and its degree
+// (the bottom-up sweep walks original ids and reads these coalesced)
+__global__ void k_rl_orig(const uint32_t *perm, const int64_t *row2, int64_t n, int64_t *ostart, uint32_t *odeg)
+{
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t p = perm[o];
+        const int64_t s = row2[p];
+        ostart[o] = s;
+        odeg[o] = (uint32_t)(row2[p + 1] - s);
     }
 }
 
@@ -844,7 +844,6 @@ struct g5_batch {
     uint8_t *chunk_graph = nullptr;
     uint32_t *deg = nullptr;
     uint32_t *iso = nullptr;
-    uint32_t *iso0 = nullptr;
     uint64_t *words = nullptr;  // vis | front | next
     uint32_t *queue = nullptr;
     uint64_t *qoff = nullptr;
@@ -944,7 +943,6 @@ void free_batch(g5_batch *b)
     cudaFree(b->chunk_graph);
     cudaFree(b->deg);
     cudaFree(b->iso);
-    cudaFree(b->iso0);
     cudaFree(b->words);
     cudaFree(b->queue);
     cudaFree(b->qoff);
@@ -979,13 +977,16 @@ g5_status build_relabel(g5_batch *b, const g5_graph *g, GraphDesc &d)
         b->owned.push_back(*p);
         return true;
     };
-    uint32_t *orig = nullptr, *perm = nullptr, *col2 = nullptr;
-    int64_t *row2 = nullptr;
+    uint32_t *orig = nullptr, *perm = nullptr, *col2 = nullptr, *odeg = nullptr;
+    int64_t *row2 = nullptr, *ostart = nullptr;
     if (!alloc((void **)&orig, sizeof(uint32_t) * n) || !alloc((void **)&perm, sizeof(uint32_t) * n) ||
-        !alloc((void **)&row2, sizeof(int64_t) * (n + 1)) || !alloc((void **)&col2, sizeof(uint32_t) * nnz))
+        !alloc((void **)&row2, sizeof(int64_t) * (n + 1)) || !alloc((void **)&col2, sizeof(uint32_t) * nnz) ||
+        !alloc((void **)&ostart, sizeof(int64_t) * n) || !alloc((void **)&odeg, sizeof(uint32_t) * n))
         return G5_ERR_OOM;
     d.orig = orig;
     d.perm = perm;
+    d.ostart = ostart;
+    d.odeg = odeg;
     d.row_off = row2;
     d.col = col2;
     if (n == 0) {
@@ -1005,6 +1006,7 @@ g5_status build_relabel(g5_batch *b, const g5_graph *g, GraphDesc &d)
     k_rl_perm<<<blocks, 256, 0, s>>>(orig, deg_sorted.p, n, perm, row2);
     G5_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, t2, row2, row2, n + 1, s));
     k_rl_cols<<<blocks, 256, 0, s>>>(g->row_off, g->col, orig, perm, row2, n, col2);
+    k_rl_orig<<<blocks, 256, 0, s>>>(perm, row2, n, ostart, odeg);
     G5_CUDA(cudaStreamSynchronize(s));
     return G5_OK;
 }
@@ -1061,7 +1063,6 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     B_ALLOC(b->chunk_graph, cg.size());
     B_ALLOC(b->deg, sizeof(uint32_t) * vb);
     B_ALLOC(b->iso, sizeof(uint32_t) * (vb / 32));
-    B_ALLOC(b->iso0, sizeof(uint32_t) * (vb / 32));
     B_ALLOC(b->words, sizeof(uint64_t) * 3 * vb);
     B_ALLOC(b->queue, sizeof(uint32_t) * vb);
     B_ALLOC(b->qoff, sizeof(uint64_t) * (vb + 1));
@@ -1084,7 +1085,6 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     a.chunk_graph = b->chunk_graph;
     a.deg = b->deg;
     a.iso = b->iso;
-    a.iso0 = b->iso0;
     a.vis = b->words;
     a.front = b->words + vb;
     a.next = b->words + 2 * vb;
@@ -1100,7 +1100,6 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     a.root_off = b->root_off;
     a.level_log = b->level_log;
     k_bdeg<<<g5::grid_for(8), kB, 0, b->stream>>>(b->gd, b->chunk_graph, vb, b->deg, b->iso);
-    k_biso0<<<g5::grid_for(8), kB, 0, b->stream>>>(b->gd, b->chunk_graph, vb, b->deg, b->iso0);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
     *out = b;
     return G5_OK;

@@ -19,6 +19,9 @@ ALPHAS = (4.0, 14.0, 40.0, 120.0, 400.0)
 BETAS = (64.0, 200.0, 600.0, 2000.0, 6000.0)
 TILES = (64, 128, 256, 512)
 SERIALS = (4, 8, 16, 32)
+# the batched search steps 64 roots at once and its bottom-up levels are
+# cheap per root, so it leaves bottom-up at larger frontiers (smaller beta)
+BATCH_BETAS = (12.0, 24.0, 64.0, 200.0)
 
 _cache: dict = {}
 
@@ -56,7 +59,7 @@ def tune_plain(g5, graph, roots: Sequence[int], nedges: Sequence[int], alphas=AL
     return out
 
 
-def tune_batch(g5, torch, graphs, roots_per_graph, alphas=ALPHAS, betas=BETAS) -> dict:
+def tune_batch(g5, torch, graphs, roots_per_graph, alphas=ALPHAS, betas=BATCH_BETAS) -> dict:
     """Best (alpha, beta) for a batched search over the given graphs and roots."""
     import numpy as np
 
