@@ -316,6 +316,11 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
             }
 #pragma unroll
             for (int q = 0; q < 2; ++q) hq[q] = uq[q] != 0xFFFFFFFFu ? (a.front[d.vbase + uq[q]] & hq[q]) : 0ull;
+            // the parent's original id, loaded for every hit before the scans
+            // below, so its latency overlaps them
+            uint32_t oq[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) oq[q] = hq[q] ? __ldg(d.orig + uq[q]) : 0u;
             // segmented inclusive prefix OR: slots 0..31, then 32..63 with
             // the carry of a row that crosses slot 32
             uint64_t ia = hq[0], ib = hq[1];
@@ -337,7 +342,7 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
                 uint64_t x = hq[q] & ~(q ? eb : ea);
                 if (x) {
                     uint32_t *pv = a.pred + d.pred_base + vq[q] * R;
-                    const uint32_t uo = __ldg(d.orig + uq[q]);
+                    const uint32_t uo = oq[q];
                     while (x) {
                         const int rr = __ffsll((long long)x) - 1;
                         x &= x - 1;
@@ -395,6 +400,7 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
                         jj += 32;
                         continue;
                     }
+                    const uint32_t uo = hit ? __ldg(d.orig + uw[q]) : 0u;  // overlaps the scan
                     // first lane of each root: exclusive prefix OR over the lanes
                     uint64_t incl = hit;
 #pragma unroll
@@ -406,7 +412,6 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
                     if (lane == 0) excl = 0;
                     uint64_t x = hit & ~excl;
                     if (x) {
-                        const uint32_t uo = __ldg(d.orig + uw[q]);
                         while (x) {
                             const int rr = __ffsll((long long)x) - 1;
                             x &= x - 1;
@@ -428,25 +433,22 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
             }
         }
         __syncwarp();
-        // serial hits: lane k takes roots k and k + 32 of each vertex; the
-        // events' root sets are disjoint, so each root has one event
-        unsigned vm = __ballot_sync(0xFFFFFFFFu, sfound != 0);
-        while (vm) {
-            const int vi = __ffs(vm) - 1;
-            vm &= vm - 1;
-            const uint64_t sf = __shfl_sync(0xFFFFFFFFu, sfound, vi);
-            uint32_t *pv = a.pred + d.pred_base + (uint64_t)__shfl_sync(0xFFFFFFFFu, vo, vi) * R;
-            uint32_t p0 = 0, p1 = 0;
+        // serial hits, one (vertex, parent, roots) event at a time over the
+        // warp: lane k writes roots k and k + 32.  Empty events cost nothing,
+        // and the events' root sets are disjoint, so each parent is written
+        // once.
 #pragma unroll
-            for (int k = 0; k < kSerial; ++k) {
+        for (int k = 0; k < kSerial; ++k) {
+            unsigned em = __ballot_sync(0xFFFFFFFFu, s_evm[wib][k][lane] != 0ull);
+            while (em) {
+                const int vi = __ffs(em) - 1;
+                em &= em - 1;
                 const uint64_t m = s_evm[wib][k][vi];
-                if (!m) continue;
                 const uint32_t u = s_evu[wib][k][vi];
-                if ((m >> lane) & 1ull) p0 = u;
-                if ((m >> (lane + 32)) & 1ull) p1 = u;
+                uint32_t *pv = a.pred + d.pred_base + (uint64_t)__shfl_sync(0xFFFFFFFFu, vo, vi) * R;
+                if ((m >> lane) & 1ull) pv[lane] = u;
+                if ((m >> (lane + 32)) & 1ull) pv[lane + 32] = u;
             }
-            if ((sf >> lane) & 1ull) pv[lane] = p0;
-            if ((sf >> (lane + 32)) & 1ull) pv[lane + 32] = p1;
         }
         __syncwarp();
         if (found) a.next[v] |= found;  // only this lane writes v in a bottom-up level
