@@ -1183,7 +1183,8 @@ g5_status alloc_ws(g5_bfs *b)
     G5_CUDA(cudaMalloc(&b->bitmaps, sizeof(uint32_t) * 3 * a.nwords));
     G5_CUDA(cudaMalloc(&b->isolated, sizeof(uint32_t) * a.nwords));
     G5_CUDA(cudaMalloc(&b->heavy, sizeof(uint32_t) * a.nwords));
-    if (g->nnz < ((int64_t)1 << 32)) G5_CUDA(cudaMalloc(&b->ro32, sizeof(uint32_t) * (size_t)(n + 1)));
+    // 32-bit offsets while every scan position (row end + one 32-entry step) fits
+    if (g->nnz < ((int64_t)1 << 32) - 64) G5_CUDA(cudaMalloc(&b->ro32, sizeof(uint32_t) * (size_t)(n + 1)));
     G5_CUDA(cudaMalloc(&b->first, sizeof(uint32_t) * (size_t)n));
     G5_CUDA(cudaMalloc(&b->multi, sizeof(uint32_t) * a.nwords));
     G5_CUDA(cudaMalloc(&b->wdeg, sizeof(uint32_t) * a.nwords));
