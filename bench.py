@@ -408,7 +408,8 @@ def main():
                          "frac": kern["achieved"] / peak, "traffic": kern["traffic"],
                          "peak_kind": peak_kind + " (copy, burst)", "kernel": kern,
                          "search": {"achieved": achieved, "frac": achieved / peak,
-                                    "scope": "whole search (every kernel of the level loop), algorithmic bytes"}},
+                                    "scope": "whole search (every kernel of the level loop), algorithmic bytes"},
+                         "dram_measured": dram_measured(kern["name"], g.scale, peak)},
             "clocks": clocks,
             "validation": {"all_valid": all_valid, "all_min_parent": all_minpar},
             "plain": {"hmean_gteps": value_rank, "mean_ms": statistics.mean(dev_ms),
@@ -441,19 +442,44 @@ BU_KERNEL = "k_bu"
 TD_KERNEL = "k_td"
 
 
-def ncu_traffic(kernel, scale):
-    """DRAM bytes per launch of `kernel` at `scale` from the committed ncu
-    summary (profiles/<kernel>_scale<scale>.txt, line 'dram_bytes_per_launch:'),
-    or None."""
+def ncu_summary(kernel, scale):
+    """The 'key: value' lines of the committed ncu summary
+    profiles/<kernel>_scale<scale>.txt (DRAM bytes per launch, mean launch
+    time, whole-search DRAM throughput), as floats; {} when absent."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_scale{scale}.txt")
+    out = {}
     try:
         with open(path) as f:
             for ln in f:
-                if ln.startswith("dram_bytes_per_launch:"):
-                    return float(ln.split(":", 1)[1])
-    except OSError:
+                k, sep, v = ln.partition(":")
+                if sep and k in ("dram_bytes_per_launch", "ncu_mean_us", "search_dram_gbs_ncu"):
+                    out[k] = float(v)
+    except (OSError, ValueError):
         pass
-    return None
+    return out
+
+
+def ncu_traffic(kernel, scale):
+    """DRAM bytes per launch of `kernel` at `scale` from the committed ncu
+    summary, or None."""
+    return ncu_summary(kernel, scale).get("dram_bytes_per_launch")
+
+
+def dram_measured(kernel, scale, peak):
+    """Measured DRAM throughput from the committed ncu launch list: the
+    kernel's DRAM bytes over its own ncu durations (one capture for both, so
+    cold-cache and serialised), and the same for every kernel of the level
+    loop.  Reported beside the algorithmic roofline, not instead of it."""
+    s = ncu_summary(kernel, scale)
+    if "dram_bytes_per_launch" not in s or "ncu_mean_us" not in s:
+        return None
+    gbs = s["dram_bytes_per_launch"] / (s["ncu_mean_us"] * 1e-6) / 1e9
+    out = {"kernel_gbs": gbs, "kernel_frac": gbs / peak,
+           "source": f"ncu launch list, profiles/{kernel}_scale{scale}.txt (bytes and durations of one capture)"}
+    if "search_dram_gbs_ncu" in s:
+        out["search_gbs"] = s["search_dram_gbs_ncu"]
+        out["search_frac"] = s["search_dram_gbs_ncu"] / peak
+    return out
 
 
 def kernel_roofline(g5, g, roots, alpha, beta, peak, sizes=None):
