@@ -661,17 +661,27 @@ __global__ void __launch_bounds__(kB) k_bwrite(BArgs a)
     const uint32_t c = blockIdx.x;
     if (a.chunk_live[c] & 2u) return;
     const uint64_t v0 = (uint64_t)c * kChunk + (uint64_t)threadIdx.x * kPerThread;
-    uint64_t nx[kPerThread];
+    uint64_t nx[kPerThread], vs[kPerThread];
+    uint32_t dg[kPerThread];
     uint64_t cn = 0, cm = 0;
     const bool queued = a.chunk_n[c] != ~0ull;
+    // all loads before any store (the stores may alias the loads as far as
+    // the compiler knows, which would make every word its own round trip):
+    // the next words, then visited masks and degrees of the non-empty ones
+#pragma unroll
+    for (int k = 0; k < kPerThread; ++k) nx[k] = a.next[v0 + k];
 #pragma unroll
     for (int k = 0; k < kPerThread; ++k) {
-        nx[k] = a.next[v0 + k];
+        vs[k] = nx[k] ? a.vis[v0 + k] : 0ull;
+        dg[k] = nx[k] ? a.deg[v0 + k] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kPerThread; ++k) {
         if (nx[k]) {
-            a.vis[v0 + k] |= nx[k];
+            a.vis[v0 + k] = vs[k] | nx[k];
             a.next[v0 + k] = 0;
             ++cn;
-            cm += a.deg[v0 + k];
+            cm += dg[k];
         }
         a.front[v0 + k] = nx[k];
     }
@@ -710,14 +720,13 @@ __global__ void __launch_bounds__(kB) k_bwrite(BArgs a)
     for (int k = 0; k < kPerThread; ++k) {
         if (!nx[k]) continue;
         const uint64_t v = v0 + k;
-        const uint64_t dg = a.deg[v];
         a.queue[pos] = (uint32_t)v;
         a.qoff[pos] = mpos;
         a.qbase[pos] = d.row_off[v - d.vbase] - (int64_t)mpos;
         uint64_t t = (mpos + kTile - 1) / kTile;
-        const uint64_t tend = (mpos + dg + kTile - 1) / kTile;
+        const uint64_t tend = (mpos + dg[k] + kTile - 1) / kTile;
         for (; t < tend && t < a.max_tiles; ++t) a.tile_start[t] = (uint32_t)pos;
-        mpos += dg;
+        mpos += dg[k];
         ++pos;
     }
 }
