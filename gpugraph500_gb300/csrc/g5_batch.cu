@@ -470,45 +470,51 @@ __global__ void __launch_bounds__(kB, 8) k_btd(BArgs a)
 
 // ---- compaction ---------------------------------------------------------------------------
 
+// One warp per chunk over a persistent grid: the chunk's 2048 next words in
+// coalesced 256-byte loads, 16 in flight per lane, then the degrees of the
+// non-empty ones (no per-chunk block, barrier or serial tail).
 __global__ void __launch_bounds__(kB) k_bcount(BArgs a)
 {
-    const uint32_t c = blockIdx.x;
-    const uint64_t v0 = (uint64_t)c * kChunk + (uint64_t)threadIdx.x * kPerThread;
-    uint64_t cn = 0, cm = 0, act = 0;
+    constexpr int kBatch = 16;
+    const int lane = g5_lane();
+    const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
+    for (uint64_t c = gw; c < a.nchunks; c += nw) {
+        const uint64_t v0 = c * kChunk;
+        const uint8_t live = a.chunk_live[c];
+        uint64_t cn = 0, cm = 0, act = 0;
+        for (int i0 = 0; i0 < kChunk / 32; i0 += kBatch) {
+            uint64_t x[kBatch];
 #pragma unroll
-    for (int k = 0; k < kPerThread; ++k) {
-        const uint64_t x = a.next[v0 + k];
-        if (x) {
-            ++cn;
-            cm += a.deg[v0 + k];
-            act |= x;
-        }
-    }
-    cn = wsum(cn);
-    cm = wsum(cm);
-    // roots present in the next frontier of this chunk's graph
+            for (int k = 0; k < kBatch; ++k) x[k] = __ldg(a.next + v0 + (uint64_t)(i0 + k) * 32 + lane);
 #pragma unroll
-    for (int o = 16; o; o >>= 1) act |= __shfl_xor_sync(0xFFFFFFFFu, act, o);
-    if (g5_lane() == 0 && act)
-        atomicOr((unsigned long long *)&a.gd[a.chunk_graph[c]].amask_next, (unsigned long long)act);
-    __shared__ uint64_t s_n[kW], s_m[kW];
-    if (g5_lane() == 0) {
-        s_n[threadIdx.x >> 5] = cn;
-        s_m[threadIdx.x >> 5] = cm;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint64_t tn = 0, tm = 0;
-        for (int i = 0; i < kW; ++i) {
-            tn += s_n[i];
-            tm += s_m[i];
+            for (int k = 0; k < kBatch; ++k) {
+                if (x[k]) {
+                    ++cn;
+                    cm += __ldg(a.deg + v0 + (uint64_t)(i0 + k) * 32 + lane);
+                    act |= x[k];
+                }
+            }
         }
-        a.chunk_n[c] = tn;
-        a.chunk_m[c] = tm;
-        // no frontier this level nor the last: visited, front and next of
-        // the chunk stay as they are, so the write pass skips it
-        const bool prev = a.chunk_live[c] & 1u, cur = tn != 0;
-        a.chunk_live[c] = (uint8_t)(cur ? 1u : (prev ? 0u : 2u));
+        cn = wsum(cn);
+        cm = wsum(cm);
+        // roots present in the next frontier of this chunk's graph
+#pragma unroll
+        for (int o = 16; o; o >>= 1) act |= __shfl_xor_sync(0xFFFFFFFFu, act, o);
+        if (lane == 0) {
+            a.chunk_n[c] = cn;
+            a.chunk_m[c] = cm;
+            // all chunks of a graph OR into one word: an atomic only for
+            // roots not already recorded
+            if (act) {
+                unsigned long long *am = (unsigned long long *)&a.gd[a.chunk_graph[c]].amask_next;
+                if (act & ~*(volatile unsigned long long *)am) atomicOr(am, (unsigned long long)act);
+            }
+            // no frontier this level nor the last: visited, front and next of
+            // the chunk stay as they are, so the write pass skips it
+            const bool prev = live & 1u, cur = cn != 0;
+            a.chunk_live[c] = (uint8_t)(cur ? 1u : (prev ? 0u : 2u));
+        }
     }
 }
 
@@ -896,7 +902,7 @@ void enqueue_batch(g5_batch *b, const BArgs &a, cudaStream_t s, bool body, std::
         return;
     }
     mark();
-    k_bcount<<<a.nchunks, kB, 0, s>>>(a);
+    k_bcount<<<g5::grid_for(8), kB, 0, s>>>(a);
     mark();
     k_bscan<<<1, 1024, 0, s>>>(a);
     mark();
