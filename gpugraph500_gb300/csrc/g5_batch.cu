@@ -662,78 +662,69 @@ __global__ void __launch_bounds__(1024) k_bscan(BArgs a)
     }
 }
 
-__global__ void __launch_bounds__(kB) k_bwrite(BArgs a)
+// One warp per live chunk over a persistent grid: visited |= next, next ->
+// front, and for chunks of top-down graphs the queue entries in ascending
+// vertex order (a ballot per 32 words gives the positions, a warp scan the
+// edge offsets).  All loads of a step come before its stores.
+__global__ void __launch_bounds__(kB, 4) k_bwrite(BArgs a)
 {
-    const uint32_t c = blockIdx.x;
-    if (a.chunk_live[c] & 2u) return;
-    const uint64_t v0 = (uint64_t)c * kChunk + (uint64_t)threadIdx.x * kPerThread;
-    uint64_t nx[kPerThread], vs[kPerThread];
-    uint32_t dg[kPerThread];
-    uint64_t cn = 0, cm = 0;
-    const bool queued = a.chunk_n[c] != ~0ull;
-    // all loads before any store (the stores may alias the loads as far as
-    // the compiler knows, which would make every word its own round trip):
-    // the next words, then visited masks and degrees of the non-empty ones
+    constexpr int kBatch = 8;
+    const int lane = g5_lane();
+    const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
+    for (uint64_t c = gw; c < a.nchunks; c += nw) {
+        if (a.chunk_live[c] & 2u) continue;
+        const uint64_t v0 = c * kChunk;
+        uint64_t pos = a.chunk_n[c], mpos = a.chunk_m[c];
+        const bool queued = pos != ~0ull;
+        const GraphDesc &d = a.gd[a.chunk_graph[c]];
+        for (int i0 = 0; i0 < kChunk / 32; i0 += kBatch) {
+            uint64_t nx[kBatch], vs[kBatch];
+            uint32_t dg[kBatch];
 #pragma unroll
-    for (int k = 0; k < kPerThread; ++k) nx[k] = a.next[v0 + k];
+            for (int k = 0; k < kBatch; ++k) nx[k] = a.next[v0 + (uint64_t)(i0 + k) * 32 + lane];
 #pragma unroll
-    for (int k = 0; k < kPerThread; ++k) {
-        vs[k] = nx[k] ? a.vis[v0 + k] : 0ull;
-        dg[k] = nx[k] ? a.deg[v0 + k] : 0u;
-    }
+            for (int k = 0; k < kBatch; ++k) {
+                const uint64_t v = v0 + (uint64_t)(i0 + k) * 32 + lane;
+                vs[k] = nx[k] ? a.vis[v] : 0ull;
+                dg[k] = (nx[k] && queued) ? a.deg[v] : 0u;
+            }
 #pragma unroll
-    for (int k = 0; k < kPerThread; ++k) {
-        if (nx[k]) {
-            a.vis[v0 + k] = vs[k] | nx[k];
-            a.next[v0 + k] = 0;
-            ++cn;
-            cm += dg[k];
+            for (int k = 0; k < kBatch; ++k) {
+                const uint64_t v = v0 + (uint64_t)(i0 + k) * 32 + lane;
+                if (nx[k]) {
+                    a.vis[v] = vs[k] | nx[k];
+                    a.next[v] = 0;
+                }
+                a.front[v] = nx[k];
+            }
+            if (!queued) continue;
+#pragma unroll
+            for (int k = 0; k < kBatch; ++k) {
+                const unsigned bal = __ballot_sync(0xFFFFFFFFu, nx[k] != 0ull);
+                if (!bal) continue;
+                const uint64_t v = v0 + (uint64_t)(i0 + k) * 32 + lane;
+                const uint64_t dv = dg[k];
+                uint64_t incl = dv;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint64_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                if (nx[k]) {
+                    const uint64_t p = pos + __popc(bal & g5_lanemask_lt());
+                    const uint64_t mp = mpos + incl - dv;
+                    a.queue[p] = (uint32_t)v;
+                    a.qoff[p] = mp;
+                    a.qbase[p] = d.row_off[v - d.vbase] - (int64_t)mp;
+                    uint64_t t = (mp + kTile - 1) / kTile;
+                    const uint64_t tend = (mp + dv + kTile - 1) / kTile;
+                    for (; t < tend && t < a.max_tiles; ++t) a.tile_start[t] = (uint32_t)p;
+                }
+                pos += __popc(bal);
+                mpos += __shfl_sync(0xFFFFFFFFu, incl, 31);
+            }
         }
-        a.front[v0 + k] = nx[k];
-    }
-    if (!queued) return;
-    __shared__ uint64_t s_n[kW], s_m[kW];
-    const int lane = g5_lane(), wid = threadIdx.x >> 5;
-    uint64_t xn = cn, xm = cm;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint64_t yn = __shfl_up_sync(0xFFFFFFFFu, xn, o), ym = __shfl_up_sync(0xFFFFFFFFu, xm, o);
-        if (lane >= o) {
-            xn += yn;
-            xm += ym;
-        }
-    }
-    if (lane == 31) {
-        s_n[wid] = xn;
-        s_m[wid] = xm;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint64_t an = 0, am = 0;
-        for (int i = 0; i < kW; ++i) {
-            const uint64_t tn = s_n[i], tm = s_m[i];
-            s_n[i] = an;
-            s_m[i] = am;
-            an += tn;
-            am += tm;
-        }
-    }
-    __syncthreads();
-    uint64_t pos = a.chunk_n[c] + s_n[wid] + xn - cn;
-    uint64_t mpos = a.chunk_m[c] + s_m[wid] + xm - cm;
-    const GraphDesc &d = a.gd[a.chunk_graph[c]];
-#pragma unroll
-    for (int k = 0; k < kPerThread; ++k) {
-        if (!nx[k]) continue;
-        const uint64_t v = v0 + k;
-        a.queue[pos] = (uint32_t)v;
-        a.qoff[pos] = mpos;
-        a.qbase[pos] = d.row_off[v - d.vbase] - (int64_t)mpos;
-        uint64_t t = (mpos + kTile - 1) / kTile;
-        const uint64_t tend = (mpos + dg[k] + kTile - 1) / kTile;
-        for (; t < tend && t < a.max_tiles; ++t) a.tile_start[t] = (uint32_t)pos;
-        mpos += dg[k];
-        ++pos;
     }
 }
 
@@ -906,7 +897,7 @@ void enqueue_batch(g5_batch *b, const BArgs &a, cudaStream_t s, bool body, std::
     mark();
     k_bscan<<<1, 1024, 0, s>>>(a);
     mark();
-    k_bwrite<<<a.nchunks, kB, 0, s>>>(a);
+    k_bwrite<<<g5::grid_for(4), kB, 0, s>>>(a);
     mark();
     k_btd<<<g5::grid_for(8), kB, 0, s>>>(a);
     k_bbu<<<g5::grid_for(4), kB, 0, s>>>(a);
