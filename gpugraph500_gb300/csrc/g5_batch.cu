@@ -123,6 +123,16 @@ __device__ __forceinline__ uint64_t wsum(uint64_t v)
 
 __device__ __forceinline__ int graph_of(const BArgs &a, uint64_t v) { return a.chunk_graph[v / kChunk]; }
 
+// 4-byte asynchronous copy global -> shared (cp.async): the issuing thread
+// goes on at once; cp_async_wait_all() waits for all of its copies.
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    const size_t ga = __cvta_generic_to_global(gmem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(ga) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // ---- init: roots into next, parents of roots -------------------------------------
 
 __global__ void k_binit(BArgs a)
@@ -268,7 +278,9 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
         for (int k = 0; k < kSerial; ++k) {
             const uint64_t hit = f[k] & need;
             s_evm[wib][k][lane] = hit;
-            if (hit) s_evu[wib][k][lane] = __ldg(d.orig + u[k]);
+            // the parent's original id lands in shared memory while the
+            // rest of the row is scanned (read at the write-out below)
+            if (hit) cp_async4(&s_evu[wib][k][lane], d.orig + u[k]);
             need &= ~hit;
             sfound |= hit;
             if (u[k] != 0xFFFFFFFFu && (need | hit)) j = s + k + 1;
@@ -432,6 +444,7 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
                 ex += (uint64_t)(jj - st);
             }
         }
+        cp_async_wait_all();
         __syncwarp();
         // serial hits, one (vertex, parent, roots) event at a time over the
         // warp: lane k writes roots k and k + 32.  Empty events cost nothing,
