@@ -280,7 +280,8 @@ __device__ __forceinline__ void first_hit(const BfsArgs &a, bool mine, Off s, Of
         }
         j = s + 1;
     }
-    const Off lim = min(e, (Off)(s + a.bu_serial));
+    // lanes without a candidate scan nothing, whatever s and e they hold
+    const Off lim = mine ? min(e, (Off)(s + a.bu_serial)) : s;
     while (j < lim && !found) {
         uint32_t u[4];
         bool h[4];

@@ -77,12 +77,42 @@ def test_kronecker_parents_match_oracle(scale):
 
 
 def test_direction_extremes():
-    """Pure top-down (alpha huge) and early bottom-up (alpha tiny) agree."""
+    """Bottom-up from the first level on (alpha and beta huge), pure top-down
+    (both tiny) and a mix agree."""
     e = orc.kronecker(12)
     ro, col = orc.build_csr(1 << 12, e)
     roots = orc.select_roots(ro, 4)
     for alpha, beta in ((1e12, 1e12), (1e-6, 1e-6), (1.0, 2.0)):
         run_all_roots(ro, col, roots, alpha=alpha, beta=beta)
+
+
+@pytest.mark.parametrize("alpha,beta", [(1e12, 1e12), (14.0, 2000.0), (1e-6, 1e-6)])
+def test_level_log_matches_oracle(alpha, beta):
+    """Every level's frontier size and adjacency entries (the degree sum the
+    direction switch reads) equal the oracle's.  With alpha and beta huge the
+    search stays bottom-up from level 1 on, so the unvisited-list sweep, whose
+    per-word degree sums the count pass adds up, runs at consecutive levels."""
+    e = orc.kronecker(13)
+    ro, col = orc.build_csr(1 << 13, e)
+    deg = np.diff(ro)
+    roots = orc.select_roots(ro, 6)
+    g = g5.Graph.from_csr(ro, col)
+    for use_graph in (True, False):
+        b = g5.CudaBFS(g, alpha=alpha, beta=beta, use_graph=use_graph)
+        for r in roots:
+            b.runBFS(int(r))
+            _, lev = orc.bfs(ro, col, int(r))
+            log = b.level_log()
+            nlev = int(lev.max()) + 1
+            assert len(log) >= nlev
+            for L in range(nlev):
+                m = lev == L
+                assert (int(log[L, 1]), int(log[L, 2])) == (int(m.sum()), int(deg[m].sum())), (r, L, use_graph)
+            assert all(int(x) == 0 for x in log[nlev:, 1])
+            if alpha > 1e6 and nlev > 3:
+                assert int(log[2, 0]) == 1 and int(log[3, 0]) == 1  # consecutive bottom-up levels
+        b.close()
+    g.close()
 
 
 @pytest.mark.parametrize("tile,serial", [(32, 1), (128, 4), (1024, 16), (4096, 64)])
