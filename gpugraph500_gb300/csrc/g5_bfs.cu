@@ -280,8 +280,9 @@ __device__ __forceinline__ void first_hit(const BfsArgs &a, bool mine, Off s, Of
         }
         j = s + 1;
     }
-    // lanes without a candidate scan nothing, whatever s and e they hold
-    const Off lim = mine ? min(e, (Off)(s + a.bu_serial)) : s;
+    // (callers pass s = e = 0 on lanes without a candidate, so those lanes
+    // scan nothing here)
+    const Off lim = min(e, (Off)(s + a.bu_serial));
     while (j < lim && !found) {
         uint32_t u[4];
         bool h[4];
