@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="keep Beamer's alpha=14, beta=24")
     ap.add_argument("--alpha", type=float, default=None)
     ap.add_argument("--beta", type=float, default=None)
+    ap.add_argument("--tile-edges", type=int, default=None, help="fixed top-down tile size (skips the sizes tuner)")
+    ap.add_argument("--bu-serial", type=int, default=None, help="fixed bottom-up serial length (skips the sizes tuner)")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-codec", action="store_true")
@@ -295,7 +297,10 @@ def main():
         tuned = tune.tune_plain(g5, g, roots[:k], nedges[:k])
         alpha, beta = tuned["alpha"], tuned["beta"]
     sizes = {}
-    if not args.no_tune:
+    if args.tile_edges is not None or args.bu_serial is not None:
+        sizes = {k: v for k, v in (("tile_edges", args.tile_edges), ("bu_serial", args.bu_serial)) if v is not None}
+        tuned_sizes = None
+    elif not args.no_tune:
         st = tune.tune_sizes(g5, g, roots[:min(8, nr)], nedges[:min(8, nr)], alpha, beta)
         sizes = {"tile_edges": st["tile_edges"], "bu_serial": st["bu_serial"]}
         tuned_sizes = st["grid"][:6]
