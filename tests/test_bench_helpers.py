@@ -1,0 +1,42 @@
+"""bench.py's host-side helpers on CPU: the committed ncu summary parses into
+the roofline fields, and absent summaries give empty results, not errors."""
+import importlib.util
+import os
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def bench():
+    spec = importlib.util.spec_from_file_location("bench_module", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_committed_summary_parses(bench):
+    s = bench.ncu_summary("k_bu", 26)
+    assert {"dram_bytes_per_launch", "ncu_mean_us", "search_dram_gbs_ncu"} <= set(s)
+    assert bench.ncu_traffic("k_bu", 26) == s["dram_bytes_per_launch"] > 0
+    m = bench.dram_measured("k_bu", 26, 6786.9)
+    gbs = s["dram_bytes_per_launch"] / (s["ncu_mean_us"] * 1e-6) / 1e9
+    assert m["kernel_gbs"] == pytest.approx(gbs)
+    assert m["kernel_frac"] == pytest.approx(gbs / 6786.9)
+    assert m["search_frac"] == pytest.approx(s["search_dram_gbs_ncu"] / 6786.9)
+    # a measured fraction far above 1 would mean the summary is not the kernel's
+    assert 0 < m["kernel_frac"] < 1.2 and 0 < m["search_frac"] < 1.2
+
+
+def test_missing_summary(bench):
+    assert bench.ncu_summary("k_bu", 99) == {}
+    assert bench.ncu_traffic("k_bu", 99) is None
+    assert bench.dram_measured("k_bu", 99, 6786.9) is None
+
+
+def test_size_flags_parse(bench, monkeypatch):
+    monkeypatch.setattr("sys.argv", ["bench.py", "--tile-edges", "128", "--bu-serial", "8", "--alpha", "14"])
+    a = bench.parse()
+    assert (a.tile_edges, a.bu_serial, a.alpha, a.beta) == (128, 8, 14.0, None)
+    assert (a.scale, a.roots, a.gpus) == (26, 64, 1)
