@@ -293,7 +293,7 @@ def main():
         alpha = args.alpha if args.alpha is not None else alpha
         beta = args.beta if args.beta is not None else beta
     elif not args.no_tune:
-        k = min(8, nr)
+        k = min(16, nr)
         tuned = tune.tune_plain(g5, g, roots[:k], nedges[:k])
         alpha, beta = tuned["alpha"], tuned["beta"]
     sizes = {}
@@ -301,7 +301,7 @@ def main():
         sizes = {k: v for k, v in (("tile_edges", args.tile_edges), ("bu_serial", args.bu_serial)) if v is not None}
         tuned_sizes = None
     elif not args.no_tune:
-        st = tune.tune_sizes(g5, g, roots[:min(8, nr)], nedges[:min(8, nr)], alpha, beta)
+        st = tune.tune_sizes(g5, g, roots[:min(16, nr)], nedges[:min(16, nr)], alpha, beta)
         sizes = {"tile_edges": st["tile_edges"], "bu_serial": st["bu_serial"]}
         tuned_sizes = st["grid"][:6]
     else:
