@@ -414,7 +414,8 @@ def main():
                          "peak_kind": peak_kind + " (copy, burst)", "kernel": kern,
                          "search": {"achieved": achieved, "frac": achieved / peak,
                                     "scope": "whole search (every kernel of the level loop), algorithmic bytes"},
-                         "dram_measured": dram_measured(kern["name"], g.scale, peak)},
+                         "dram_measured": dram_measured(kern["name"], g.scale, peak),
+                         "traffic_settings": capture_settings(kern["name"], g.scale, alpha, beta, sizes or {})},
             "clocks": clocks,
             "validation": {"all_valid": all_valid, "all_min_parent": all_minpar},
             "plain": {"hmean_gteps": value_rank, "mean_ms": statistics.mean(dev_ms),
@@ -459,7 +460,10 @@ def ncu_summary(kernel, scale):
                 k, sep, v = ln.partition(":")
                 if sep and k in ("dram_bytes_per_launch", "ncu_mean_us", "search_dram_gbs_ncu"):
                     out[k] = float(v)
-    except (OSError, ValueError):
+                elif sep and k == "settings":
+                    # "alpha=14 beta=2000 tile_edges=128 bu_serial=8"
+                    out["settings"] = {kv.split("=")[0]: float(kv.split("=")[1]) for kv in v.split() if "=" in kv}
+    except (OSError, ValueError, IndexError):
         pass
     return out
 
@@ -468,6 +472,17 @@ def ncu_traffic(kernel, scale):
     """DRAM bytes per launch of `kernel` at `scale` from the committed ncu
     summary, or None."""
     return ncu_summary(kernel, scale).get("dram_bytes_per_launch")
+
+
+def capture_settings(kernel, scale, alpha, beta, sizes):
+    """The thresholds and sizes of the committed capture, and whether they are
+    this run's (the per-launch traffic depends on the launch mix they give)."""
+    cap = ncu_summary(kernel, scale).get("settings")
+    if cap is None:
+        return None
+    run = {"alpha": float(alpha), "beta": float(beta),
+           "tile_edges": float(sizes.get("tile_edges", 256)), "bu_serial": float(sizes.get("bu_serial", 8))}
+    return {"capture": cap, "run": run, "match": all(cap.get(k) == v for k, v in run.items())}
 
 
 def dram_measured(kernel, scale, peak):

@@ -29,6 +29,16 @@ def test_committed_summary_parses(bench):
     assert 0 < m["kernel_frac"] < 1.2 and 0 < m["search_frac"] < 1.2
 
 
+def test_capture_settings(bench):
+    cap = bench.ncu_summary("k_bu", 26)["settings"]
+    assert set(cap) == {"alpha", "beta", "tile_edges", "bu_serial"}
+    same = bench.capture_settings("k_bu", 26, cap["alpha"], cap["beta"],
+                                  {"tile_edges": int(cap["tile_edges"]), "bu_serial": int(cap["bu_serial"])})
+    assert same["match"]
+    other = bench.capture_settings("k_bu", 26, cap["alpha"] * 2, cap["beta"], {})
+    assert not other["match"] and other["run"]["tile_edges"] == 256
+
+
 def test_missing_summary(bench):
     assert bench.ncu_summary("k_bu", 99) == {}
     assert bench.ncu_traffic("k_bu", 99) is None
