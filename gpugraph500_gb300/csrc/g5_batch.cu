@@ -47,7 +47,6 @@ namespace {
 constexpr int kB = 256;
 constexpr int kW = kB / 32;
 constexpr int kChunk = 2048;           // vertices per compaction chunk
-constexpr int kPerThread = kChunk / kB;
 constexpr uint64_t kTile = 256;        // edges per top-down warp tile
 constexpr int kSerial = 4;             // bottom-up entries scanned per lane first
 constexpr int kMaxGraphs = 64;
@@ -74,7 +73,7 @@ struct GraphDesc {
     uint64_t mu;         // adjacency entries of not fully visited vertices
     uint64_t examined;
     uint64_t amask;      // roots whose frontier is not empty (this level)
-    uint64_t amask_next; // being collected by k_bwrite for the next level
+    uint64_t amask_next; // being collected by k_bcount for the next level
 };
 
 struct BState {
