@@ -68,3 +68,29 @@ def test_product_does_not_reference_oracle():
             if f.endswith((".py", ".cu", ".cpp", ".h", ".cuh")):
                 src = open(os.path.join(dirpath, f)).read()
                 assert "g5_oracle" not in src and "libg5oracle" not in src and "import oracle" not in src, f
+
+
+def test_config_defaults(libg5):
+    """The defaults the tuner starts from: Beamer's thresholds, tile 256, serial 8."""
+    import gpugraph500_gb300 as g5
+    from gpugraph500_gb300 import tune
+    cfg = g5.BfsConfig()
+    g5.lib().g5_bfs_config_default(C.byref(cfg))
+    assert (cfg.alpha, cfg.beta) == tune.DEFAULT_THRESHOLDS
+    assert (cfg.tile_edges, cfg.bu_serial) == tune.DEFAULT_SIZES
+    assert (cfg.parent_mode, cfg.codec_threshold, cfg.max_levels, cfg.use_graph) == (0, 64, 4096, 1)
+
+
+def test_codec_batch_bound(libg5):
+    """The batched bound: every stream's single-call bound rounded up to 4
+    words (16-byte aligned stream starts), summed."""
+    import numpy as np
+    import gpugraph500_gb300 as g5
+    sizes = [0, 1, 63, 64, 65, 127, 128, 2049, 100000]
+    in_off = np.zeros(len(sizes) + 1, np.uint64)
+    in_off[1:] = np.cumsum(sizes)
+    libg5.g5_codec_bound.restype = C.c_size_t
+    libg5.g5_codec_bound.argtypes = [C.c_size_t]
+    want = sum((libg5.g5_codec_bound(n) + 3) // 4 * 4 for n in sizes)
+    assert g5.Codec.batch_bound(in_off) == want
+    assert g5.Codec.batch_bound(np.zeros(1, np.uint64)) == 0
