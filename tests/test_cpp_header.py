@@ -1,0 +1,27 @@
+"""include/g5bfs.hpp, the C++ host classes over the C ABI, compiles against
+the in-tree library and behaves on the host (no GPU needed)."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_cpp_header_builds_and_runs(tmp_path):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    import gpugraph500_gb300 as g5
+    if not os.path.exists(g5.LIB_PATH):
+        from gpugraph500_gb300 import build
+        build.build()
+    libdir = os.path.dirname(g5.LIB_PATH)
+    exe = str(tmp_path / "g5bfs_hpp_check")
+    subprocess.run([gxx, "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "g5bfs_hpp_check.cpp"), "-L", libdir, "-lg5bfs",
+                    "-Wl,-rpath," + libdir, "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    assert "g5bfs.hpp ok" in r.stdout
