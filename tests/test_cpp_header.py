@@ -25,3 +25,30 @@ def test_cpp_header_builds_and_runs(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
     assert "g5bfs.hpp ok" in r.stdout
+
+
+@pytest.mark.gpu
+def test_cpp_classes_on_gpu_match_oracle(tmp_path):
+    """g5::CudaBFS from C++: parents equal the oracle's, the device validator
+    accepts them; g5::GpuSimd round-trips a compressed queue."""
+    import numpy as np
+
+    import oracle as orc
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    import gpugraph500_gb300 as g5
+    libdir = os.path.dirname(g5.LIB_PATH)
+    exe = str(tmp_path / "g5bfs_hpp_gpu")
+    subprocess.run([gxx, "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "g5bfs_hpp_gpu.cpp"), "-L", libdir, "-lg5bfs",
+                    "-Wl,-rpath," + libdir, "-o", exe], check=True)
+    scale = 12
+    ro, col = orc.build_csr(1 << scale, orc.kronecker(scale))
+    roots = [int(r) for r in orc.select_roots(ro, 3)]
+    out = str(tmp_path / "parents.bin")
+    r = subprocess.run([exe, str(scale), out] + [str(x) for x in roots], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    got = np.fromfile(out, np.int64).reshape(len(roots), 1 << scale)
+    for i, root in enumerate(roots):
+        assert np.array_equal(got[i], orc.bfs(ro, col, root)[0]), root
