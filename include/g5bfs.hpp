@@ -140,6 +140,90 @@ public:
     }
 };
 
+// Batched search: up to 64 roots per graph over one or more resident graphs
+// in one level loop.  Parents go to a device buffer the caller owns, per
+// graph vertex-major ([v][roots of the graph]) and graphs one after another.
+class Batch {
+    g5_batch *bt_ = nullptr;
+
+public:
+    explicit Batch(const std::vector<const Graph *> &graphs)
+    {
+        std::vector<g5_graph *> gs;
+        for (const Graph *g : graphs) gs.push_back(g->get());
+        check(g5_batch_create(gs.data(), (int)gs.size(), &bt_), "g5_batch_create");
+    }
+    void set_direction(double alpha, double beta)
+    {
+        check(g5_batch_set_direction(bt_, alpha, beta), "g5_batch_set_direction");
+    }
+    // roots: graph-major, nroots[g] of them per graph; returns device ms
+    double run(const std::vector<int64_t> &roots, const std::vector<int> &nroots, uint32_t *pred_dev)
+    {
+        double ms = 0;
+        check(g5_batch_run(bt_, roots.data(), nroots.data(), pred_dev, &ms), "g5_batch_run");
+        return ms;
+    }
+    g5_batch *get() const { return bt_; }
+
+    Batch(const Batch &) = delete;
+    Batch &operator=(const Batch &) = delete;
+    ~Batch()
+    {
+        if (bt_) g5_batch_destroy(bt_);
+    }
+};
+
+// Serving: resident graphs, queries submitted as they arrive and batched
+// on the GPU (continuous batching), results fetched by ticket.
+class Server {
+    g5_server *sv_ = nullptr;
+    std::vector<int64_t> n_;
+
+public:
+    Server(const std::vector<const Graph *> &graphs, size_t mem_budget, int mode = G5_SERVE_STREAMS,
+           bool keep_results = true)
+    {
+        std::vector<g5_graph *> gs;
+        for (const Graph *g : graphs) {
+            gs.push_back(g->get());
+            n_.push_back(g->n());
+        }
+        check(g5_server_create(gs.data(), (int)gs.size(), mem_budget, keep_results ? 1 : 0, mode, &sv_),
+              "g5_server_create");
+    }
+    uint64_t submit(int graph, int64_t root)
+    {
+        uint64_t t = 0;
+        check(g5_server_submit(sv_, graph, root, &t), "g5_server_submit");
+        return t;
+    }
+    // true once the query has finished (false on timeout)
+    bool wait(uint64_t ticket, double timeout_s)
+    {
+        int done = 0;
+        check(g5_server_wait(sv_, ticket, timeout_s, &done), "g5_server_wait");
+        return done != 0;
+    }
+    // the query's parents (graph's vertex count entries); latency in ms
+    std::vector<int64_t> result(uint64_t ticket, int graph, double *latency_ms = nullptr)
+    {
+        std::vector<int64_t> pred((size_t)n_.at((size_t)graph));
+        double lat = 0, queue = 0;
+        check(g5_server_result(sv_, ticket, pred.data(), &lat, &queue), "g5_server_result");
+        if (latency_ms) *latency_ms = lat;
+        return pred;
+    }
+    g5_server *get() const { return sv_; }
+
+    Server(const Server &) = delete;
+    Server &operator=(const Server &) = delete;
+    ~Server()
+    {
+        if (sv_) g5_server_destroy(sv_);
+    }
+};
+
 // The codec plugin.  Base is the reference's Compression<int64_t, uint32_t>
 // (a template parameter, so this header needs none of the reference's).
 // The plugin emits the stream of the reference's cpusimd plugin: by default

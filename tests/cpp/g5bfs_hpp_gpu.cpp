@@ -1,12 +1,16 @@
 // The C++ host classes of include/g5bfs.hpp on a GPU: builds the Graph500
-// Kronecker graph of the given scale on the device, runs g5::CudaBFS for
-// each root given, checks the device validator, and writes the parents
-// (int64, n per root) to the output file for comparison with the oracle;
-// then round-trips a queue longer than the threshold through g5::GpuSimd
-// (the device codec).  Exit code 0 = pass; otherwise the failed step.
+// Kronecker graph of the given scale on the device; for the roots given runs
+// g5::CudaBFS (device validator checked), one g5::Batch over all of them and
+// one g5::Server query each, and writes the three sets of parents to the
+// output file for comparison with the oracle (plain: int64 [root][v];
+// batch: uint32 [v][root]; server: int64 [root][v]); then round-trips a queue
+// longer than the threshold through g5::GpuSimd (the device codec).
+// Exit code 0 = pass; otherwise the failed step.
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
+
+#include <cuda_runtime_api.h>
 
 #include "g5bfs.hpp"
 
@@ -33,14 +37,39 @@ static int run(int argc, char **argv)
     FILE *f = std::fopen(argv[2], "wb");
     if (!f) return 101;
     g5::Graph g = g5::Graph::kronecker(scale);
+    const size_t n = (size_t)g.n();
+    std::vector<int64_t> roots;
+    for (int i = 3; i < argc; ++i) roots.push_back(std::atoll(argv[i]));
     g5::CudaBFS bfs(g);
-    for (int i = 3; i < argc; ++i) {
-        const int64_t root = std::atoll(argv[i]);
+    for (int64_t root : roots) {
         bfs.runBFS(root);
         bool minp = false;
         if (!bfs.validate(&minp) || !minp) return 1;
         if (bfs.getPredecessor()[root] != root) return 2;
-        if (std::fwrite(bfs.getPredecessor(), sizeof(int64_t), (size_t)g.n(), f) != (size_t)g.n()) return 3;
+        if (std::fwrite(bfs.getPredecessor(), sizeof(int64_t), n, f) != n) return 3;
+    }
+
+    g5::Batch bt({&g});
+    const int R = (int)roots.size();
+    uint32_t *pred_dev = nullptr;
+    if (cudaMalloc((void **)&pred_dev, sizeof(uint32_t) * n * R) != cudaSuccess) return 20;
+    bt.run(roots, {R}, pred_dev);
+    std::vector<uint32_t> bp(n * R);
+    if (cudaMemcpy(bp.data(), pred_dev, sizeof(uint32_t) * n * R, cudaMemcpyDeviceToHost) != cudaSuccess) return 21;
+    cudaFree(pred_dev);
+    if (std::fwrite(bp.data(), sizeof(uint32_t), n * R, f) != n * R) return 22;
+
+    {
+        g5::Server sv({&g}, (size_t)1 << 30);
+        std::vector<uint64_t> tickets;
+        for (int64_t root : roots) tickets.push_back(sv.submit(0, root));
+        for (uint64_t t : tickets) {
+            if (!sv.wait(t, 60.0)) return 30;
+            double lat = -1;
+            const std::vector<int64_t> p = sv.result(t, 0, &lat);
+            if (p.size() != n || lat < 0) return 31;
+            if (std::fwrite(p.data(), sizeof(int64_t), n, f) != n) return 32;
+        }
     }
     std::fclose(f);
 
@@ -53,10 +82,10 @@ static int run(int argc, char **argv)
     c.compress(q.data(), q.size(), &z, zs);
     if (!z || !c.isCompressed(q.size(), zs) || zs >= q.size()) return 4;
     int64_t *back = nullptr;
-    size_t n = q.size();
-    c.decompress(z, (int)zs, &back, n);
-    if (!back || n != q.size()) return 5;
-    for (size_t i = 0; i < n; ++i)
+    size_t m = q.size();
+    c.decompress(z, (int)zs, &back, m);
+    if (!back || m != q.size()) return 5;
+    for (size_t i = 0; i < m; ++i)
         if (back[i] != q[i]) return 6;
     std::free(z);
     std::free(back);

@@ -29,8 +29,9 @@ def test_cpp_header_builds_and_runs(tmp_path):
 
 @pytest.mark.gpu
 def test_cpp_classes_on_gpu_match_oracle(tmp_path):
-    """g5::CudaBFS from C++: parents equal the oracle's, the device validator
-    accepts them; g5::GpuSimd round-trips a compressed queue."""
+    """g5::CudaBFS, g5::Batch and g5::Server from C++: parents equal the
+    oracle's (the device validator accepts the plain ones); g5::GpuSimd
+    round-trips a compressed queue."""
     import numpy as np
 
     import oracle as orc
@@ -42,13 +43,22 @@ def test_cpp_classes_on_gpu_match_oracle(tmp_path):
     exe = str(tmp_path / "g5bfs_hpp_gpu")
     subprocess.run([gxx, "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "g5bfs_hpp_gpu.cpp"), "-L", libdir, "-lg5bfs",
-                    "-Wl,-rpath," + libdir, "-o", exe], check=True)
+                    "-I", "/usr/local/cuda/include", "-L", "/usr/local/cuda/lib64", "-lcudart",
+                    "-Wl,-rpath," + libdir, "-Wl,-rpath,/usr/local/cuda/lib64", "-o", exe], check=True)
     scale = 12
     ro, col = orc.build_csr(1 << scale, orc.kronecker(scale))
     roots = [int(r) for r in orc.select_roots(ro, 3)]
     out = str(tmp_path / "parents.bin")
     r = subprocess.run([exe, str(scale), out] + [str(x) for x in roots], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
-    got = np.fromfile(out, np.int64).reshape(len(roots), 1 << scale)
+    n, k = 1 << scale, len(roots)
+    raw = open(out, "rb").read()
+    assert len(raw) == 8 * n * k + 4 * n * k + 8 * n * k
+    plain = np.frombuffer(raw[: 8 * n * k], np.int64).reshape(k, n)
+    batch = np.frombuffer(raw[8 * n * k: 12 * n * k], np.uint32).reshape(n, k)
+    served = np.frombuffer(raw[12 * n * k:], np.int64).reshape(k, n)
     for i, root in enumerate(roots):
-        assert np.array_equal(got[i], orc.bfs(ro, col, root)[0]), root
+        want = orc.bfs(ro, col, root)[0]
+        assert np.array_equal(plain[i], want), root
+        assert np.array_equal(batch[:, i].astype(np.int64), np.where(want < 0, 0xFFFFFFFF, want)), root
+        assert np.array_equal(served[i], want), root
