@@ -20,7 +20,6 @@ path (the oracle port of CPUBFS_bin) on the host cores instead.
 from __future__ import annotations
 
 import argparse
-import ctypes as C
 import json
 import os
 import statistics
