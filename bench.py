@@ -413,7 +413,8 @@ def main():
                          "peak_kind": peak_kind + " (copy, burst)", "kernel": kern,
                          "search": {"achieved": achieved, "frac": achieved / peak,
                                     "scope": "whole search (every kernel of the level loop), algorithmic bytes"},
-                         "dram_measured": dram_measured(kern["name"], g.scale, peak),
+                         "dram_measured": dram_measured(kern["name"], g.scale, peak, value_rank,
+                                                        statistics.mean(nedges) if nedges else None),
                          "traffic_settings": capture_settings(kern["name"], g.scale, alpha, beta, sizes or {})},
             "clocks": clocks,
             "validation": {"all_valid": all_valid, "all_min_parent": all_minpar},
@@ -457,7 +458,8 @@ def ncu_summary(kernel, scale):
         with open(path) as f:
             for ln in f:
                 k, sep, v = ln.partition(":")
-                if sep and k in ("dram_bytes_per_launch", "ncu_mean_us", "search_dram_gbs_ncu"):
+                if sep and k in ("dram_bytes_per_launch", "ncu_mean_us", "search_dram_gbs_ncu",
+                                 "search_dram_bytes_per_search"):
                     out[k] = float(v)
                 elif sep and k == "settings":
                     # "alpha=14 beta=2000 tile_edges=128 bu_serial=8"
@@ -484,11 +486,15 @@ def capture_settings(kernel, scale, alpha, beta, sizes):
     return {"capture": cap, "run": run, "match": all(cap.get(k) == v for k, v in run.items())}
 
 
-def dram_measured(kernel, scale, peak):
+def dram_measured(kernel, scale, peak, gteps=None, edges_per_search=None):
     """Measured DRAM throughput from the committed ncu launch list: the
     kernel's DRAM bytes over its own ncu durations (one capture for both, so
     cold-cache and serialised), and the same for every kernel of the level
-    loop.  Reported beside the algorithmic roofline, not instead of it."""
+    loop.  With the run's TEPS and mean Graph500 edge count per search, also
+    the "measured bytes per traversed edge" view: the capture's DRAM bytes per
+    search over the edges, times the run's TEPS, against the nominal 8 TB/s
+    and the measured peak (cold-cache bytes, so an upper estimate).  Reported
+    beside the algorithmic roofline, not instead of it."""
     s = ncu_summary(kernel, scale)
     if "dram_bytes_per_launch" not in s or "ncu_mean_us" not in s:
         return None
@@ -498,6 +504,13 @@ def dram_measured(kernel, scale, peak):
     if "search_dram_gbs_ncu" in s:
         out["search_gbs"] = s["search_dram_gbs_ncu"]
         out["search_frac"] = s["search_dram_gbs_ncu"] / peak
+    if "search_dram_bytes_per_search" in s and gteps and edges_per_search:
+        bpe = s["search_dram_bytes_per_search"] / edges_per_search
+        gbs = bpe * gteps
+        out["bytes_per_teps_edge"] = bpe
+        out["at_value_gbs"] = gbs
+        out["at_value_frac_of_8tbs"] = gbs / 8000.0
+        out["at_value_frac"] = gbs / peak
     return out
 
 

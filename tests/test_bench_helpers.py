@@ -29,6 +29,16 @@ def test_committed_summary_parses(bench):
     assert 0 < m["kernel_frac"] < 1.2 and 0 < m["search_frac"] < 1.2
 
 
+def test_bytes_per_edge_view(bench):
+    s = bench.ncu_summary("k_bu", 26)
+    m = bench.dram_measured("k_bu", 26, 6786.9, 640.0, 1.07e9)
+    bpe = s["search_dram_bytes_per_search"] / 1.07e9
+    assert m["bytes_per_teps_edge"] == pytest.approx(bpe)
+    assert m["at_value_gbs"] == pytest.approx(bpe * 640.0)
+    assert m["at_value_frac_of_8tbs"] == pytest.approx(bpe * 640.0 / 8000.0)
+    assert "at_value_gbs" not in bench.dram_measured("k_bu", 26, 6786.9)
+
+
 def test_capture_settings(bench):
     cap = bench.ncu_summary("k_bu", 26)["settings"]
     assert set(cap) == {"alpha", "beta", "tile_edges", "bu_serial"}
