@@ -808,8 +808,8 @@ __global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
     const bool want_u = a.st->list_mode != 0;  // next level is bottom-up
     uint64_t pos = a.chunk_n[c], mpos = a.chunk_m[c], upos = a.chunk_u[c];
     // every word of the warp's range up front (one load per lane and word,
-    // all in flight at once): xs = next, vs = visited | next (all ones past
-    // the end, so those words hold no unvisited vertex)
+    // all in flight at once): xs = next, vs = visited (all ones past the
+    // end, so those words hold no unvisited vertex)
     uint32_t xs[kWordIters], vs[kWordIters];
 #pragma unroll
     for (int i = 0; i < kWordIters; ++i) {
