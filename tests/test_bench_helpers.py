@@ -60,3 +60,28 @@ def test_size_flags_parse(bench, monkeypatch):
     a = bench.parse()
     assert (a.tile_edges, a.bu_serial, a.alpha, a.beta) == (128, 8, 14.0, None)
     assert (a.scale, a.roots, a.gpus) == (26, 64, 1)
+
+
+def _profile_commands():
+    """Every `python bench.py ...` command quoted in profiles/ (continuation
+    lines joined), as argument lists."""
+    import glob
+    import shlex
+    cmds = []
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*"))):
+        text = open(path).read().replace("\\\n", " ")
+        for line in text.splitlines():
+            if "python bench.py" in line:
+                args = shlex.split(line.split("python bench.py", 1)[1])
+                cmds.append((os.path.basename(path), args))
+    return cmds
+
+
+def test_profile_commands_parse(bench, monkeypatch):
+    """The captures under profiles/ can be re-run: their bench.py command
+    lines use options the current bench.py accepts."""
+    cmds = _profile_commands()
+    assert cmds, "no bench.py command quoted under profiles/"
+    for name, args in cmds:
+        monkeypatch.setattr("sys.argv", ["bench.py"] + args)
+        bench.parse()  # argparse exits on an unknown option
