@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-codec", action="store_true")
+    ap.add_argument("--no-c2", action="store_true", help="skip the scale-22 search with the codec in the level loop")
+    ap.add_argument("--c2-scale", type=int, default=22)
     ap.add_argument("--big-scale", type=int, default=0,
                     help="also compare plain and batched search on a second, larger graph (e.g. 28)")
     ap.add_argument("--serve-rates", default="1000,5000,20000")
@@ -206,44 +208,109 @@ def cpu_bfs_sample(ro, col, roots, nedges, seconds, threads):
     return hmean(res), len(res)
 
 
-def reference_arm(args):
-    rank, ws, dist = dist_init(args)
-    if rank != 0:
-        return 0
-    import gpugraph500_gb300 as g5
+def workload_name(scale, roots):
+    """config.workload of both arms: the same string for the same workload."""
+    return f"plain BFS, kronecker scale {scale} edgefactor 16, {roots} roots"
 
-    # graph built by the GPU generator (bit-exact with the reference generator),
-    # copied to the host; the timed path is the CPU BFS only
-    g = g5.Graph.kronecker(args.scale)
-    roots = g5.select_roots(g, args.roots)
-    b = g5.CudaBFS(g)
-    nedges = []
-    for r in roots:
-        b.runBFS(int(r))
-        nedges.append(b.teps_edges())
-    b.close()
-    ro, col = g.csr()
-    g.close()
-    cores = os.cpu_count() or 1
-    per_step = max(args.cpu_seconds / max(args.steps + args.warmup, 1), 1.0)
-    for _ in range(args.warmup):
-        cpu_bfs_sample(ro, col, roots, nedges, per_step, cores)
-    vals, times, nrun = [], [], 0
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        v, k = cpu_bfs_sample(ro, col, roots, nedges, per_step, cores)
-        times.append(time.perf_counter() - t0)
-        vals.append(v)
-        nrun += k
-    value = hmean(vals)
-    sample = (f"oracle CPUBFS_bin port, scale {args.scale}, {nrun} searches over {args.steps} steps, "
-              f"{cores} searches in parallel (one per host thread)")
+
+def cpu_throughput_windows(lib, ro, col, roots, end_deg, threads, win_s, warm, steps):
+    """The oracle's CPUBFS_bin restatement on `threads` host threads, each
+    running one serial search after another over the roots, for warm + steps
+    windows of win_s seconds.  A search's Graph500 edges are credited to each
+    window in proportion to the part of its run inside the window (its edges
+    per second times the overlap), so a window's value is the threads'
+    aggregate edges per second whether or not a search ends inside it.
+    Returns per timed window GTEPS, the per-search GTEPS of every search that
+    overlapped the timed windows, and the searches run."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    n = len(ro) - 1
+    lock = threading.Lock()
+    runs = []  # (t_start, t_end, edges)
+    nxt = [0]
+    t0 = time.perf_counter()
+    t_stop = t0 + (warm + steps) * win_s
+
+    def worker():
+        pred = np.empty(n, np.int64)
+        while True:
+            with lock:
+                if time.perf_counter() >= t_stop:
+                    return
+                i = nxt[0] % len(roots)
+                nxt[0] += 1
+            a = time.perf_counter()
+            lib.g5o_bfs(n, ro.ctypes.data, col.ctypes.data, int(roots[i]), pred.ctypes.data, None)
+            b = time.perf_counter()
+            ne = orc.teps_edges(end_deg, pred)
+            with lock:
+                runs.append((a, b, ne))
+
+    ts = [threading.Thread(target=worker) for _ in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    vals = []
+    for k in range(warm, warm + steps):
+        w0, w1 = t0 + k * win_s, t0 + (k + 1) * win_s
+        e = sum(ne * max(0.0, min(b, w1) - max(a, w0)) / (b - a) for a, b, ne in runs if b > a)
+        vals.append(e / win_s / 1e9)
+    lo, hi = t0 + warm * win_s, t_stop
+    per = [ne / (b - a) / 1e9 for a, b, ne in runs if b > lo and a < hi and b > a]
+    return vals, per, len(runs)
+
+
+def reference_arm(args):
+    """The reference's CPU path (the oracle's restatement of CPUBFS_bin,
+    cpu_2d/cpubfs_bin.cpp:116-180, in the level order of
+    cpu_2d/globalbfs.hh:657-1128) on the host cores, on the same workload:
+    the Kronecker graph generated, built and searched by the oracle on the
+    host (generator cpu_2d/generator/graph_generator.c:157-187, CSR
+    cpu_2d/distmatrix2d.hh:745-1166, roots cpu_2d/main.cpp:351-392), TEPS
+    edge counts as the validator counts them (validate.h:440-443,485).  No
+    part of the GPU library is loaded.  Under torchrun only rank 0 runs."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    threads = orc.host_threads()
+    n = 1 << args.scale
+    t0 = time.perf_counter()
+    edges = orc.kronecker(args.scale, threads=threads)
+    end_deg = orc.endpoint_counts(n, edges, threads)
+    ro, col = orc.build_csr(n, edges, threads=threads)
+    del edges
+    build_s = time.perf_counter() - t0
+    roots = orc.select_roots(ro, args.roots)
+    lib = orc.lib()
+    # one search alone on one core: the reference loop is serial
+    # (cpu_2d/cpubfs_bin.cpp:147,168)
+    pred = np.empty(n, np.int64)
+    for _ in range(2):  # the first run also faults in the output's pages
+        a = time.perf_counter()
+        lib.g5o_bfs(n, ro.ctypes.data, col.ctypes.data, int(roots[0]), pred.ctypes.data, None)
+        serial_s = time.perf_counter() - a
+    serial = orc.teps_edges(end_deg, pred) / serial_s / 1e9
+    del pred
+    # aggregate over the host threads, one serial search per thread
+    win = max(args.cpu_seconds / max(args.steps + args.warmup, 1), 0.5)
+    vals, per, nrun = cpu_throughput_windows(lib, ro, col, roots, end_deg, threads, win, args.warmup, args.steps)
+    value = sum(vals) / len(vals) if vals else 0.0
+    sample = (f"oracle CPUBFS_bin restatement on the oracle-built graph, scale {args.scale}: {threads} host "
+              f"threads each running serial searches over the {len(roots)} roots, {nrun} searches; each step is "
+              f"a {win:.2f} s window credited with the edges per second of the searches running in it")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / max(len(times), 1),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * win,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
-            "data": "synthetic (Graph500 Kronecker, seeds 1,2)",
-            "config": {"workload": f"kronecker scale {args.scale} edgefactor 16, {args.roots} roots"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "data": "synthetic (Graph500 Kronecker, seeds 1,2, generated on the host by the oracle)",
+            "config": {"workload": workload_name(args.scale, len(roots)), "graph_build_s": round(build_s, 1),
+                       "nnz": int(ro[-1])},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                             "serial_one_core_gteps": serial,
+                             "per_search_hmean_gteps_under_load": hmean(per)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -366,7 +433,9 @@ def main():
         except g5.G5Error as e:
             batched = {"error": str(e)}
 
-    serve = mixed = codec = None
+    serve = mixed = codec = c2 = None
+    if rank == 0 and not args.no_c2:
+        c2 = bench_c2(g5, args)
     if rank == 0 and not args.no_serve:
         serve = bench_serve(g5, g, args)
     if rank == 0 and not args.no_mixed:
@@ -399,7 +468,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int64",
             "data": "synthetic (Graph500 Kronecker generated on the GPU, seeds 1,2)",
-            "config": {"workload": f"plain BFS, kronecker scale {args.scale} edgefactor 16, {nr} roots",
+            "config": {"workload": workload_name(args.scale, nr),
                        "n": g.n, "nnz": g.nnz, "roots": nr, "parallelism": "replicas" if ws > 1 else "1 GPU",
                        "l2": "inputs larger than L2 (CSR %.1f GB)" % ((g.nnz * 4 + g.n * 8) / 1e9),
                        "graph_build_s": round(gen_s, 2), "alpha": alpha, "beta": beta,
@@ -424,6 +493,7 @@ def main():
             "serve": serve,
             "mixed_batch": mixed,
             "codec": codec,
+            "codec_in_loop": c2,
             "big_scale": big,
             "cpu_baseline": cpu,
         }
@@ -698,6 +768,55 @@ def plain_vs_batched(g5, torch, g, args, tune, ab):
     bfs.close()
     return {"plain_hmean_gteps": plain, "plain_mean_ms": statistics.mean(ms), "batched": batched,
             "batched_over_plain": batched["aggregate_gteps"] / plain if plain else None}
+
+
+def bench_c2(g5, args):
+    """Plain search with every level's sorted queue encoded and decoded by the
+    s4-bp128-d4 codec inside the level loop (the decoded queue feeds the next
+    top-down level; a device-side compare of the round trip turns any
+    difference into G5_ERR_MISMATCH): 64 roots on a Kronecker graph of scale
+    --c2-scale, harmonic-mean GTEPS with and without the codec, and the codec's
+    share of the search from a profile-mode pass."""
+    g = g5.Graph.kronecker(args.c2_scale)
+    roots = g5.select_roots(g, 64)
+    res = {"scale": args.c2_scale, "roots": len(roots), "codec": "s4-bp128-d4", "threshold": 64}
+    nedges = None
+    for name, codec in (("no_codec", g5.CODEC_NONE), ("codec", g5.CODEC_D4)):
+        b = g5.CudaBFS(g, codec=codec, codec_threshold=64)
+        if nedges is None:
+            nedges = []
+            for r in roots:
+                b.runBFS(int(r))
+                nedges.append(b.teps_edges())
+        ms, vals, words = [], 0, 0
+        for rep in range(2):
+            for r in roots:
+                code = b.run(int(r), None, None, stats=True)
+                if code != 0:
+                    raise g5.G5Error(code, "g5_bfs_run (codec in loop)")
+                if rep:
+                    ms.append(b.stats.device_ms)
+                    vals += b.stats.codec_values
+                    words += b.stats.codec_words
+        b.close()
+        res[name] = {"hmean_gteps": hmean([ne / (t * 1e-3) / 1e9 for ne, t in zip(nedges, ms)]),
+                     "mean_ms": statistics.mean(ms)}
+        if codec:
+            res[name]["values_through_codec"] = vals
+            res[name]["ratio_words_per_value"] = words / vals if vals else None
+    pb = g5.CudaBFS(g, codec=g5.CODEC_D4, codec_threshold=64, use_graph=False, profile=True)
+    tot = {}
+    for r in roots[:16]:
+        pb.run(int(r), None, None, stats=True)
+        for k, t in pb.profile_log():
+            tot[k] = tot.get(k, 0.0) + t
+    pb.close()
+    g.close()
+    allt = sum(tot.values())
+    res["codec_share_of_search"] = tot.get("codec", 0.0) / allt if allt else None
+    res["codec_ms_per_search"] = tot.get("codec", 0.0) / 16
+    res["round_trip"] = "device compare of every level's decoded queue with the encoded one (no mismatch)"
+    return res
 
 
 def bench_mixed(g5, torch, args):

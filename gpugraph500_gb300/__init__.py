@@ -92,6 +92,8 @@ SIGNATURES = {
     "g5_bfs_level_log": (_I, [_P, _P, _I, C.POINTER(_I)]),
     "g5_bfs_profile_log": (_I, [_P, _P, _P, _I, C.POINTER(_I)]),
     "g5_bfs_device_pred": (_I, [_P, C.POINTER(_P)]),
+    "g5_bfs_codec_capture": (_I, [_P, _P, _U64, _P, _I]),
+    "g5_bfs_codec_captured": (_I, [_P, C.POINTER(_I), C.POINTER(_I)]),
     "g5_bfs_teps_edges": (_I, [_P, C.POINTER(_I64)]),
     "g5_bfs_validate": (_I, [_P, _I64, C.POINTER(_I), C.POINTER(_I)]),
     "g5_batch_create": (_I, [_P, _I, C.POINTER(_P)]),
@@ -311,6 +313,20 @@ class CudaBFS:
         _check(lib().g5_bfs_profile_log(self._h, _ptr(kinds), _ptr(ms), 65536, C.byref(rows)),
                "g5_bfs_profile_log")
         return [(BfsStats.KERNELS[k], float(t)) for k, t in zip(kinds[: rows.value], ms[: rows.value])]
+
+    def codec_capture(self, buf_dev, cap_words: int, rec_dev, max_levels: int) -> None:
+        """Copy every level's in-loop codec stream of the following searches to
+        buf_dev (device, cap_words uint32) with (level, values, words, offset)
+        per level in rec_dev (device, 4 x max_levels uint64); buf_dev None
+        turns the copy off."""
+        _check(lib().g5_bfs_codec_capture(self._h, _ptr(buf_dev), int(cap_words), _ptr(rec_dev), int(max_levels)),
+               "g5_bfs_codec_capture")
+
+    def codec_captured(self) -> tuple[int, bool]:
+        """(levels recorded by the last search, whether any did not fit)."""
+        lv, ov = C.c_int(), C.c_int()
+        _check(lib().g5_bfs_codec_captured(self._h, C.byref(lv), C.byref(ov)), "g5_bfs_codec_captured")
+        return lv.value, bool(ov.value)
 
     def device_pred_ptr(self) -> int:
         p = C.c_void_p()

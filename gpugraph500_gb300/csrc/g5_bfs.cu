@@ -72,6 +72,19 @@ struct BfsState {
     uint64_t ulen;      // unvisited list length
 };
 
+// Where the in-loop codec's streams are copied when a caller asks for them
+// (g5_bfs_codec_capture); buf == nullptr leaves the copy off.
+struct CodecCapture {
+    uint32_t *buf;         // streams, each starting at a multiple of 4 words
+    uint64_t cap;          // words in buf
+    uint64_t *rec;         // per captured level: level, values, words, offset
+    uint32_t max_rec;
+    uint32_t count;        // levels captured by the current search
+    uint64_t off;          // next free word of buf
+    uint32_t overflow;     // a stream or record did not fit
+    uint32_t blocks_done;  // blocks of k_codec_capture finished
+};
+
 struct BfsArgs {
     const int64_t *row_off;
     const uint32_t *col;
@@ -112,6 +125,7 @@ struct BfsArgs {
     double alpha, beta;
     int codec;
     const uint64_t *codec_scal; // CS_* scalars of the codec work
+    CodecCapture *ccap;         // stream capture descriptor (codec searches), or null
     cudaGraphConditionalHandle cond;
     int use_cond;
 };
@@ -153,6 +167,11 @@ __global__ void k_init(BfsArgs a)
         a.log[0].nf = st->nf;
         a.log[0].mf = st->mf;
         a.log[0].examined = 0;
+        if (a.ccap) {
+            a.ccap->count = 0;
+            a.ccap->off = 0;
+            a.ccap->overflow = 0;
+        }
         if (s_ok) {
             const int64_t r = s_root;
             a.pred[r] = r;
@@ -899,6 +918,44 @@ __global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
     }
 }
 
+// Copies the level's encoded stream (scal[CS_WORDS] words) to the capture
+// buffer and records (level, values, words, offset); a no-op unless a caller
+// set a buffer.  All blocks read the same starting offset; the last block to
+// finish advances it.
+__global__ void __launch_bounds__(kBlock) k_codec_capture(CodecCapture *cc, const uint32_t *stream,
+                                                          const uint64_t *scal, const BfsState *st)
+{
+    if (!cc->buf) return;
+    const uint64_t words = scal[g5::CS_WORDS], off = cc->off;
+    const uint32_t count = cc->count;
+    const bool fits = count < cc->max_rec && off + words <= cc->cap;
+    if (fits)
+        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < words;
+             i += (uint64_t)gridDim.x * blockDim.x)
+            cc->buf[off + i] = stream[i];
+    __syncthreads();
+    __shared__ bool s_last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&cc->blocks_done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        if (fits) {
+            uint64_t *r = cc->rec + 4 * (uint64_t)count;
+            r[0] = (uint64_t)st->level;
+            r[1] = st->nf;
+            r[2] = words;
+            r[3] = off;
+            cc->off = off + ((words + 3) & ~(uint64_t)3);
+            cc->count = count + 1;
+        } else {
+            cc->overflow = 1;
+        }
+        cc->blocks_done = 0;
+    }
+}
+
 // ---- TEPS edge count and validation -----------------------------------------------
 
 __global__ void k_teps(const int64_t *__restrict__ pred, const uint32_t *__restrict__ end_deg, int64_t n,
@@ -1081,6 +1138,7 @@ struct g5_bfs {
     LevelRec *log = nullptr;
     int64_t *root_dev = nullptr;
     uint32_t *codec_stream = nullptr;
+    CodecCapture *ccap = nullptr;  // device descriptor (codec searches)
     g5::CodecWork cw;
     // host mirrors
     int64_t *h_root = nullptr;  // pinned
@@ -1126,6 +1184,7 @@ void enqueue_level(g5_bfs *b, const BfsArgs &a, cudaStream_t s, Prof *pf = nullp
     if (a.codec) {
         g5::codec_encode_launch(b->cw, b->queue, &b->st->nf, b->codec_stream, a.codec,
                                 b->cfg.codec_threshold, s);
+        k_codec_capture<<<g5::grid_for(1), kBlock, 0, s>>>(a.ccap, b->codec_stream, b->cw.scal, b->st);
         g5::decode_launch_acc(b->cw, b->codec_stream, b->cw.scal + g5::CS_WORDS, b->dqueue, (size_t)a.n,
                               a.codec, b->cfg.codec_threshold, &b->st->nf, b->queue, b->st->codec_acc, s);
     }
@@ -1212,6 +1271,8 @@ g5_status alloc_ws(g5_bfs *b)
         G5_CUDA(cudaMalloc(&b->dqueue, sizeof(uint32_t) * (size_t)n + 16));
         G5_CUDA(cudaMalloc(&b->codec_stream, sizeof(uint32_t) * g5::codec_bound((size_t)n)));
         G5_TRY(g5::codec_work_alloc(b->cw, (size_t)n));
+        G5_CUDA(cudaMalloc(&b->ccap, sizeof(CodecCapture)));
+        G5_CUDA(cudaMemset(b->ccap, 0, sizeof(CodecCapture)));
     }
     a.row_off = g->row_off;
     a.col = g->col;
@@ -1244,6 +1305,7 @@ g5_status alloc_ws(g5_bfs *b)
     a.beta = b->cfg.beta;
     a.codec = b->cfg.codec;
     a.codec_scal = b->cfg.codec ? b->cw.scal : nullptr;
+    a.ccap = b->ccap;
     a.use_cond = 0;
     return G5_OK;
 }
@@ -1298,6 +1360,7 @@ void free_ws(g5_bfs *b)
     cudaFree(b->log);
     cudaFree(b->root_dev);
     cudaFree(b->codec_stream);
+    cudaFree(b->ccap);
     cudaFreeHost(b->h_root);
     cudaFreeHost(b->h_st);
     cudaFreeHost(b->h_log);
@@ -1525,6 +1588,33 @@ g5_status g5_bfs_poll(g5_bfs *b, int *done, double *device_ms)
     const BfsState &hs = *b->h_st;
     if (hs.err & G5_DEVERR_LEVELS) return G5_ERR_TIMEOUT;
     if (hs.err) return G5_ERR_CAPACITY;
+    return G5_OK;
+}
+
+g5_status g5_bfs_codec_capture(g5_bfs *b, uint32_t *buf_dev, uint64_t cap_words, uint64_t *rec_dev,
+                               int max_levels)
+{
+    if (!b || !b->ccap) return G5_ERR_INVALID_ARG;
+    if (buf_dev && (!rec_dev || max_levels < 1 || !g5::is_device_ptr(buf_dev) || !g5::is_device_ptr(rec_dev)))
+        return G5_ERR_INVALID_ARG;
+    CodecCapture h = {};
+    h.buf = buf_dev;
+    h.cap = buf_dev ? cap_words : 0;
+    h.rec = buf_dev ? rec_dev : nullptr;
+    h.max_rec = buf_dev ? (uint32_t)max_levels : 0;
+    G5_CUDA(cudaStreamSynchronize(b->stream));
+    G5_CUDA(cudaMemcpy(b->ccap, &h, sizeof h, cudaMemcpyHostToDevice));
+    return G5_OK;
+}
+
+g5_status g5_bfs_codec_captured(g5_bfs *b, int *levels, int *overflow)
+{
+    if (!b || !b->ccap || !levels) return G5_ERR_INVALID_ARG;
+    CodecCapture h;
+    G5_CUDA(cudaStreamSynchronize(b->stream));
+    G5_CUDA(cudaMemcpy(&h, b->ccap, sizeof h, cudaMemcpyDeviceToHost));
+    *levels = (int)h.count;
+    if (overflow) *overflow = (int)h.overflow;
     return G5_OK;
 }
 

@@ -1487,8 +1487,12 @@ g5_status g5_codec_decode_batch(g5_codec *c, const uint32_t *in_dev, const uint6
 // host process whose device memory is owned by another allocator (a
 // framework's caching pool) with no headroom for cudaMalloc.  The encoder's
 // scratch (bit widths, payload offsets, scan partials, length scalars) lives
-// in the file-scope array below instead of a g5_codec workspace.  Every GPU
-// that loads the library holds these bytes until the process exits.
+// in the file-scope array below instead of a g5_codec workspace: 57,741
+// bytes (about 56 KiB, kNoAllocBytes) that every GPU which loads the library
+// holds until the process exits.  The array's device address is looked up
+// once per device and cached for the life of the process, so the entry point
+// must not be used again on a device after cudaDeviceReset in the same
+// process (the reset frees the module that holds the array).
 
 namespace {
 
@@ -1496,6 +1500,7 @@ constexpr size_t kNoAllocMaxValues = (size_t)1 << 20;          // values per cal
 constexpr size_t kNoAllocMb = kNoAllocMaxValues / 128 + 1;       // miniblocks
 constexpr size_t kNoAllocParts = 4096;                           // scan partials
 constexpr size_t kNoAllocBytes = 128 + 8 + kNoAllocMb * 4 + kNoAllocMb + kNoAllocParts * 4 + 256;
+static_assert(kNoAllocBytes == 57741, "the documented size of the scratch array");
 
 // In host code this name is only a host-side stand-in for the device array;
 // kernels receive the device address fetched with cudaGetSymbolAddress.

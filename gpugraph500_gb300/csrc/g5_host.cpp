@@ -33,7 +33,20 @@ PluginState &plugin()
     return p;
 }
 
-g5_status ensure(PluginState &p, size_t n, size_t words)
+// Drops every buffer, so that the next call after a failed growth
+// reallocates all of them instead of trusting stale capacities.
+void reset(PluginState &p)
+{
+    if (p.codec) g5_codec_destroy(p.codec);
+    cudaFree(p.d_in);
+    cudaFree(p.d_out);
+    cudaFreeHost(p.h_buf);
+    p.codec = nullptr;
+    p.d_in = p.d_out = p.h_buf = nullptr;
+    p.cap_n = p.cap_words = p.h_cap = 0;
+}
+
+g5_status grow(PluginState &p, size_t n, size_t words)
 {
     if (n > p.cap_n || !p.codec) {
         size_t c = std::max<size_t>(n, 1 << 16);
@@ -61,6 +74,13 @@ g5_status ensure(PluginState &p, size_t n, size_t words)
         p.h_cap = hb;
     }
     return G5_OK;
+}
+
+g5_status ensure(PluginState &p, size_t n, size_t words)
+{
+    const g5_status s = grow(p, n, words);
+    if (s != G5_OK) reset(p);
+    return s;
 }
 
 }  // namespace

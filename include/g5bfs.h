@@ -207,6 +207,22 @@ g5_status g5_bfs_level_log(g5_bfs *b, int64_t *out, int max_rows, int *rows);
  * g5_bfs_stats.kernel_ms) and its CUDA-event time in ms. */
 g5_status g5_bfs_profile_log(g5_bfs *b, int32_t *kinds, double *ms, int max_rows, int *rows);
 
+/* Capture of the in-loop codec's output (workspaces created with codec !=
+ * G5_CODEC_NONE), so that a caller can compare every level's stream with
+ * the one the reference encoder produces for that level's queue (the
+ * reference encodes each level's queue at cpu_2d/globalbfs.hh:853,873-877
+ * and cpu_2d/vreduce.hpp:426 through cpu_2d/compression/cpusimd.hh:70-118).
+ * From the next search on, each level's stream is also copied to buf_dev
+ * (device, cap_words words; each stream starts at a multiple of 4 words)
+ * and rec_dev (device, 4 x max_levels uint64) receives per level: the level
+ * index of the encoded queue, its length, the stream's words and its offset
+ * in buf_dev.  buf_dev = NULL turns the copy off.  g5_bfs_codec_captured
+ * gives the levels recorded by the last search and whether a stream or
+ * record did not fit (the rest were then dropped). */
+g5_status g5_bfs_codec_capture(g5_bfs *b, uint32_t *buf_dev, uint64_t cap_words, uint64_t *rec_dev,
+                               int max_levels);
+g5_status g5_bfs_codec_captured(g5_bfs *b, int *levels, int *overflow);
+
 /* Device pointer to the workspace's int64 parent array of the last search. */
 g5_status g5_bfs_device_pred(g5_bfs *b, const int64_t **pred);
 
@@ -387,15 +403,17 @@ g5_status g5_codec_decode_batch(g5_codec *c, const uint32_t *in_dev, const uint6
  * memory: a serving loop that must never block on or fragment the CUDA
  * allocator between requests, or a process whose device memory belongs to
  * another allocator (a framework's caching pool) with nothing left for
- * cudaMalloc.  It needs no g5_codec: its scratch is a fixed 64 KiB array in
- * the library's device image, held on every GPU that loads the library until
- * the process exits, and it calls no allocating function.  At most 1,048,576
- * values per call (more gives G5_ERR_CAPACITY).  The first call on a device
- * looks up that device's copy of the array (cudaGetSymbolAddress), so make
- * it before any stream capture.  All calls share the one array: calls that
- * overlap on the GPU (other streams, other host threads) race and must be
- * serialised by the caller.  This entry point has no counterpart in the
- * reference. */
+ * cudaMalloc.  It needs no g5_codec: its scratch is a fixed array of 57,741
+ * bytes (about 56 KiB) in the library's device image, held on every GPU that
+ * loads the library until the process exits, and it calls no allocating
+ * function.  At most 1,048,576 values per call (more gives
+ * G5_ERR_CAPACITY).  The first call on a device looks up that device's copy
+ * of the array (cudaGetSymbolAddress) and keeps the address for the life of
+ * the process, so make that call before any stream capture, and do not call
+ * this entry point on a device again after cudaDeviceReset in the same
+ * process.  All calls share the one array: calls that overlap on the GPU
+ * (other streams, other host threads) race and must be serialised by the
+ * caller.  This entry point has no counterpart in the reference. */
 g5_status g5_codec_encode_noalloc(const uint32_t *in_dev, size_t n, uint32_t *out_dev,
                                   size_t *out_words, int mode, void *stream);
 

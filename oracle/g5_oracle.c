@@ -7,8 +7,10 @@
  * this file is pinned against the reference compiled from its own sources
  * (oracle/_ref, built by oracle/Makefile) through tests/golden.
  */
+#define _POSIX_C_SOURCE 200809L
 #include "g5_oracle.h"
 
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -45,9 +47,16 @@ static void mat5_mul(const mat5_t *a, const mat5_t *b, mat5_t *r)
 /* The skip table holds A^(v * 256^k); the reference ships it precomputed
  * (cpu_2d/generator/mrg_transitions.c, produced by dump_mrg_powers); here it
  * is recomputed from the one-step matrix A. */
+static void skip_fill(void);
+static pthread_once_t g_skip_once = PTHREAD_ONCE_INIT;
+
 static void skip_init(void)
 {
-    if (g_skip_ready) return;
+    if (!g_skip_ready) pthread_once(&g_skip_once, skip_fill);
+}
+
+static void skip_fill(void)
+{
     mat5_t a;
     memset(&a, 0, sizeof a);
     a.m[0] = MRG_X; a.m[4] = MRG_Y;
@@ -72,13 +81,27 @@ void g5o_mrg_skip_matrix(int byte_index, int val, uint32_t out[25])
     memcpy(out, g_skip[byte_index][val].m, 25 * sizeof(uint32_t));
 }
 
+/* x mod 2^31-1 for any 64-bit x (2^31 = 1 mod p, so fold the high bits in
+ * twice); the same residue as the reference's `%`, computed without a
+ * division. */
+static inline uint32_t fold31(uint64_t x)
+{
+    x = (x & MRG_P) + (x >> 31);
+    x = (x & MRG_P) + (x >> 31);
+    return (uint32_t)(x >= MRG_P ? x - MRG_P : x);
+}
+
 static void mrg_apply(const mat5_t *m, mrg_t *s)
 {
     uint32_t o[5];
     for (int i = 0; i < 5; ++i) {
+        /* each product < 2^62 folds below 2^32, so five of them sum below 2^35 */
         uint64_t acc = 0;
-        for (int k = 0; k < 5; ++k) acc = (acc + (uint64_t)m->m[i * 5 + k] * s->z[k]) % MRG_P;
-        o[i] = (uint32_t)acc;
+        for (int k = 0; k < 5; ++k) {
+            const uint64_t p = (uint64_t)m->m[i * 5 + k] * s->z[k];
+            acc += (p & MRG_P) + (p >> 31);
+        }
+        o[i] = fold31(acc);
     }
     memcpy(s->z, o, sizeof o);
 }
@@ -94,7 +117,7 @@ static void mrg_skip(mrg_t *s, uint64_t hi, uint64_t mid, uint64_t lo)
 /* splittable_mrg.c:79-87,123-127 */
 static uint32_t mrg_next(mrg_t *s)
 {
-    uint32_t nz = (uint32_t)(((uint64_t)MRG_X * s->z[0] + (uint64_t)MRG_Y * s->z[4]) % MRG_P);
+    uint32_t nz = fold31((uint64_t)MRG_X * s->z[0] + (uint64_t)MRG_Y * s->z[4]);
     s->z[4] = s->z[3]; s->z[3] = s->z[2]; s->z[2] = s->z[1]; s->z[1] = s->z[0];
     s->z[0] = nz;
     return nz;
@@ -137,32 +160,55 @@ static int64_t scramble(int64_t v0, int lg, uint64_t val0, uint64_t val1)
     return (int64_t)v;
 }
 
-void g5o_generate_kronecker(int scale, uint64_t seed1, uint64_t seed2,
-                            int64_t start, int64_t end, int64_t *edges)
+typedef struct {
+    mrg_t seed;
+    uint64_t val0, val1;
+    int scale;
+} gen_ctx_t;
+
+/* utils.c:60-67 make_mrg_seed and graph_generator.c:168-178 scrambling values */
+static void gen_setup(gen_ctx_t *c, int scale, uint64_t seed1, uint64_t seed2)
 {
     skip_init();
-    /* utils.c:60-67 make_mrg_seed */
-    mrg_t seed;
-    seed.z[0] = (uint32_t)((seed1 & 0x3FFFFFFF) + 1);
-    seed.z[1] = (uint32_t)(((seed1 >> 30) & 0x3FFFFFFF) + 1);
-    seed.z[2] = (uint32_t)((seed2 & 0x3FFFFFFF) + 1);
-    seed.z[3] = (uint32_t)(((seed2 >> 30) & 0x3FFFFFFF) + 1);
-    seed.z[4] = (uint32_t)(((seed2 >> 60) << 4) + (seed1 >> 60) + 1);
-
-    /* graph_generator.c:168-178 scrambling values */
-    mrg_t t = seed;
+    c->scale = scale;
+    c->seed.z[0] = (uint32_t)((seed1 & 0x3FFFFFFF) + 1);
+    c->seed.z[1] = (uint32_t)(((seed1 >> 30) & 0x3FFFFFFF) + 1);
+    c->seed.z[2] = (uint32_t)((seed2 & 0x3FFFFFFF) + 1);
+    c->seed.z[3] = (uint32_t)(((seed2 >> 30) & 0x3FFFFFFF) + 1);
+    c->seed.z[4] = (uint32_t)(((seed2 >> 60) << 4) + (seed1 >> 60) + 1);
+    mrg_t t = c->seed;
     mrg_skip(&t, 50, 7, 0);
-    uint64_t val0 = mrg_next(&t);
-    val0 *= 0xFFFFFFFFull;
-    val0 += mrg_next(&t);
-    uint64_t val1 = mrg_next(&t);
-    val1 *= 0xFFFFFFFFull;
-    val1 += mrg_next(&t);
+    uint64_t v0 = mrg_next(&t);
+    v0 *= 0xFFFFFFFFull;
+    v0 += mrg_next(&t);
+    uint64_t v1 = mrg_next(&t);
+    v1 *= 0xFFFFFFFFull;
+    v1 += mrg_next(&t);
+    c->val0 = v0;
+    c->val1 = v1;
+}
 
-    const int64_t nverts = (int64_t)1 << scale;
+/* Edges [start, end).  Edge ei draws from the seed skipped by ei * 2^64
+ * steps (graph_generator.c:157-187 calls mrg_skip(&state, 0, ei, 0)).  The
+ * skip is a product of commuting powers of the step matrix, one per byte of
+ * ei, so the state after the bytes above the lowest is shared by 256
+ * consecutive edges and is computed once for them; each edge then applies
+ * only its lowest byte.  Same states, same edges as skipping every edge from
+ * the seed. */
+static void gen_range(const gen_ctx_t *c, int64_t start, int64_t end, int64_t *edges)
+{
+    const int64_t nverts = (int64_t)1 << c->scale;
+    mrg_t base = c->seed;
+    int64_t base_hi = -1;
     for (int64_t ei = start; ei < end; ++ei) {
-        mrg_t s = seed;
-        mrg_skip(&s, 0, (uint64_t)ei, 0);
+        if ((ei >> 8) != base_hi) {
+            base_hi = ei >> 8;
+            base = c->seed;
+            uint64_t hi = (uint64_t)ei >> 8;
+            for (int b = 9; hi; ++b, hi >>= 8) if (hi & 0xFF) mrg_apply(&g_skip[b][hi & 0xFF], &base);
+        }
+        mrg_t s = base;
+        if (ei & 0xFF) mrg_apply(&g_skip[8][ei & 0xFF], &s);
         /* graph_generator.c:122-151 make_one_edge with clip-and-flip */
         int64_t bs = 0, bt = 0, nv = nverts;
         while (nv > 1) {
@@ -173,9 +219,75 @@ void g5o_generate_kronecker(int scale, uint64_t seed1, uint64_t seed2,
             bs += nv * so;
             bt += nv * to;
         }
-        edges[2 * (ei - start)] = scramble(bs, scale, val0, val1);
-        edges[2 * (ei - start) + 1] = scramble(bt, scale, val0, val1);
+        edges[2 * (ei - start)] = scramble(bs, c->scale, c->val0, c->val1);
+        edges[2 * (ei - start) + 1] = scramble(bt, c->scale, c->val0, c->val1);
     }
+}
+
+void g5o_generate_kronecker(int scale, uint64_t seed1, uint64_t seed2,
+                            int64_t start, int64_t end, int64_t *edges)
+{
+    gen_ctx_t c;
+    gen_setup(&c, scale, seed1, seed2);
+    gen_range(&c, start, end, edges);
+}
+
+/* ---- host threads ---------------------------------------------------------- */
+
+typedef void (*par_fn)(void *ctx, int tid, int nthreads);
+typedef struct { par_fn fn; void *ctx; int tid, n; } par_arg_t;
+
+static void *par_tramp(void *p)
+{
+    par_arg_t *a = (par_arg_t *)p;
+    a->fn(a->ctx, a->tid, a->n);
+    return NULL;
+}
+
+/* Runs fn(ctx, t, T) for t = 0..T-1 on T host threads (the caller's is t = 0). */
+static void run_parallel(int T, par_fn fn, void *ctx)
+{
+    if (T < 1) T = 1;
+    if (T > 256) T = 256;
+    pthread_t th[256];
+    par_arg_t arg[256];
+    int started = 1;
+    for (int t = 1; t < T; ++t) {
+        arg[t].fn = fn; arg[t].ctx = ctx; arg[t].tid = t; arg[t].n = T;
+        if (pthread_create(&th[t], NULL, par_tramp, &arg[t]) != 0) break;
+        started = t + 1;
+    }
+    /* threads that could not be started: their shares run here */
+    for (int t = started; t < T; ++t) fn(ctx, t, T);
+    fn(ctx, 0, T);
+    for (int t = 1; t < started; ++t) pthread_join(th[t], NULL);
+}
+
+static void split(int64_t n, int tid, int T, int64_t *lo, int64_t *hi)
+{
+    *lo = n * tid / T;
+    *hi = n * (tid + 1) / T;
+}
+
+typedef struct { gen_ctx_t g; int64_t start, end; int64_t *edges; } gen_job_t;
+
+static void gen_worker(void *p, int tid, int T)
+{
+    gen_job_t *j = (gen_job_t *)p;
+    int64_t lo, hi;
+    split(j->end - j->start, tid, T, &lo, &hi);
+    gen_range(&j->g, j->start + lo, j->start + hi, j->edges + 2 * lo);
+}
+
+void g5o_generate_kronecker_mt(int scale, uint64_t seed1, uint64_t seed2,
+                               int64_t start, int64_t end, int64_t *edges, int threads)
+{
+    gen_job_t j;
+    gen_setup(&j.g, scale, seed1, seed2);
+    j.start = start;
+    j.end = end;
+    j.edges = edges;
+    run_parallel(threads, gen_worker, &j);
 }
 
 /* ======================================================================= */
@@ -217,6 +329,157 @@ int64_t g5o_build_csr(int64_t n, const int64_t *edges, int64_t nedges,
     }
     free(keys);
     return nnz;
+}
+
+/* The same CSR on host threads, by counting instead of one global sort:
+ * count each vertex's non-loop endpoints, scatter the neighbours into per-row
+ * buckets, then sort each row and drop duplicates.  Row v ends up as the
+ * ascending distinct neighbours of v other than v itself, which is exactly
+ * what the sort-based build above (the reference's order of work) leaves, so
+ * the arrays are identical; only the work is divided differently. */
+typedef struct {
+    int64_t n, nedges;
+    const int64_t *edges;
+    uint64_t *cur;   /* n + 1: bucket starts, then scatter cursors */
+    uint64_t *start; /* n + 1: bucket starts (kept) */
+    uint32_t *tmp;   /* 2 * nedges bucket entries */
+    int64_t *row_off;
+    uint32_t *col;
+    int phase;
+} csr_job_t;
+
+static int cmp_u32(const void *a, const void *b)
+{
+    uint32_t x = *(const uint32_t *)a, y = *(const uint32_t *)b;
+    return (x > y) - (x < y);
+}
+
+static void sort_u32(uint32_t *x, int64_t n)
+{
+    if (n <= 24) {
+        for (int64_t i = 1; i < n; ++i) {
+            uint32_t v = x[i];
+            int64_t j = i;
+            while (j > 0 && x[j - 1] > v) { x[j] = x[j - 1]; --j; }
+            x[j] = v;
+        }
+    } else {
+        qsort(x, (size_t)n, sizeof(uint32_t), cmp_u32);
+    }
+}
+
+static void csr_worker(void *p, int tid, int T)
+{
+    csr_job_t *j = (csr_job_t *)p;
+    int64_t lo, hi;
+    if (j->phase == 0) { /* endpoint counts */
+        split(j->nedges, tid, T, &lo, &hi);
+        for (int64_t i = lo; i < hi; ++i) {
+            int64_t a = j->edges[2 * i], b = j->edges[2 * i + 1];
+            if (a == b) continue;
+            __atomic_fetch_add(&j->cur[a + 1], 1, __ATOMIC_RELAXED);
+            __atomic_fetch_add(&j->cur[b + 1], 1, __ATOMIC_RELAXED);
+        }
+    } else if (j->phase == 1) { /* scatter */
+        split(j->nedges, tid, T, &lo, &hi);
+        for (int64_t i = lo; i < hi; ++i) {
+            int64_t a = j->edges[2 * i], b = j->edges[2 * i + 1];
+            if (a == b) continue;
+            j->tmp[__atomic_fetch_add(&j->cur[a], 1, __ATOMIC_RELAXED)] = (uint32_t)b;
+            j->tmp[__atomic_fetch_add(&j->cur[b], 1, __ATOMIC_RELAXED)] = (uint32_t)a;
+        }
+    } else if (j->phase == 2) { /* sort and dedup each row in place; count */
+        /* rows interleaved in blocks of 4096 so the heavy low rows spread */
+        for (int64_t b0 = (int64_t)tid * 4096; b0 < j->n; b0 += (int64_t)T * 4096) {
+            int64_t b1 = b0 + 4096 < j->n ? b0 + 4096 : j->n;
+            for (int64_t v = b0; v < b1; ++v) {
+                uint32_t *r = j->tmp + j->start[v];
+                int64_t len = (int64_t)(j->start[v + 1] - j->start[v]);
+                sort_u32(r, len);
+                int64_t k = 0;
+                for (int64_t i = 0; i < len; ++i)
+                    if (k == 0 || r[i] != r[k - 1]) r[k++] = r[i];
+                j->cur[v] = (uint64_t)k;
+            }
+        }
+    } else { /* copy the distinct entries to their final place */
+        for (int64_t b0 = (int64_t)tid * 4096; b0 < j->n; b0 += (int64_t)T * 4096) {
+            int64_t b1 = b0 + 4096 < j->n ? b0 + 4096 : j->n;
+            for (int64_t v = b0; v < b1; ++v)
+                memcpy(j->col + j->row_off[v], j->tmp + j->start[v],
+                       (size_t)(j->row_off[v + 1] - j->row_off[v]) * sizeof(uint32_t));
+        }
+    }
+}
+
+int64_t g5o_build_csr_mt(int64_t n, const int64_t *edges, int64_t nedges,
+                         int64_t *row_off, uint32_t *col, int threads)
+{
+    csr_job_t j;
+    j.n = n;
+    j.nedges = nedges;
+    j.edges = edges;
+    j.row_off = row_off;
+    j.col = col;
+    j.cur = (uint64_t *)calloc((size_t)n + 2, sizeof(uint64_t));
+    j.start = (uint64_t *)malloc(((size_t)n + 2) * sizeof(uint64_t));
+    j.tmp = NULL;
+    if (!j.cur || !j.start) { free(j.cur); free(j.start); return -1; }
+    j.phase = 0;
+    run_parallel(threads, csr_worker, &j);
+    for (int64_t v = 0; v < n; ++v) j.cur[v + 1] += j.cur[v];
+    memcpy(j.start, j.cur, ((size_t)n + 1) * sizeof(uint64_t));
+    j.tmp = (uint32_t *)malloc((size_t)(j.start[n] ? j.start[n] : 1) * sizeof(uint32_t));
+    if (!j.tmp) { free(j.cur); free(j.start); return -1; }
+    j.phase = 1;
+    run_parallel(threads, csr_worker, &j);
+    j.phase = 2;
+    run_parallel(threads, csr_worker, &j);
+    row_off[0] = 0;
+    for (int64_t v = 0; v < n; ++v) row_off[v + 1] = row_off[v] + (int64_t)j.cur[v];
+    j.phase = 3;
+    run_parallel(threads, csr_worker, &j);
+    free(j.tmp);
+    free(j.cur);
+    free(j.start);
+    return row_off[n];
+}
+
+/* Generated endpoints per vertex: end_deg[v] = occurrences of v in the edge
+ * list (a self loop counts twice), duplicates included. */
+typedef struct { const int64_t *edges; int64_t nedges; uint32_t *deg; } ecount_job_t;
+
+static void ecount_worker(void *p, int tid, int T)
+{
+    ecount_job_t *j = (ecount_job_t *)p;
+    int64_t lo, hi;
+    split(j->nedges, tid, T, &lo, &hi);
+    for (int64_t i = lo; i < hi; ++i) {
+        __atomic_fetch_add(&j->deg[j->edges[2 * i]], 1, __ATOMIC_RELAXED);
+        __atomic_fetch_add(&j->deg[j->edges[2 * i + 1]], 1, __ATOMIC_RELAXED);
+    }
+}
+
+void g5o_endpoint_counts(int64_t n, const int64_t *edges, int64_t nedges, uint32_t *end_deg,
+                         int threads)
+{
+    memset(end_deg, 0, (size_t)n * sizeof(uint32_t));
+    ecount_job_t j = {edges, nedges, end_deg};
+    run_parallel(threads, ecount_worker, &j);
+}
+
+/* validate.h:440-443,485: the TEPS edge count is the number of generated
+ * edge orientations (a, b), both orientations of every edge swept, whose
+ * first endpoint has a parent, halved.  Each vertex v is the first endpoint
+ * of end_deg[v] orientations, so the count is the sum of end_deg over the
+ * visited vertices, halved: the figure g5o_validate returns, without the
+ * edge sweep. */
+int64_t g5o_teps_edges(int64_t n, const uint32_t *end_deg, const int64_t *pred)
+{
+    uint64_t s = 0;
+    for (int64_t v = 0; v < n; ++v)
+        if (pred[v] != -1) s += end_deg[v];
+    return (int64_t)(s / 2);
 }
 
 /* ======================================================================= */

@@ -31,6 +31,11 @@ extern "C" {
 void g5o_generate_kronecker(int scale, uint64_t seed1, uint64_t seed2,
                             int64_t start, int64_t end, int64_t *edges);
 
+/* The same edges generated on `threads` host threads (edge ranges split
+ * evenly; every edge is independent of the others through the MRG skip). */
+void g5o_generate_kronecker_mt(int scale, uint64_t seed1, uint64_t seed2,
+                               int64_t start, int64_t end, int64_t *edges, int threads);
+
 /* Per-edge MRG state skip table entry: A^(val * 2^(8*byte_index)), 5x5 mod
  * 2^31-1, row-major.  Exposed so the GPU generator can be checked entry-wise. */
 void g5o_mrg_skip_matrix(int byte_index, int val, uint32_t out[25]);
@@ -43,6 +48,22 @@ void g5o_mrg_skip_matrix(int byte_index, int val, uint32_t out[25]);
  * must hold 2*nedges entries.  Returns nnz. */
 int64_t g5o_build_csr(int64_t n, const int64_t *edges, int64_t nedges,
                       int64_t *row_off, uint32_t *col);
+
+/* The same CSR (identical arrays) built on `threads` host threads by a
+ * counting sort into per-row buckets, each row then sorted and deduplicated.
+ * Returns nnz, or -1 if host memory runs out. */
+int64_t g5o_build_csr_mt(int64_t n, const int64_t *edges, int64_t nedges,
+                         int64_t *row_off, uint32_t *col, int threads);
+
+/* end_deg[v] = occurrences of v as an endpoint of the generated edges
+ * (duplicates included, a self loop twice). */
+void g5o_endpoint_counts(int64_t n, const int64_t *edges, int64_t nedges, uint32_t *end_deg,
+                         int threads);
+
+/* TEPS edge count of a search (validate.h:440-443,485) from the endpoint
+ * counts: the sum of end_deg over vertices with a parent, halved -- equal to
+ * the nedge_out of g5o_validate. */
+int64_t g5o_teps_edges(int64_t n, const uint32_t *end_deg, const int64_t *pred);
 
 /* ---- CPU BFS (the reference's CPUBFS_bin driven in runBFS order) ------- */
 

@@ -32,8 +32,14 @@ def lib():
         h = C.CDLL(LIB)
         P, I64, SZ = C.c_void_p, C.c_int64, C.c_size_t
         h.g5o_generate_kronecker.argtypes = [C.c_int, C.c_uint64, C.c_uint64, I64, I64, P]
+        h.g5o_generate_kronecker_mt.argtypes = [C.c_int, C.c_uint64, C.c_uint64, I64, I64, P, C.c_int]
         h.g5o_build_csr.argtypes = [I64, P, I64, P, P]
         h.g5o_build_csr.restype = I64
+        h.g5o_build_csr_mt.argtypes = [I64, P, I64, P, P, C.c_int]
+        h.g5o_build_csr_mt.restype = I64
+        h.g5o_endpoint_counts.argtypes = [I64, P, I64, P, C.c_int]
+        h.g5o_teps_edges.argtypes = [I64, P, P]
+        h.g5o_teps_edges.restype = I64
         h.g5o_bfs.argtypes = [I64, P, P, I64, P, P]
         h.g5o_validate.argtypes = [I64, P, I64, I64, P, C.POINTER(I64), P]
         h.g5o_codec_bound.argtypes = [SZ]
@@ -57,21 +63,57 @@ def _p(a):
     return None if a is None else a.ctypes.data
 
 
+def host_threads() -> int:
+    """Host threads the oracle may use (all the cores this process may run on)."""
+    try:
+        return max(1, len(os.sched_getaffinity(0)))
+    except (AttributeError, OSError):
+        return max(1, os.cpu_count() or 1)
+
+
 def kronecker(scale: int, seed1: int = 1, seed2: int = 2, edgefactor: int = 16,
-              start: int = 0, end: int | None = None) -> np.ndarray:
+              start: int = 0, end: int | None = None, threads: int = 0) -> np.ndarray:
+    """Edges [start, end); threads = 0 uses every host thread, 1 the serial path."""
     m = edgefactor << scale
     end = m if end is None else end
     out = np.empty((end - start, 2), np.int64)
-    lib().g5o_generate_kronecker(scale, seed1, seed2, start, end, _p(out))
+    t = threads or host_threads()
+    if t == 1:
+        lib().g5o_generate_kronecker(scale, seed1, seed2, start, end, _p(out))
+    else:
+        lib().g5o_generate_kronecker_mt(scale, seed1, seed2, start, end, _p(out), t)
     return out
 
 
-def build_csr(n: int, edges: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+def build_csr(n: int, edges: np.ndarray, threads: int = 1) -> tuple[np.ndarray, np.ndarray]:
+    """threads = 1: one global sort (the reference's order of work); more (0 =
+    every host thread): the counting build, identical arrays."""
     edges = np.ascontiguousarray(edges, dtype=np.int64)
     ro = np.empty(n + 1, np.int64)
     col = np.empty(max(2 * len(edges), 1), np.uint32)
-    nnz = lib().g5o_build_csr(n, _p(edges), len(edges), _p(ro), _p(col))
+    t = threads or host_threads()
+    if t == 1:
+        nnz = lib().g5o_build_csr(n, _p(edges), len(edges), _p(ro), _p(col))
+    else:
+        nnz = lib().g5o_build_csr_mt(n, _p(edges), len(edges), _p(ro), _p(col), t)
+        if nnz < 0:
+            raise MemoryError("g5o_build_csr_mt: host memory")
     return ro, col[:nnz].copy()
+
+
+def endpoint_counts(n: int, edges: np.ndarray, threads: int = 0) -> np.ndarray:
+    """Generated endpoints per vertex (duplicates included, self loops twice)."""
+    edges = np.ascontiguousarray(edges, dtype=np.int64)
+    out = np.empty(max(n, 1), np.uint32)
+    lib().g5o_endpoint_counts(n, _p(edges), len(edges), _p(out), threads or host_threads())
+    return out[:n]
+
+
+def teps_edges(end_deg: np.ndarray, pred: np.ndarray) -> int:
+    """TEPS edge count of a search from the endpoint counts (validate.h:440-443,485)."""
+    end_deg = np.ascontiguousarray(end_deg, dtype=np.uint32)
+    pred = np.ascontiguousarray(pred, dtype=np.int64)
+    return int(lib().g5o_teps_edges(len(pred), _p(end_deg), _p(pred)))
 
 
 def bfs(row_off: np.ndarray, col: np.ndarray, root: int) -> tuple[np.ndarray, np.ndarray]:

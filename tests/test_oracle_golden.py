@@ -160,3 +160,33 @@ def test_skip_table_is_powers_of_a():
     for _ in range(256):
         acc = acc.dot(m1) % 0x7FFFFFFF
     assert (acc == b1).all()
+
+
+def test_threaded_generator_and_csr_match_serial(golden_dir):
+    """The host-thread generator and counting CSR build give the reference's
+    arrays: the scale-16 digests, and element-wise equality with the serial
+    paths on an odd edge range and thread count."""
+    info = json.load(open(os.path.join(golden_dir, "kron_s16.json")))
+    e = orc.kronecker(16, threads=5)
+    assert sha(e) == info["edges_sha256"]
+    ro, col = orc.build_csr(info["n"], e, threads=3)
+    assert sha(ro) == info["row_off_sha256"] and sha(col) == info["col_u32_sha256"]
+    part = orc.kronecker(12, start=1000, end=23457, threads=7)
+    assert np.array_equal(part, orc.kronecker(12, start=1000, end=23457, threads=1))
+    e12 = orc.kronecker(12, threads=1)
+    a = orc.build_csr(1 << 12, e12, threads=1)
+    b = orc.build_csr(1 << 12, e12, threads=6)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_teps_edges_equal_validator_count(s10):
+    """The endpoint-count form of the TEPS edge count equals the validator's
+    edge sweep (validate.h:440-443,485) and the reference-run fixture."""
+    n = int(s10["n"])
+    ro, col, e = s10["row_off"], s10["col"], s10["edges"]
+    deg = orc.endpoint_counts(n, e)
+    assert int(deg.sum()) == 2 * len(e)
+    for i, root in enumerate(s10["roots"][:16]):
+        pred, _ = orc.bfs(ro, col, int(root))
+        ok, ne, _ = orc.validate(n, e, int(root), pred)
+        assert orc.teps_edges(deg, pred) == ne == int(s10["nedge"][i])
