@@ -59,11 +59,11 @@ def parse():
     ap.add_argument("--no-codec", action="store_true")
     ap.add_argument("--no-c2", action="store_true", help="skip the scale-22 search with the codec in the level loop")
     ap.add_argument("--c2-scale", type=int, default=22)
-    ap.add_argument("--big-scale", type=int, default=0,
+    ap.add_argument("--big-scale", type=int, default=28,
                     help="also compare plain and batched search on a second, larger graph (e.g. 28)")
     ap.add_argument("--serve-rates", default="1000,5000,20000")
-    ap.add_argument("--serve-modes", default="streams",
-                    help="comma list of server slot kinds to measure: streams, levels, auto")
+    ap.add_argument("--serve-modes", default="streams,cohorts",
+                    help="comma list of server slot kinds to measure: streams, levels, auto, cohorts")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--profile-batch", action="store_true",
                     help="only the batched search, host-driven with per-kernel CUDA events (for ncu)")
@@ -413,17 +413,27 @@ def main():
     # events around every launch) over the same roots
     kern = kernel_roofline(g5, g, roots, alpha, beta, peak, sizes)
 
-    # end to end through the C ABI with host (pinned) output buffers
-    pinned = torch.empty(g.n, dtype=torch.int64, pin_memory=True)
-    e2e = []
+    # end to end through the C ABI with host (pinned) output buffers: one
+    # g5_bfs_run_many call per step over the 64 roots (each search's 8n-byte
+    # parent array copied to the host while the next search runs), and the
+    # one-call-per-root form beside it
+    pinned = [torch.empty(g.n, dtype=torch.int64, pin_memory=True) for _ in range(2)]
+    outs = [pinned[i & 1] for i in range(nr)]
+    bfs.run_many(roots[:2], outs[:2])  # first use builds the second buffer's graph
+    e2e_steps = []
+    for _ in range(max(args.steps, 1)):
+        t1 = time.perf_counter()
+        bfs.run_many(roots, outs)
+        e2e_steps.append(sum(nedges) / (time.perf_counter() - t1) / 1e9)
+    e2e_value = hmean(e2e_steps)
+    e2e_seq = []
     for i, r in enumerate(roots):
         t1 = time.perf_counter()
-        code = bfs.run(int(r), pinned.data_ptr(), None, stats=False)
+        code = bfs.run(int(r), pinned[0].data_ptr(), None, stats=False)
         dt = time.perf_counter() - t1
         if code != 0:
             raise g5.G5Error(code, "g5_bfs_run")
-        e2e.append(nedges[i] / dt / 1e9)
-    e2e_value = hmean(e2e)
+        e2e_seq.append(nedges[i] / dt / 1e9)
 
     # batched form
     batched = None
@@ -434,6 +444,7 @@ def main():
             batched = {"error": str(e)}
 
     serve = mixed = codec = c2 = None
+    torch.cuda.empty_cache()  # the batched leg's output goes back to the device
     if rank == 0 and not args.no_c2:
         c2 = bench_c2(g5, args)
     if rank == 0 and not args.no_serve:
@@ -475,7 +486,10 @@ def main():
                        "tuner": tuned["grid"][:6] if tuned else None, "sizes": sizes or "defaults (256, 8)",
                        "sizes_tuner": tuned_sizes},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * nr,
-                    "d2h_bytes_per_step": 8 * g.n * nr},
+                    "d2h_bytes_per_step": 8 * g.n * nr,
+                    "how": "g5_bfs_run_many over the roots, int64 parents of every search copied to pinned host "
+                           "memory inside the timed call; GTEPS = Graph500 edges of all searches / wall time",
+                    "one_call_per_root_hmean": hmean(e2e_seq)},
             "gpu_launches": None,
             "roofline": {"bound": "hbm", "achieved": kern["achieved"], "peak": peak, "unit": "GB/s",
                          "frac": kern["achieved"] / peak, "traffic": kern["traffic"],
@@ -501,11 +515,14 @@ def main():
             line["batched_over_plain"] = batched["aggregate_gteps"] / value_rank if value_rank else None
         if serve:
             # headline: the lowest offered rate, from the serving mode with the lower p99 there
-            modes = [m for m in ("streams", "levels", "auto") if m in serve]
+            modes = [m for m in ("streams", "levels", "auto", "cohorts") if m in serve]
             best = min(modes, key=lambda m: serve[m]["rates"][0]["p99_ms"])
             line["p99_query_ms"] = serve[best]["rates"][0]["p99_ms"]
             line["p50_query_ms"] = serve[best]["rates"][0]["p50_ms"]
             line["serve_mode"] = best
+            # p99 and GTEPS of every mode at every offered rate
+            line["p99_query_ms_by_rate"] = {m: {str(int(r["rate_qps"])): {"p99_ms": r["p99_ms"], "gteps": r["gteps"]}
+                                                for r in serve[m]["rates"]} for m in modes}
         # per search: k_init + (k_td, k_bu, k_count, k_write) per level
         line["gpu_launches"] = sum(1 + 4 * rec[3] for rec in recs)
         print(json.dumps(line))
@@ -690,9 +707,10 @@ def bench_serve(g5, big, args):
         b.close()
         pools.append(roots)
         nedge.append(ne)
-    budget = 64 << 30
+    budget = 96 << 30
     res = {"graphs_scales": scales, "mem_budget_bytes": budget}
-    kinds = {"streams": g5.Server.STREAMS, "levels": g5.Server.LEVELS, "auto": g5.Server.AUTO}
+    kinds = {"streams": g5.Server.STREAMS, "levels": g5.Server.LEVELS, "auto": g5.Server.AUTO,
+             "cohorts": g5.Server.COHORTS}
     for name in args.serve_modes.split(","):
         sv = g5.Server(graphs, mem_budget=budget, keep_results=False, mode=kinds[name])
         res[name] = {"slots": sv.slots(), "rates": serve_rates(sv, args, pools, nedge, len(graphs))}
@@ -700,7 +718,9 @@ def bench_serve(g5, big, args):
     for gr in graphs[:-1]:
         gr.close()
     res["mode_note"] = ("streams: one-root workspaces for every graph; levels: root slots of the bit-sliced "
-                        "batch; auto: level slots for graphs of >= 2^25 vertices, workspaces for the rest")
+                        "batch; auto: level slots for graphs of >= 2^25 vertices, workspaces for the rest; "
+                        "cohorts: the queued queries of a graph of >= 2^21 vertices start together as one "
+                        "batched search whenever one of its two batch workspaces is free, workspaces for the rest")
     return res
 
 
@@ -936,18 +956,32 @@ def bench_codec(g5, torch, args):
                 bits = rng.random(1 << 24) < dens
                 srcs.append(torch.from_numpy(np.packbits(bits, bitorder="little").view(np.int64)).cuda())
             sets.append((torch.zeros(words64, dtype=torch.int64, device="cuda"), srcs))
+        # the calls are captured once in a CUDA graph and replayed, so the
+        # events time the kernels back to back, not the host's launch rate
+        reps = 24
+        st = torch.cuda.Stream()
+        st.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(st):
+            for k in range(len(sets)):
+                g5.bitmap_or(sets[k][0], sets[k][1], words64, stream=st.cuda_stream)
+        torch.cuda.current_stream().wait_stream(st)
+        cg = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(cg, stream=st):
+            for k in range(reps):
+                dst, srcs = sets[k % len(sets)]
+                g5.bitmap_or(dst, srcs, words64, stream=st.cuda_stream)
+        cg.replay()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
-        reps = 24
         e0.record()
-        for k in range(reps):
-            dst, srcs = sets[k % len(sets)]
-            g5.bitmap_or(dst, srcs, words64, stream=torch.cuda.current_stream().cuda_stream)
+        cg.replay()
         e1.record(); torch.cuda.synchronize()
         t = e0.elapsed_time(e1) * 1e-3 / reps
-        res[str(dens)] = {"GBps": 10 * words64 * 8 / t / 1e9, "us": t * 1e6}
+        res[str(dens)] = {"GBps": 10 * words64 * 8 / t / 1e9, "us": t * 1e6, "frac": 10 * words64 * 8 / t / 1e9 / peaks()[0]}
+        del cg
     return {"queues": len(queues), "values": vals, "max_queue": maxn, "codecs": stats,
             "bitmap_or_8x2^24": res, "bitmap_or_bytes_per_call": 10 * words64 * 8,
+            "bitmap_or_timing": "24 calls captured in one CUDA graph, CUDA events around its replay",
             "l2": "12 bitmap sets used round-robin (216 MB > L2)"}
 
 

@@ -92,6 +92,7 @@ SIGNATURES = {
     "g5_bfs_level_log": (_I, [_P, _P, _I, C.POINTER(_I)]),
     "g5_bfs_profile_log": (_I, [_P, _P, _P, _I, C.POINTER(_I)]),
     "g5_bfs_device_pred": (_I, [_P, C.POINTER(_P)]),
+    "g5_bfs_run_many": (_I, [_P, _P, _I, _P, _P]),
     "g5_bfs_codec_capture": (_I, [_P, _P, _U64, _P, _I]),
     "g5_bfs_codec_captured": (_I, [_P, C.POINTER(_I), C.POINTER(_I)]),
     "g5_bfs_teps_edges": (_I, [_P, C.POINTER(_I64)]),
@@ -102,6 +103,8 @@ SIGNATURES = {
     "g5_batch_profile": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _I, C.POINTER(_I)]),
     "g5_batch_run": (_I, [_P, _P, _P, _P, C.POINTER(C.c_double)]),
     "g5_batch_root_parents": (_I, [_P, C.c_int64, _I, _I, _P, _P]),
+    "g5_batch_launch": (_I, [_P, _P, _P, _P]),
+    "g5_batch_poll": (_I, [_P, _I, C.POINTER(_I), C.POINTER(C.c_double)]),
     "g5_batch_serve_begin": (_I, [_P, _P, _P]),
     "g5_batch_serve_step": (_I, [_P, _P, _P, _P, _I, _P, _P, C.POINTER(C.c_double)]),
     "g5_bfs_launch": (_I, [_P, _I64]),
@@ -288,6 +291,21 @@ class CudaBFS:
                                 C.byref(self.stats) if stats else None)
         self.last_root = int(root)
         return code
+
+    def run_many(self, roots, pred_outs=None, device_ms: bool = False):
+        """Searches every root, each search's parents copied to pred_outs[i]
+        (host or device buffers of n int64, None entries skip the copy) while
+        the next search runs.  Returns the per-search device ms if asked."""
+        roots = np.ascontiguousarray(roots, dtype=np.int64)
+        k = len(roots)
+        outs = None
+        if pred_outs is not None:
+            outs = (C.c_void_p * k)(*[_ptr(p) for p in pred_outs])
+        ms = np.zeros(max(k, 1), np.float64) if device_ms else None
+        _check(lib().g5_bfs_run_many(self._h, _ptr(roots), k, outs, _ptr(ms)), "g5_bfs_run_many")
+        if k:
+            self.last_root = int(roots[-1])
+        return ms[:k] if device_ms else None
 
     def runBFS(self, start: int) -> None:
         _check(self.run(start, self._pred, self._level), "g5_bfs_run")
@@ -536,6 +554,18 @@ class Batch:
                "g5_batch_run")
         return ms.value
 
+    def launch(self, roots: np.ndarray, nroots: Sequence[int], pred_out_dev) -> None:
+        """Asynchronous run: returns at once; poll() reports completion."""
+        roots = np.ascontiguousarray(roots, dtype=np.int64)
+        nr = np.ascontiguousarray(nroots, dtype=np.int32)
+        _check(lib().g5_batch_launch(self._h, _ptr(roots), _ptr(nr), _ptr(pred_out_dev)), "g5_batch_launch")
+
+    def poll(self, wait: bool = False):
+        """(done, device ms) of the last launch."""
+        done, ms = C.c_int(), C.c_double()
+        _check(lib().g5_batch_poll(self._h, int(wait), C.byref(done), C.byref(ms)), "g5_batch_poll")
+        return bool(done.value), ms.value
+
     def close(self) -> None:
         if self._h:
             lib().g5_batch_destroy(self._h)
@@ -551,7 +581,7 @@ class Batch:
 class Server:
     """Resident graphs answering single-root queries with continuous batching (g5_server)."""
 
-    STREAMS, LEVELS, AUTO = 0, 1, 2
+    STREAMS, LEVELS, AUTO, COHORTS = 0, 1, 2, 3
 
     def __init__(self, graphs: Sequence[Graph], mem_budget: int, keep_results: bool = True, mode: int = 0,
                  modes: Optional[Sequence[int]] = None):

@@ -1035,7 +1035,15 @@ g5_status build_relabel(g5_batch *b, const g5_graph *g, GraphDesc &d)
 
 extern "C" {
 
-g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
+}  // extern "C"
+
+namespace {
+
+// A batch workspace over `graphs`; with `share` (a workspace over the same
+// graphs), its degree-ordered graph copies are borrowed instead of built, so
+// several workspaces on one graph hold one copy (the owner must outlive the
+// borrowers).
+g5_status batch_create_impl(g5_graph *const *graphs, int ngraphs, const g5_batch *share, g5_batch **out)
 {
     if (!graphs || !out || ngraphs < 1 || ngraphs > kMaxGraphs) return G5_ERR_INVALID_ARG;
     *out = nullptr;
@@ -1074,6 +1082,18 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     cudaEventCreate(&b->ev0);
     cudaEventCreate(&b->ev1);
     for (int i = 0; i < ngraphs; ++i) {
+        if (share) {
+            if ((int)share->graphs.size() != ngraphs || share->graphs[i] != graphs[i]) return fail(G5_ERR_INVALID_ARG);
+            GraphDesc &d = b->hgd[i];
+            const GraphDesc &o = share->hgd[i];
+            d.row_off = o.row_off;
+            d.col = o.col;
+            d.orig = o.orig;
+            d.perm = o.perm;
+            d.ostart = o.ostart;
+            d.odeg = o.odeg;
+            continue;
+        }
         const g5_status rs = build_relabel(b, graphs[i], b->hgd[i]);
         if (rs != G5_OK) return fail(rs);
     }
@@ -1123,6 +1143,38 @@ g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
     *out = b;
     return G5_OK;
+}
+
+}  // namespace
+
+namespace g5 {
+
+g5_status batch_create_sharing(g5_batch *owner, g5_batch **out)
+{
+    if (!owner || !out) return G5_ERR_INVALID_ARG;
+    return batch_create_impl(owner->graphs.data(), (int)owner->graphs.size(), owner, out);
+}
+
+size_t batch_workspace_bytes(const g5_graph *g)
+{
+    // per vertex: 3 x 8 B words, degree, queue, edge offset, row base;
+    // per 256 edges a tile start; the fixed parts rounded up
+    return (size_t)g->n * (24 + 4 + 4 + 8 + 8) + (size_t)g->nnz / 64 + ((size_t)1 << 20);
+}
+
+size_t batch_copy_bytes(const g5_graph *g)
+{
+    // degree-ordered copy: two id maps, offsets, per-vertex row start and degree, columns
+    return (size_t)g->n * (4 + 4 + 8 + 8 + 4) + (size_t)g->nnz * 4 + ((size_t)1 << 20);
+}
+
+}  // namespace g5
+
+extern "C" {
+
+g5_status g5_batch_create(g5_graph *const *graphs, int ngraphs, g5_batch **out)
+{
+    return batch_create_impl(graphs, ngraphs, nullptr, out);
 }
 
 g5_status g5_batch_set_direction(g5_batch *b, double alpha, double beta)
@@ -1303,8 +1355,7 @@ g5_status g5_batch_destroy(g5_batch *b)
     return G5_OK;
 }
 
-g5_status g5_batch_run(g5_batch *b, const int64_t *roots_host, const int *nroots, uint32_t *pred_out_dev,
-                       double *device_ms)
+g5_status g5_batch_launch(g5_batch *b, const int64_t *roots_host, const int *nroots, uint32_t *pred_out_dev)
 {
     if (!b || !roots_host || !nroots || !pred_out_dev) return G5_ERR_INVALID_ARG;
     const int ng = (int)b->graphs.size();
@@ -1341,7 +1392,23 @@ g5_status g5_batch_run(g5_batch *b, const int64_t *roots_host, const int *nroots
     G5_CUDA(cudaGraphLaunch(b->exec, s));
     G5_CUDA(cudaEventRecord(b->ev1, s));
     G5_CUDA(cudaMemcpyAsync(b->h_st, b->st, sizeof(BState), cudaMemcpyDeviceToHost, s));
-    G5_CUDA(cudaStreamSynchronize(s));
+    return G5_OK;
+}
+
+g5_status g5_batch_poll(g5_batch *b, int wait, int *done, double *device_ms)
+{
+    if (!b || !done) return G5_ERR_INVALID_ARG;
+    if (wait) {
+        G5_CUDA(cudaStreamSynchronize(b->stream));
+    } else {
+        const cudaError_t e = cudaStreamQuery(b->stream);
+        if (e == cudaErrorNotReady) {
+            *done = 0;
+            return G5_OK;
+        }
+        G5_CUDA(e);
+    }
+    *done = 1;
     if (device_ms) {
         float ms = 0;
         cudaEventElapsedTime(&ms, b->ev0, b->ev1);
@@ -1350,6 +1417,14 @@ g5_status g5_batch_run(g5_batch *b, const int64_t *roots_host, const int *nroots
     if (b->h_st->err & 8u) return G5_ERR_TIMEOUT;
     if (b->h_st->err) return G5_ERR_CAPACITY;
     return G5_OK;
+}
+
+g5_status g5_batch_run(g5_batch *b, const int64_t *roots_host, const int *nroots, uint32_t *pred_out_dev,
+                       double *device_ms)
+{
+    G5_TRY(g5_batch_launch(b, roots_host, nroots, pred_out_dev));
+    int done = 0;
+    return g5_batch_poll(b, 1, &done, device_ms);
 }
 
 }  // extern "C"

@@ -1146,6 +1146,18 @@ struct g5_bfs {
     LevelRec *h_log = nullptr;  // pinned
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
+    // g5_bfs_run_many: a second parent buffer with its own graph, a copy
+    // stream, and events (created on first use)
+    int64_t *pred2 = nullptr;
+    cudaGraphExec_t exec2 = nullptr;
+    cudaGraph_t graph2 = nullptr;
+    cudaStream_t cstream = nullptr;
+    cudaEvent_t searched[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+    std::vector<cudaEvent_t> tev;   // start/end of each search of a run_many call
+    int64_t *h_roots = nullptr;     // pinned roots of a run_many call
+    uint32_t *h_errs = nullptr;     // pinned error flags, one per search
+    int roots_cap = 0;
+    int64_t *cur_pred = nullptr;    // parent array of the last search
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     Prof prof;
     bool ran = false;
@@ -1154,14 +1166,13 @@ struct g5_bfs {
 
 namespace {
 
-void enqueue_prologue(g5_bfs *b, cudaStream_t s)
+void enqueue_prologue(g5_bfs *b, const BfsArgs &a, cudaStream_t s)
 {
-    const BfsArgs &a = b->args;
     // vertices without edges can never be reached: they start out visited, so
     // bottom-up sweeps skip them (the root is set again by k_init)
     cudaMemcpyAsync(b->bitmaps, b->isolated, sizeof(uint32_t) * a.nwords, cudaMemcpyDeviceToDevice, s);
     cudaMemsetAsync(b->bitmaps + a.nwords, 0, sizeof(uint32_t) * 2 * a.nwords, s);
-    cudaMemsetAsync(b->pred, 0xFF, sizeof(int64_t) * (size_t)a.n, s);
+    cudaMemsetAsync(a.pred, 0xFF, sizeof(int64_t) * (size_t)a.n, s);
     if (b->level) cudaMemsetAsync(b->level, 0xFF, sizeof(int32_t) * (size_t)a.n, s);
     k_init<<<1, kBlock, 0, s>>>(a);
 }
@@ -1190,13 +1201,17 @@ void enqueue_level(g5_bfs *b, const BfsArgs &a, cudaStream_t s, Prof *pf = nullp
     }
 }
 
-g5_status build_graph(g5_bfs *b)
+// The search as one CUDA graph writing its parents to `pred`: the prologue,
+// then the level loop under a conditional while node.
+g5_status build_graph(g5_bfs *b, int64_t *pred, cudaGraphExec_t *exec_out, cudaGraph_t *graph_out)
 {
     cudaStream_t s = b->stream;
+    BfsArgs a = b->args;
+    a.pred = pred;
     // prologue captured as a child graph
     cudaGraph_t pro = nullptr;
     G5_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    enqueue_prologue(b, s);
+    enqueue_prologue(b, a, s);
     G5_CUDA(cudaStreamEndCapture(s, &pro));
     cudaGraph_t g = nullptr;
     G5_CUDA(cudaGraphCreate(&g, 0));
@@ -1213,15 +1228,14 @@ g5_status build_graph(g5_bfs *b)
     cudaGraphNode_t cnode;
     G5_CUDA(cudaGraphAddNode(&cnode, g, &pro_node, nullptr, 1, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    BfsArgs a = b->args;
     a.cond = h;
     a.use_cond = 1;
     G5_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     enqueue_level(b, a, s);
     cudaGraph_t body_out = nullptr;
     G5_CUDA(cudaStreamEndCapture(s, &body_out));
-    G5_CUDA(cudaGraphInstantiate(&b->exec, g, 0));
-    b->graph = g;
+    G5_CUDA(cudaGraphInstantiate(exec_out, g, 0));
+    *graph_out = g;
     return G5_OK;
 }
 
@@ -1338,6 +1352,17 @@ void free_ws(g5_bfs *b)
 {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->exec2) cudaGraphExecDestroy(b->exec2);
+    if (b->graph2) cudaGraphDestroy(b->graph2);
+    cudaFree(b->pred2);
+    if (b->cstream) cudaStreamDestroy(b->cstream);
+    for (int i = 0; i < 2; ++i) {
+        if (b->searched[i]) cudaEventDestroy(b->searched[i]);
+        if (b->copied[i]) cudaEventDestroy(b->copied[i]);
+    }
+    for (cudaEvent_t e : b->tev) cudaEventDestroy(e);
+    cudaFreeHost(b->h_roots);
+    cudaFreeHost(b->h_errs);
     cudaFree(b->deg);
     cudaFree(b->bitmaps);
     cudaFree(b->isolated);
@@ -1436,7 +1461,8 @@ g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
     k_degrees<<<g5::grid_for(8), kBlock, 0, b->stream>>>(g->row_off, g->col, g->n, b->deg, b->isolated,
                                                           b->heavy, b->ro32, b->first);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
-    if (b->cfg.use_graph && (st = build_graph(b)) != G5_OK) return fail(st);
+    if (b->cfg.use_graph && (st = build_graph(b, b->pred, &b->exec, &b->graph)) != G5_OK) return fail(st);
+    b->cur_pred = b->pred;
     *out = b;
     return G5_OK;
 }
@@ -1464,7 +1490,7 @@ g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_
         G5_CUDA(cudaGraphLaunch(b->exec, s));
     } else {
         b->prof.mark(KP_PRO, s);
-        enqueue_prologue(b, s);
+        enqueue_prologue(b, b->args, s);
         for (int L = 0; L < b->cfg.max_levels; ++L) {
             enqueue_level(b, b->args, s, &b->prof);
             G5_CUDA(cudaMemcpyAsync(b->h_st, b->st, sizeof(BfsState), cudaMemcpyDeviceToHost, s));
@@ -1484,6 +1510,7 @@ g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_
     G5_CUDA(cudaStreamSynchronize(s));
     b->ran = true;
     b->last_root = root;
+    b->cur_pred = b->pred;
     const BfsState &hs = *b->h_st;
     g5_status rc = G5_OK;
     if (hs.err & G5_DEVERR_LEVELS) rc = G5_ERR_TIMEOUT;
@@ -1567,6 +1594,7 @@ g5_status g5_bfs_launch(g5_bfs *b, int64_t root)
     G5_CUDA(cudaMemcpyAsync(b->h_st, b->st, sizeof(BfsState), cudaMemcpyDeviceToHost, s));
     b->ran = true;
     b->last_root = root;
+    b->cur_pred = b->pred;
     return G5_OK;
 }
 
@@ -1589,6 +1617,90 @@ g5_status g5_bfs_poll(g5_bfs *b, int *done, double *device_ms)
     if (hs.err & G5_DEVERR_LEVELS) return G5_ERR_TIMEOUT;
     if (hs.err) return G5_ERR_CAPACITY;
     return G5_OK;
+}
+
+g5_status g5_bfs_run_many(g5_bfs *b, const int64_t *roots, int k, int64_t *const *pred_out, double *device_ms)
+{
+    if (!b || k < 0 || (k && !roots)) return G5_ERR_INVALID_ARG;
+    for (int i = 0; i < k; ++i)
+        if (roots[i] < 0 || roots[i] >= b->g->n) return G5_ERR_INVALID_ARG;
+    if (!b->exec) {
+        // host-driven workspaces: one search after the other
+        for (int i = 0; i < k; ++i) {
+            g5_bfs_stats st;
+            G5_TRY(g5_bfs_run(b, roots[i], pred_out ? pred_out[i] : nullptr, nullptr, device_ms ? &st : nullptr));
+            if (device_ms) device_ms[i] = st.device_ms;
+        }
+        return G5_OK;
+    }
+    const int64_t n = b->g->n;
+    cudaStream_t s = b->stream;
+    // first use: the second parent buffer, its graph, the copy stream, events
+    if (!b->exec2) {
+        G5_CUDA(cudaMalloc(&b->pred2, sizeof(int64_t) * (size_t)n));
+        G5_TRY(build_graph(b, b->pred2, &b->exec2, &b->graph2));
+        G5_CUDA(cudaStreamCreateWithFlags(&b->cstream, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; ++i) {
+            G5_CUDA(cudaEventCreateWithFlags(&b->searched[i], cudaEventDisableTiming));
+            G5_CUDA(cudaEventCreateWithFlags(&b->copied[i], cudaEventDisableTiming));
+        }
+    }
+    if (k > b->roots_cap) {
+        cudaFreeHost(b->h_roots);
+        cudaFreeHost(b->h_errs);
+        b->h_roots = nullptr;
+        b->h_errs = nullptr;
+        b->roots_cap = 0;
+        G5_CUDA(cudaMallocHost(&b->h_roots, sizeof(int64_t) * (size_t)k));
+        G5_CUDA(cudaMallocHost(&b->h_errs, sizeof(uint32_t) * (size_t)k));
+        b->roots_cap = k;
+    }
+    while (device_ms && b->tev.size() < 2 * (size_t)k) {
+        cudaEvent_t e;
+        G5_CUDA(cudaEventCreate(&e));
+        b->tev.push_back(e);
+    }
+    int64_t *buf[2] = {b->pred, b->pred2};
+    cudaGraphExec_t ex[2] = {b->exec, b->exec2};
+    for (int i = 0; i < k; ++i) {
+        b->h_roots[i] = roots[i];
+        b->h_errs[i] = 0;
+    }
+    // search i writes buffer i % 2 on the search stream while the copy stream
+    // moves search i - 1's parents out; search i + 2 waits for that copy
+    for (int i = 0; i < k; ++i) {
+        const int slot = i & 1;
+        if (i >= 2) G5_CUDA(cudaStreamWaitEvent(s, b->copied[slot], 0));
+        G5_CUDA(cudaMemcpyAsync(b->root_dev, b->h_roots + i, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+        if (device_ms) G5_CUDA(cudaEventRecord(b->tev[2 * i], s));
+        G5_CUDA(cudaGraphLaunch(ex[slot], s));
+        if (device_ms) G5_CUDA(cudaEventRecord(b->tev[2 * i + 1], s));
+        G5_CUDA(cudaMemcpyAsync(b->h_errs + i, &b->st->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        G5_CUDA(cudaEventRecord(b->searched[slot], s));
+        G5_CUDA(cudaStreamWaitEvent(b->cstream, b->searched[slot], 0));
+        if (pred_out && pred_out[i])
+            G5_CUDA(cudaMemcpyAsync(pred_out[i], buf[slot], sizeof(int64_t) * (size_t)n, cudaMemcpyDefault,
+                                    b->cstream));
+        G5_CUDA(cudaEventRecord(b->copied[slot], b->cstream));
+    }
+    G5_CUDA(cudaStreamSynchronize(s));
+    G5_CUDA(cudaStreamSynchronize(b->cstream));
+    if (k) {
+        b->ran = true;
+        b->last_root = roots[k - 1];
+        b->cur_pred = buf[(k - 1) & 1];
+        G5_CUDA(cudaMemcpy(b->h_st, b->st, sizeof(BfsState), cudaMemcpyDeviceToHost));
+    }
+    g5_status rc = G5_OK;
+    for (int i = 0; i < k; ++i) {
+        if (device_ms) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, b->tev[2 * i], b->tev[2 * i + 1]);
+            device_ms[i] = ms;
+        }
+        if (rc == G5_OK && b->h_errs[i]) rc = (b->h_errs[i] & G5_DEVERR_LEVELS) ? G5_ERR_TIMEOUT : G5_ERR_CAPACITY;
+    }
+    return rc;
 }
 
 g5_status g5_bfs_codec_capture(g5_bfs *b, uint32_t *buf_dev, uint64_t cap_words, uint64_t *rec_dev,
@@ -1621,7 +1733,7 @@ g5_status g5_bfs_codec_captured(g5_bfs *b, int *levels, int *overflow)
 g5_status g5_bfs_device_pred(g5_bfs *b, const int64_t **pred)
 {
     if (!b || !pred) return G5_ERR_INVALID_ARG;
-    *pred = b->pred;
+    *pred = b->cur_pred;
     return G5_OK;
 }
 
@@ -1631,7 +1743,7 @@ g5_status g5_bfs_teps_edges(g5_bfs *b, int64_t *nedge)
     unsigned long long *d = nullptr;
     G5_CUDA(cudaMalloc(&d, sizeof *d));
     cudaMemsetAsync(d, 0, sizeof *d, b->stream);
-    k_teps<<<g5::grid_for(8), kBlock, 0, b->stream>>>(b->pred, b->g->end_deg, b->g->n, d);
+    k_teps<<<g5::grid_for(8), kBlock, 0, b->stream>>>(b->cur_pred, b->g->end_deg, b->g->n, d);
     unsigned long long h = 0;
     cudaMemcpyAsync(&h, d, sizeof h, cudaMemcpyDeviceToHost, b->stream);
     cudaError_t e = cudaStreamSynchronize(b->stream);
@@ -1666,7 +1778,8 @@ g5_status g5_bfs_validate(g5_bfs *b, int64_t root, int *valid, int *min_parent_o
         return G5_ERR_OOM;
     }
     cudaMemsetAsync(flags, 0, sizeof(unsigned) * 2, s);
-    k_val_init<<<g5::grid_for(8), kBlock, 0, s>>>(b->pred, n, root, anc[0], dist[0], flags);
+    const int64_t *pred = b->cur_pred;
+    k_val_init<<<g5::grid_for(8), kBlock, 0, s>>>(pred, n, root, anc[0], dist[0], flags);
     int cur = 0;
     for (int r = 0; r < 64; ++r) {
         cudaMemsetAsync(flags + 1, 0, sizeof(unsigned), s);
@@ -1683,8 +1796,8 @@ g5_status g5_bfs_validate(g5_bfs *b, int64_t root, int *valid, int *min_parent_o
     }
     if (rc == G5_OK) {
         int32_t *lev = dist[1 - cur];  // free after the last jump round
-        k_val_level<<<g5::grid_for(8), kBlock, 0, s>>>(b->pred, anc[cur], dist[cur], n, root, lev);
-        k_val_edges<<<g5::grid_for(8), kBlock, 0, s>>>(b->g->row_off, b->g->col, b->pred, lev, n, root, flags);
+        k_val_level<<<g5::grid_for(8), kBlock, 0, s>>>(pred, anc[cur], dist[cur], n, root, lev);
+        k_val_edges<<<g5::grid_for(8), kBlock, 0, s>>>(b->g->row_off, b->g->col, pred, lev, n, root, flags);
         unsigned f = 0;
         cudaMemcpyAsync(&f, flags, sizeof f, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) rc = G5_ERR_CUDA;

@@ -27,4 +27,12 @@ const uint32_t *mrg_skip_table_host();
 // Degree of vertex v of a device graph (reads two row offsets).
 g5_status graph_degree(const g5_graph *g, int64_t v, int64_t *deg);
 
+// A batch workspace over the same graphs as `owner` that borrows owner's
+// degree-ordered graph copies (owner must outlive it).
+g5_status batch_create_sharing(g5_batch *owner, g5_batch **out);
+// Device bytes of a batch workspace on one graph without its graph copy and
+// parent output, and of the degree-ordered copy alone.
+size_t batch_workspace_bytes(const g5_graph *g);
+size_t batch_copy_bytes(const g5_graph *g);
+
 }  // namespace g5

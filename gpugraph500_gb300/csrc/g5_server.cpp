@@ -16,6 +16,13 @@
 // automatic mode gives the large graphs, whose one-root searches would
 // saturate the GPU first, the level slots and the small ones the stream
 // workspaces, each kind with its own worker thread.
+// A third kind, cohorts, runs the batched kernel itself: a graph holds a few
+// batch workspaces (sharing one degree-ordered copy of the graph), and when a
+// workspace is free the queries queued for that graph -- up to the
+// workspace's root slots -- start together as one bit-sliced search.  Under
+// light load a cohort holds one or two queries and starts at once; under
+// heavy load queries gather while the workspaces are busy, so the cohorts
+// grow and one adjacency read serves up to 64 queries.
 // Admission is by device memory: a graph gets as many slots (at most 64) as
 // its share of the budget holds.
 #include <cuda_runtime.h>
@@ -41,11 +48,28 @@ using Clock = std::chrono::steady_clock;
 
 // Automatic mode: graphs of at least this many vertices get level slots.
 constexpr int64_t kAutoLevelsVertices = int64_t(1) << 25;
+// Cohort mode: graphs of at least this many vertices get cohorts, smaller
+// ones (whose one-root searches are short) stream workspaces.
+constexpr int64_t kCohortVertices = int64_t(1) << 21;
+constexpr int kCohortWorkspaces = 2;  // batch workspaces per cohort graph
+
+// One batch workspace of a cohort graph and the queries it runs.
+struct Cohort {
+    g5_batch *bt = nullptr;
+    uint32_t *pred = nullptr;      // vertex-major [v][nroots]
+    int cap = 0;                   // root slots
+    int nroots = 0;                // roots of the running or finished cohort
+    int state = 0;                 // 0 free, 1 running, 2 finished (results held)
+    int held = 0;                  // finished queries whose results are not yet released
+    std::vector<uint64_t> tickets; // ticket of each root
+    std::vector<int64_t> roots;
+};
 
 struct Query {
     int graph = 0;
     int64_t root = 0;
     int slot = -1;
+    int cohort = -1;  // cohort graphs: workspace index (slot = root index in it)
     int state = 0;  // 0 queued, 1 running, 2 done, 3 released
     Clock::time_point t_submit, t_start, t_done;
 };
@@ -59,6 +83,11 @@ struct g5_server {
     std::vector<int> levels_graphs;         // graphs in the batch, in batch order
     std::vector<int> bidx;                  // per graph: index in the batch (-1 if none)
     std::vector<std::vector<g5_bfs *>> ws;  // streams mode: workspaces per graph
+    std::vector<std::vector<Cohort>> cohorts;  // cohort graphs: batch workspaces
+    uint32_t *col_buf = nullptr;          // one root's uint32 parents, gathered for a result
+    std::vector<uint32_t> col_host;
+    std::mutex result_mu;                 // guards col_buf / col_host
+    cudaStream_t rstream = nullptr;       // result gathers
     g5_batch *bt = nullptr;
     uint32_t *pred = nullptr;             // parents of every slot (device)
     std::vector<uint64_t> pred_base;      // per graph
@@ -71,7 +100,7 @@ struct g5_server {
     int keep_results = 1;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::thread worker, worker2;          // stream-workspace and level-slot workers
+    std::thread worker, worker2, worker3; // stream-workspace, level-slot and cohort workers
     std::atomic<bool> stop{false};
     g5_status error = G5_OK;
     // statistics
@@ -245,6 +274,90 @@ void worker_loop(g5_server *sv)
     }
 }
 
+// Cohorts: when a batch workspace of a graph is free, the queries queued
+// for that graph (up to its root slots) start together as one batched
+// search; finished cohorts are polled and their queries completed.
+void worker_cohorts(g5_server *sv)
+{
+    cudaSetDevice(sv->graphs[0]->device);
+    const int ng = (int)sv->graphs.size();
+    int nrun = 0;
+    auto fail = [&](g5_status st) {
+        sv->error = st;
+        sv->stop.store(true);
+        sv->cv_done.notify_all();
+    };
+    while (!sv->stop.load()) {
+        {
+            std::unique_lock<std::mutex> lk(sv->mu);
+            for (int g = 0; g < ng; ++g) {
+                if (sv->kind[g] != G5_SERVE_COHORTS) continue;
+                for (int w = 0; w < (int)sv->cohorts[g].size() && !sv->queue[g].empty(); ++w) {
+                    Cohort &c = sv->cohorts[g][w];
+                    if (c.state != 0) continue;
+                    c.tickets.clear();
+                    c.roots.clear();
+                    const Clock::time_point now = Clock::now();
+                    while (!sv->queue[g].empty() && (int)c.tickets.size() < c.cap) {
+                        const uint64_t t = sv->queue[g].front();
+                        sv->queue[g].pop_front();
+                        Query &q = sv->queries[t];
+                        q.cohort = w;
+                        q.slot = (int)c.tickets.size();
+                        q.state = 1;
+                        q.t_start = now;
+                        c.tickets.push_back(t);
+                        c.roots.push_back(q.root);
+                    }
+                    c.nroots = (int)c.tickets.size();
+                    const g5_status st = g5_batch_launch(c.bt, c.roots.data(), &c.nroots, c.pred);
+                    if (st != G5_OK) return fail(st);
+                    c.state = 1;
+                    ++nrun;
+                }
+            }
+            if (nrun == 0) {
+                sv->cv_work.wait_for(lk, std::chrono::milliseconds(2));
+                continue;
+            }
+        }
+        bool any_done = false;
+        for (int g = 0; g < ng; ++g) {
+            if (sv->kind[g] != G5_SERVE_COHORTS) continue;
+            for (Cohort &c : sv->cohorts[g]) {
+                if (c.state != 1) continue;
+                int done = 0;
+                double ms = 0;
+                const g5_status st = g5_batch_poll(c.bt, 0, &done, &ms);
+                if (!done) continue;
+                --nrun;
+                any_done = true;
+                std::lock_guard<std::mutex> lk(sv->mu);
+                if (st != G5_OK) return fail(st);
+                sv->steps += 1;
+                sv->device_ms += ms;
+                const Clock::time_point now = Clock::now();
+                for (uint64_t t : c.tickets) {
+                    Query &q = sv->queries[t];
+                    q.state = sv->keep_results ? 2 : 3;
+                    q.t_done = now;
+                    sv->completed += 1;
+                }
+                // without kept results the workspace is free at once; with
+                // them it is held until every query's result is released
+                c.held = sv->keep_results ? c.nroots : 0;
+                c.state = c.held ? 2 : 0;
+            }
+        }
+        if (any_done) {
+            std::lock_guard<std::mutex> lk(sv->mu);
+            sv->cv_done.notify_all();
+        } else {
+            std::this_thread::sleep_for(std::chrono::microseconds(20));
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -255,7 +368,8 @@ g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t me
     if (!graphs || ngraphs < 1 || ngraphs > 64 || !out || !modes) return G5_ERR_INVALID_ARG;
     *out = nullptr;
     for (int i = 0; i < ngraphs; ++i)
-        if (!graphs[i] || (modes[i] != G5_SERVE_STREAMS && modes[i] != G5_SERVE_LEVELS)) return G5_ERR_INVALID_ARG;
+        if (!graphs[i] || (modes[i] != G5_SERVE_STREAMS && modes[i] != G5_SERVE_LEVELS && modes[i] != G5_SERVE_COHORTS))
+            return G5_ERR_INVALID_ARG;
     g5_server *sv = new g5_server();
     sv->keep_results = keep_results ? 1 : 0;
     sv->mode = G5_SERVE_AUTO;
@@ -266,8 +380,15 @@ g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t me
     auto fail = [&](g5_status st) {
         for (auto &v : sv->ws)
             for (g5_bfs *b : v) g5_bfs_destroy(b);
+        for (auto &v : sv->cohorts)  // borrowers first: the first workspace owns the graph copy
+            for (int w = (int)v.size() - 1; w >= 0; --w) {
+                if (v[w].bt) g5_batch_destroy(v[w].bt);
+                cudaFree(v[w].pred);
+            }
         if (sv->bt) g5_batch_destroy(sv->bt);
         cudaFree(sv->pred);
+        cudaFree(sv->col_buf);
+        if (sv->rstream) cudaStreamDestroy(sv->rstream);
         delete sv;
         return st;
     };
@@ -279,7 +400,14 @@ g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t me
     cfg.alpha = 40.0;
     cfg.beta = 200.0;
     const uint64_t share = mem_budget / (uint64_t)ngraphs;
+    // cohort graphs get what the other graphs leave of the budget, in
+    // proportion to their vertex counts (their parents take 4 bytes per
+    // vertex and root slot)
+    uint64_t cohort_n = 0, other_used = 0;
+    for (int i = 0; i < ngraphs; ++i)
+        if (sv->kind[i] == G5_SERVE_COHORTS) cohort_n += (uint64_t)graphs[i]->n;
     sv->ws.resize(ngraphs);
+    sv->cohorts.resize(ngraphs);
     sv->pred_base.assign(ngraphs, 0);
     sv->bidx.assign(ngraphs, -1);
     std::vector<g5_graph *> bgraphs;
@@ -288,10 +416,16 @@ g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t me
     for (int i = 0; i < ngraphs; ++i) {
         const uint64_t n = (uint64_t)graphs[i]->n;
         uint64_t k;
+        if (sv->kind[i] == G5_SERVE_COHORTS) {
+            sv->slots.push_back(0);  // set below, once the other graphs' use is known
+            sv->slot_query.emplace_back();
+            continue;
+        }
         if (sv->kind[i] == G5_SERVE_STREAMS) {
             const uint64_t per = 48ull * n + (uint64_t)graphs[i]->nnz / 64 + (1u << 20);
             k = std::min<uint64_t>(64, share / per);
             if (k == 0) return fail(G5_ERR_OOM);
+            other_used += k * per;
             for (uint64_t j = 0; j < k; ++j) {
                 g5_bfs *b = nullptr;
                 const g5_status st = g5_bfs_create(graphs[i], &cfg, &b);
@@ -301,6 +435,7 @@ g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t me
         } else {
             k = std::min<uint64_t>(64, share / (4ull * n));
             if (k == 0) return fail(G5_ERR_OOM);
+            other_used += k * 4ull * n;
             sv->bidx[i] = (int)bgraphs.size();
             sv->levels_graphs.push_back(i);
             bgraphs.push_back(graphs[i]);
@@ -311,6 +446,52 @@ g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t me
         sv->slots.push_back((int)k);
         sv->slot_query.emplace_back(k, 0);
     }
+    const uint64_t left = mem_budget > other_used ? mem_budget - other_used : 0;
+    uint64_t col_n = 0;
+    for (int i = 0; i < ngraphs; ++i) {
+        if (sv->kind[i] == G5_SERVE_LEVELS) col_n = std::max<uint64_t>(col_n, (uint64_t)graphs[i]->n);
+        if (sv->kind[i] != G5_SERVE_COHORTS) continue;
+        const uint64_t n = (uint64_t)graphs[i]->n;
+        col_n = std::max(col_n, n);
+        const uint64_t gshare = (uint64_t)((double)left * (double)n / (double)cohort_n);
+        const uint64_t fixed = g5::batch_copy_bytes(graphs[i]);
+        const uint64_t per_ws = g5::batch_workspace_bytes(graphs[i]);
+        // as many workspaces (up to kCohortWorkspaces) as leave room for at
+        // least 8 root slots each, and every workspace the slots that fit
+        int nw = kCohortWorkspaces;
+        uint64_t cap = 0;
+        for (; nw >= 1; --nw) {
+            const uint64_t need = fixed + (uint64_t)nw * per_ws;
+            cap = gshare > need ? (gshare - need) / ((uint64_t)nw * 4ull * n) : 0;
+            if (cap >= 8 || (nw == 1 && cap >= 1)) break;
+        }
+        if (nw < 1 || cap < 1) return fail(G5_ERR_OOM);
+        cap = std::min<uint64_t>(64, cap);
+        sv->slots[i] = (int)cap * nw;
+        for (int w = 0; w < nw; ++w) {
+            Cohort c;
+            c.cap = (int)cap;
+            const g5_status st = w == 0 ? g5_batch_create(&sv->graphs[i], 1, &c.bt)
+                                        : g5::batch_create_sharing(sv->cohorts[i][0].bt, &c.bt);
+            if (st == G5_OK && cudaMalloc(&c.pred, sizeof(uint32_t) * cap * n) != cudaSuccess) {
+                cudaGetLastError();
+                c.pred = nullptr;
+                sv->cohorts[i].push_back(c);
+                return fail(G5_ERR_OOM);
+            }
+            sv->cohorts[i].push_back(c);
+            if (st != G5_OK) return fail(st);
+        }
+    }
+    if (col_n) {
+        if (cudaMalloc(&sv->col_buf, sizeof(uint32_t) * col_n) != cudaSuccess) {
+            cudaGetLastError();
+            sv->col_buf = nullptr;
+            return fail(G5_ERR_OOM);
+        }
+        sv->col_host.resize(col_n);
+    }
+    if (cudaStreamCreateWithFlags(&sv->rstream, cudaStreamNonBlocking) != cudaSuccess) return fail(G5_ERR_CUDA);
     sv->retire.assign(ngraphs, 0);
     sv->queue.resize(ngraphs);
     if (!bgraphs.empty()) {
@@ -324,7 +505,13 @@ g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t me
         if (st != G5_OK) return fail(st);
         sv->worker2 = std::thread(worker_loop, sv);
     }
-    if (bgraphs.size() < (size_t)ngraphs) sv->worker = std::thread(worker_streams, sv);
+    bool any_streams = false, any_cohorts = false;
+    for (int i = 0; i < ngraphs; ++i) {
+        any_streams |= sv->kind[i] == G5_SERVE_STREAMS;
+        any_cohorts |= sv->kind[i] == G5_SERVE_COHORTS;
+    }
+    if (any_streams) sv->worker = std::thread(worker_streams, sv);
+    if (any_cohorts) sv->worker3 = std::thread(worker_cohorts, sv);
     *out = sv;
     return G5_OK;
 }
@@ -333,12 +520,15 @@ g5_status g5_server_create(g5_graph *const *graphs, int ngraphs, size_t mem_budg
                            g5_server **out)
 {
     if (!graphs || ngraphs < 1 || ngraphs > 64 || !out) return G5_ERR_INVALID_ARG;
-    if (mode != G5_SERVE_STREAMS && mode != G5_SERVE_LEVELS && mode != G5_SERVE_AUTO) return G5_ERR_INVALID_ARG;
+    if (mode != G5_SERVE_STREAMS && mode != G5_SERVE_LEVELS && mode != G5_SERVE_AUTO && mode != G5_SERVE_COHORTS)
+        return G5_ERR_INVALID_ARG;
     std::vector<int> modes(ngraphs, mode);
     for (int i = 0; i < ngraphs; ++i) {
         if (!graphs[i]) return G5_ERR_INVALID_ARG;
         if (mode == G5_SERVE_AUTO)
             modes[i] = graphs[i]->n >= kAutoLevelsVertices ? G5_SERVE_LEVELS : G5_SERVE_STREAMS;
+        if (mode == G5_SERVE_COHORTS)
+            modes[i] = graphs[i]->n >= kCohortVertices ? G5_SERVE_COHORTS : G5_SERVE_STREAMS;
     }
     g5_status st = g5_server_create_modes(graphs, ngraphs, mem_budget, keep_results, modes.data(), out);
     if (st == G5_OK) (*out)->mode = mode;
@@ -390,42 +580,62 @@ g5_status g5_server_result(g5_server *sv, uint64_t ticket, int64_t *pred_host, d
     // copies a finished query's parents (int64, -1 unvisited; may be NULL)
     // and frees its slot
     if (!sv) return G5_ERR_INVALID_ARG;
+    cudaSetDevice(sv->graphs[0]->device);
     std::unique_lock<std::mutex> lk(sv->mu);
     auto it = sv->queries.find(ticket);
     if (it == sv->queries.end() || it->second.state < 2) return G5_ERR_INVALID_ARG;
     Query q = it->second;
     if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(q.t_done - q.t_submit).count();
     if (queue_ms) *queue_ms = std::chrono::duration<double, std::milli>(q.t_start - q.t_submit).count();
+    g5_status rc = G5_OK;
     if (q.state == 2 && pred_host && sv->kind[q.graph] == G5_SERVE_STREAMS) {
         const int64_t n = sv->graphs[q.graph]->n;
         const int64_t *src = nullptr;
         g5_bfs_device_pred(sv->ws[q.graph][q.slot], &src);
         lk.unlock();
         if (cudaMemcpy(pred_host, src, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
-            return G5_ERR_CUDA;
+            rc = G5_ERR_CUDA;
         lk.lock();
     } else if (q.state == 2 && pred_host) {
+        // a column of a vertex-major uint32 array (level slots or a cohort):
+        // gathered into the server's column buffer, copied out and widened;
+        // the slot is not reused before it is released below
         const int64_t n = sv->graphs[q.graph]->n;
-        std::vector<uint32_t> tmp((size_t)n);
-        const uint32_t *src = sv->pred + sv->pred_base[q.graph];
-        const int R = sv->slots[q.graph];
+        const uint32_t *src;
+        int R;
+        if (sv->kind[q.graph] == G5_SERVE_COHORTS) {
+            const Cohort &c = sv->cohorts[q.graph][q.cohort];
+            src = c.pred;
+            R = c.nroots;
+        } else {
+            src = sv->pred + sv->pred_base[q.graph];
+            R = sv->slots[q.graph];
+        }
         lk.unlock();
-        // the slot is not reused before it is released below; its column is
-        // gathered out of the vertex-major array first
-        uint32_t *col = nullptr;
-        if (cudaMalloc(&col, sizeof(uint32_t) * (size_t)std::max<int64_t>(n, 1)) != cudaSuccess) return G5_ERR_OOM;
-        g5_status gs = g5_batch_root_parents(src, n, R, q.slot, col, nullptr);
-        if (gs == G5_OK && cudaMemcpy(tmp.data(), col, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
-            gs = G5_ERR_CUDA;
-        cudaFree(col);
-        if (gs != G5_OK) return gs;
-        for (int64_t v = 0; v < n; ++v) pred_host[v] = tmp[v] == 0xFFFFFFFFu ? -1 : (int64_t)tmp[v];
+        {
+            std::lock_guard<std::mutex> rl(sv->result_mu);
+            rc = g5_batch_root_parents(src, n, R, q.slot, sv->col_buf, sv->rstream);
+            if (rc == G5_OK &&
+                (cudaMemcpyAsync(sv->col_host.data(), sv->col_buf, sizeof(uint32_t) * (size_t)n,
+                                 cudaMemcpyDeviceToHost, sv->rstream) != cudaSuccess ||
+                 cudaStreamSynchronize(sv->rstream) != cudaSuccess))
+                rc = G5_ERR_CUDA;
+            if (rc == G5_OK)
+                for (int64_t v = 0; v < n; ++v)
+                    pred_host[v] = sv->col_host[v] == 0xFFFFFFFFu ? -1 : (int64_t)sv->col_host[v];
+        }
         lk.lock();
     }
+    if (rc != G5_OK) return rc;
     Query &qq = sv->queries[ticket];
     if (qq.state == 2) {
-        sv->slot_query[qq.graph][qq.slot] = 0;
-        if (sv->kind[qq.graph] == G5_SERVE_LEVELS) sv->retire[qq.graph] |= 1ull << qq.slot;
+        if (sv->kind[qq.graph] == G5_SERVE_COHORTS) {
+            Cohort &c = sv->cohorts[qq.graph][qq.cohort];
+            if (c.held > 0 && --c.held == 0) c.state = 0;
+        } else {
+            sv->slot_query[qq.graph][qq.slot] = 0;
+            if (sv->kind[qq.graph] == G5_SERVE_LEVELS) sv->retire[qq.graph] |= 1ull << qq.slot;
+        }
         qq.state = 3;
         sv->cv_work.notify_all();
     }
@@ -450,10 +660,18 @@ g5_status g5_server_destroy(g5_server *sv)
     sv->cv_work.notify_all();
     if (sv->worker.joinable()) sv->worker.join();
     if (sv->worker2.joinable()) sv->worker2.join();
+    if (sv->worker3.joinable()) sv->worker3.join();
     for (auto &v : sv->ws)
         for (g5_bfs *b : v) g5_bfs_destroy(b);
+    for (auto &v : sv->cohorts)  // borrowers first: the first workspace owns the graph copy
+        for (int w = (int)v.size() - 1; w >= 0; --w) {
+            if (v[w].bt) g5_batch_destroy(v[w].bt);
+            cudaFree(v[w].pred);
+        }
     if (sv->bt) g5_batch_destroy(sv->bt);
     cudaFree(sv->pred);
+    cudaFree(sv->col_buf);
+    if (sv->rstream) cudaStreamDestroy(sv->rstream);
     delete sv;
     return G5_OK;
 }

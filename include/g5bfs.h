@@ -198,6 +198,20 @@ g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_
 g5_status g5_bfs_launch(g5_bfs *b, int64_t root);
 g5_status g5_bfs_poll(g5_bfs *b, int *done, double *device_ms);
 
+/* Many searches in one call, pipelined: search i+1 runs while search i's
+ * parents travel to pred_out[i] (host or device, n entries each; a NULL
+ * array or entry skips that copy) on a second stream, with two parent
+ * buffers on the device.  The per-root loop of the reference driver
+ * (cpu_2d/main.cpp:419-462: runBFS then getPredecessor for each root) with
+ * the copy of one search hidden behind the next.  Host buffers should be
+ * pinned (cudaMallocHost) for the copies to overlap; pageable ones still
+ * give the same results.  device_ms (nullable, k entries) receives each
+ * search's device time.  Same parents as g5_bfs_run root by root; afterwards
+ * g5_bfs_device_pred, g5_bfs_teps_edges and g5_bfs_validate refer to the
+ * last root.  The first call allocates the second parent buffer (8n bytes)
+ * and builds its CUDA graph. */
+g5_status g5_bfs_run_many(g5_bfs *b, const int64_t *roots, int k, int64_t *const *pred_out, double *device_ms);
+
 /* Per-level record of the last search, 4 int64 per level: direction
  * (0 top-down, 1 bottom-up), frontier vertices, their adjacency entries, and
  * adjacency entries the expansion read.  *rows = levels written. */
@@ -278,6 +292,13 @@ g5_status g5_batch_set_direction(g5_batch *bt, double alpha, double beta);
 g5_status g5_batch_run(g5_batch *bt, const int64_t *roots_host, const int *nroots,
                        uint32_t *pred_out_dev, double *device_ms);
 
+/* Asynchronous form of g5_batch_run: launches the batch on the workspace's
+ * stream and returns.  g5_batch_poll sets *done once it has finished (wait =
+ * 1 blocks until then) and gives its device time and status.  The roots are
+ * copied during the launch; pred_out_dev must stay valid until done. */
+g5_status g5_batch_launch(g5_batch *bt, const int64_t *roots_host, const int *nroots, uint32_t *pred_out_dev);
+g5_status g5_batch_poll(g5_batch *bt, int wait, int *done, double *device_ms);
+
 /* One root's parents out of a vertex-major batch array of n vertices and
  * nroots parents per vertex: dst[v] = pred[v * nroots + r] (device arrays,
  * stream may be NULL). */
@@ -316,17 +337,28 @@ g5_status g5_batch_serve_step(g5_batch *bt, const int32_t *adm_graph, const int3
  *     slots (their one-root searches would saturate the GPU first: a slot
  *     there shares every adjacency read with up to 63 other queries), the
  *     smaller ones by stream workspaces; each kind has its own worker.
+ *   mode G5_SERVE_COHORTS: graphs of 2^21 vertices or more are served by
+ *     cohorts, the smaller ones by stream workspaces.  A cohort graph holds
+ *     up to two batch workspaces (g5_batch, sharing one degree-ordered copy
+ *     of the graph); whenever one is free, the graph's queued queries, up to
+ *     its root slots (at most 64), start together as one batched search, so
+ *     cohorts are small under light load and grow to share each adjacency
+ *     read among up to 64 queries under heavy load.  Cohort graphs get the
+ *     budget the other graphs leave, in proportion to their vertex counts
+ *     (4 bytes per vertex and root slot, plus the workspaces and the copy).
+ *     With keep_results a workspace is reused once every query of its
+ *     cohort has been released by g5_server_result.
  * Queries beyond the free slots wait in a FIFO per graph (memory-based
  * admission).  keep_results = 0 frees a slot as soon as its query finishes
  * (results are discarded). */
 typedef struct g5_server g5_server;
 
-enum { G5_SERVE_STREAMS = 0, G5_SERVE_LEVELS = 1, G5_SERVE_AUTO = 2 };
+enum { G5_SERVE_STREAMS = 0, G5_SERVE_LEVELS = 1, G5_SERVE_AUTO = 2, G5_SERVE_COHORTS = 3 };
 
 g5_status g5_server_create(g5_graph *const *graphs, int ngraphs, size_t mem_budget,
                            int keep_results, int mode, g5_server **out);
 /* As g5_server_create with the slot kind given per graph (modes[i] =
- * G5_SERVE_STREAMS or G5_SERVE_LEVELS). */
+ * G5_SERVE_STREAMS, G5_SERVE_LEVELS or G5_SERVE_COHORTS). */
 g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t mem_budget,
                                  int keep_results, const int *modes, g5_server **out);
 /* Slots per graph chosen by the admission rule. */

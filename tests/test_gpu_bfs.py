@@ -271,3 +271,44 @@ def test_bad_csr_rejected():
     col = np.array([1, 5], np.uint32)  # id out of range
     with pytest.raises(g5.G5Error):
         g5.Graph.from_csr(ro, col)
+
+
+def test_run_many_pipelined_copies_match_oracle():
+    """g5_bfs_run_many: every root's parents land in its own buffer (pageable
+    host, pinned host, device or skipped), equal to the oracle's, and the
+    workspace then refers to the last root."""
+    torch = pytest.importorskip("torch")
+    e = orc.kronecker(12)
+    ro, col = orc.build_csr(1 << 12, e)
+    n = 1 << 12
+    roots = orc.select_roots(ro, 7)
+    g = g5.Graph.from_csr(ro, col)
+    b = g5.CudaBFS(g)
+    outs = [np.full(n, 7, np.int64), torch.empty(n, dtype=torch.int64, pin_memory=True),
+            torch.empty(n, dtype=torch.int64, device="cuda"), None,
+            np.empty(n, np.int64), torch.empty(n, dtype=torch.int64, pin_memory=True), np.empty(n, np.int64)]
+    for rep in range(2):
+        ms = b.run_many(roots, outs, device_ms=True)
+        assert len(ms) == len(roots) and (ms > 0).all()
+        for r, o in zip(roots, outs):
+            if o is None:
+                continue
+            got = o.cpu().numpy() if hasattr(o, "cpu") else o
+            assert np.array_equal(got, orc.bfs(ro, col, int(r))[0]), (rep, int(r))
+    # the workspace's parent array, TEPS count and validation are the last root's
+    last = torch.as_tensor(_DevI64(b.device_pred_ptr(), n), device="cuda").cpu().numpy()
+    assert np.array_equal(last, orc.bfs(ro, col, int(roots[-1]))[0])
+    assert b.validate() == (True, True)
+    b.runBFS(int(roots[0]))  # single runs still work after run_many
+    assert np.array_equal(b.getPredecessor(), orc.bfs(ro, col, int(roots[0]))[0])
+    with pytest.raises(g5.G5Error):
+        b.run_many(np.array([0, n], np.int64), None)
+    b.close()
+    g.close()
+
+
+class _DevI64:
+    """A device int64 array handed to torch through __cuda_array_interface__."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<i8", "data": (ptr, False), "version": 3}

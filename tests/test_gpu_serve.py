@@ -36,7 +36,7 @@ def run_queries(sv, queries, concurrent):
     return out
 
 
-@pytest.mark.parametrize("mode", [0, 1, (1, 0, 1), 2])
+@pytest.mark.parametrize("mode", [0, 1, (1, 0, 1), 2, (3, 3, 3), (3, 0, 3)])
 def test_alone_and_mixed_agree_with_oracle(graphs, mode):
     csrs = [g.csr() for g in graphs]
     roots = [g5.select_roots(g, 20) for g in graphs]
@@ -44,7 +44,7 @@ def test_alone_and_mixed_agree_with_oracle(graphs, mode):
     queries = [(gi, int(r)) for gi in range(3) for r in roots[gi]]
     order = rng.permutation(len(queries))
     queries = [queries[i] for i in order]
-    if isinstance(mode, tuple):  # level slots for two graphs, stream workspaces for one
+    if isinstance(mode, tuple):  # a slot kind per graph (levels or cohorts beside stream workspaces)
         sv = g5.Server(graphs, mem_budget=1 << 30, modes=list(mode))
     else:
         sv = g5.Server(graphs, mem_budget=1 << 30, mode=mode)
@@ -103,4 +103,51 @@ def test_bad_queries(graphs):
         sv.submit(0, graphs[0].n)
     with pytest.raises(g5.G5Error):
         sv.submit(5, 0)
+    sv.close()
+
+
+def _cohort_bytes(g, slots, workspaces):
+    """Device bytes of a cohort graph: the shared degree-ordered copy, the
+    batch workspaces and 4 bytes per vertex and root slot."""
+    copy = 28 * g.n + 4 * g.nnz + (1 << 20)
+    ws = 48 * g.n + g.nnz // 64 + (1 << 20)
+    return copy + workspaces * ws + workspaces * slots * 4 * g.n
+
+
+def test_cohort_admission_and_reuse(graphs):
+    """A budget for one batch workspace of 3 root slots: queries beyond the
+    slots wait for the next cohort; results match the oracle; the workspace
+    is reused once its cohort's results are released."""
+    g = graphs[2]
+    sv = g5.Server([g], mem_budget=_cohort_bytes(g, 3, 1), modes=[g5.Server.COHORTS])
+    assert sv.slots() == [3]
+    ro, col = g.csr()
+    roots = g5.select_roots(g, 12)
+    for rep in range(2):
+        tickets = [sv.submit(0, int(r)) for r in roots]
+        queued = 0
+        for t, r in zip(tickets, roots):
+            assert sv.wait(t, 60.0)
+            pred, lat, q = sv.result(t)
+            queued += q > 0.0
+            want, _ = orc.bfs(ro, col, int(r))
+            assert np.array_equal(pred[:g.n], want), (rep, int(r))
+        assert queued >= 1
+    st = sv.stats()
+    assert st["completed"] == 24 and st["steps"] >= 4  # at most 3 queries per cohort
+    sv.close()
+
+
+def test_cohorts_without_kept_results(graphs):
+    """keep_results = False frees a cohort's workspace as soon as it ends."""
+    g = graphs[1]
+    sv = g5.Server([g], mem_budget=_cohort_bytes(g, 8, 2), keep_results=False, modes=[g5.Server.COHORTS])
+    assert sv.slots() == [16]
+    roots = g5.select_roots(g, 40)
+    tickets = [sv.submit(0, int(r)) for r in roots]
+    for t in tickets:
+        assert sv.wait(t, 60.0)
+        pred, lat, q = sv.result(t, with_pred=False)
+        assert lat >= q >= 0.0
+    assert sv.stats()["completed"] == 40
     sv.close()
