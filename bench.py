@@ -870,6 +870,88 @@ def bench_mixed(g5, torch, args):
             "single_graph_64_roots": single}
 
 
+CODEC_BUCKETS = ((0, 4096, "<=4K"), (4096, 1 << 18, "4K-256K"), (1 << 18, 1 << 20, "256K-1M"),
+                 (1 << 20, 1 << 40, ">1M"))
+
+
+def codec_device_times(g5, torch, c, queues, mode):
+    """Device time of one-stream encode and decode per queue, from CUDA events
+    around a captured CUDA graph of the asynchronous entry points (lengths in
+    device memory, nothing read back), so the time is the kernels' alone.  A
+    queue of 1M values or more is copied round-robin over enough buffers to
+    exceed L2 (256 MB), so its bytes come from HBM.  Per size bucket:
+    uncompressed GB/s (4n / t) and the roofline fraction of the algorithmic
+    bytes 4n + 4w (values and stream words, read once and written once)."""
+    peak = peaks()[0]
+    reps = 6
+    acc = {}
+    words_total = vals_total = 0
+    st = torch.cuda.Stream()
+    for q in queues:
+        n = len(q)
+        copies = 1 if n < (1 << 20) else min(64, -(-(256 << 20) // (4 * n)))
+        bound = g5.Codec.bound(n) + 64
+        ins = [torch.from_numpy(q.view(np.int32)).cuda() for _ in range(copies)]
+        streams = [torch.zeros(bound, dtype=torch.int32, device="cuda") for _ in range(copies)]
+        backs = [torch.zeros(n + 256, dtype=torch.int32, device="cuda") for _ in range(copies)]
+        lens = torch.tensor([n, 0, 0], dtype=torch.int64, device="cuda")  # n, words, decoded n
+        st.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(st):  # warm-up and the word count
+            for i in range(copies):
+                c.encode_async(ins[i], lens[0:1], streams[i], lens[1:2], mode, stream=st.cuda_stream)
+                c.decode_async(streams[i], lens[1:2], backs[i], n + 256, lens[2:3], mode, stream=st.cuda_stream)
+        torch.cuda.current_stream().wait_stream(st)
+        torch.cuda.synchronize()
+        if c.status() != 0 or int(lens[2]) != n or not torch.equal(backs[0][:n].cpu(), ins[0].cpu()):
+            raise RuntimeError(f"codec round trip failed on a queue of {n}")
+        w = int(lens[1])
+        t = {}
+        for kind in ("enc", "dec"):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=st):
+                for r in range(reps):
+                    i = r % copies
+                    if kind == "enc":
+                        c.encode_async(ins[i], lens[0:1], streams[i], lens[1:2], mode, stream=st.cuda_stream)
+                    else:
+                        c.decode_async(streams[i], lens[1:2], backs[i], n + 256, lens[2:3], mode, stream=st.cuda_stream)
+            g.replay()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            g.replay()
+            e1.record()
+            torch.cuda.synchronize()
+            t[kind] = e0.elapsed_time(e1) * 1e-3 / reps
+            del g
+        for lo, hi, name in CODEC_BUCKETS:
+            if lo < n <= hi or (lo == 0 and n <= hi):
+                b = acc.setdefault(name, {"queues": 0, "values": 0, "words": 0, "enc_s": 0.0, "dec_s": 0.0})
+                b["queues"] += 1
+                b["values"] += n
+                b["words"] += w
+                b["enc_s"] += t["enc"]
+                b["dec_s"] += t["dec"]
+                break
+        words_total += w
+        vals_total += n
+        del ins, streams, backs
+    out = {"ratio_words_per_value": words_total / vals_total if vals_total else None,
+           "timing": f"device time: {reps} calls captured in a CUDA graph, CUDA events around its replay; "
+                     f"queues of >= 1M values round-robin over buffers larger than L2", "buckets": {}}
+    for name, b in acc.items():
+        alg = 4 * (b["values"] + b["words"])
+        out["buckets"][name] = {
+            "queues": b["queues"], "values": b["values"],
+            "encode_GBps": 4 * b["values"] / b["enc_s"] / 1e9, "decode_GBps": 4 * b["values"] / b["dec_s"] / 1e9,
+            "encode_us_per_queue": 1e6 * b["enc_s"] / b["queues"], "decode_us_per_queue": 1e6 * b["dec_s"] / b["queues"],
+            "encode_frac": alg / b["enc_s"] / 1e9 / peak, "decode_frac": alg / b["dec_s"] / 1e9 / peak}
+    allv = sum(b["values"] for b in acc.values())
+    out["encode_GBps"] = 4 * allv / sum(b["enc_s"] for b in acc.values()) / 1e9
+    out["decode_GBps"] = 4 * allv / sum(b["dec_s"] for b in acc.values()) / 1e9
+    return out
+
+
 def bench_codec(g5, torch, args):
     """s4-bp128 encode/decode on every level queue of 16 roots of a scale-24
     graph, and the 8-way frontier-bitmap OR on 2^24-bit bitmaps."""
@@ -902,30 +984,16 @@ def bench_codec(g5, torch, args):
     bout = torch.empty(g5.Codec.batch_bound(in_off) + 64, dtype=torch.int32, device="cuda")
     bback = torch.empty(len(cat) + 256, dtype=torch.int32, device="cuda")
     for mode, name in ((g5.CODEC_D4, "d4"), (g5.CODEC_DM, "dm")):
-        enc_s = dec_s = 0.0
-        words = vals = 0
-        singles = []
-        for q in queues:
-            din[: len(q)] = torch.from_numpy(q.view(np.int32)).cuda()
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            w = c.encode(din, len(q), dout, mode, stream=torch.cuda.current_stream().cuda_stream)
-            e1.record(); torch.cuda.synchronize()
-            enc_s += e0.elapsed_time(e1) * 1e-3
-            e0.record()
-            m = c.decode(dout, w, back, maxn + 256, mode, stream=torch.cuda.current_stream().cuda_stream)
-            e1.record(); torch.cuda.synchronize()
-            dec_s += e0.elapsed_time(e1) * 1e-3
-            assert m == len(q)
-            singles.append(dout[:w].cpu().numpy())
-            words += w
-            vals += len(q)
-        stats[name] = {"encode_GBps": 4 * vals / enc_s / 1e9, "decode_GBps": 4 * vals / dec_s / 1e9,
-                       "ratio_words_per_value": words / vals}
+        stats[name] = codec_device_times(g5, torch, c, queues, mode)
         # the same queues in one batched call each way (host set-up included)
         cs = torch.cuda.current_stream().cuda_stream
         times = {"enc": [], "dec": []}
+        singles = []
+        for q in queues:
+            din[: len(q)] = torch.from_numpy(q.view(np.int32)).cuda()
+            w = c.encode(din, len(q), dout, mode)
+            singles.append(dout[:w].cpu().numpy())
+        vals = sum(len(q) for q in queues)
         for rep in range(3):
             torch.cuda.synchronize()
             t0 = time.perf_counter()

@@ -124,6 +124,9 @@ SIGNATURES = {
     "g5_codec_encode_batch": (_I, [_P, _P, _P, _I, _P, _P, _P, _U32, _I, _P]),
     "g5_codec_decode_batch": (_I, [_P, _P, _P, _P, _P, _I, _P, _P, _P, _U32, _I, _P]),
     "g5_codec_encode": (_I, [_P, _P, _SZ, _P, C.POINTER(_SZ), _I, _P]),
+    "g5_codec_encode_async": (_I, [_P, _P, _P, _P, _P, _I, _P]),
+    "g5_codec_decode_async": (_I, [_P, _P, _P, _P, _SZ, _P, _I, _P]),
+    "g5_codec_status": (_I, [_P]),
     "g5_codec_decode": (_I, [_P, _P, _SZ, _P, _SZ, C.POINTER(_SZ), _I, _P]),
     "g5_codec_encode_noalloc": (_I, [_P, _SZ, _P, C.POINTER(_SZ), _I, _P]),
     "g5_plugin_compress": (_I, [_P, _SZ, C.POINTER(_P), C.POINTER(_SZ), _U32, _I]),
@@ -399,6 +402,22 @@ class Codec:
         _check(lib().g5_codec_decode(self._h, _ptr(in_dev), words, _ptr(out_dev), out_cap, C.byref(n),
                                      mode, stream), "g5_codec_decode")
         return n.value
+
+    def encode_async(self, in_dev, n_dev, out_dev, out_words_dev, mode: int = CODEC_D4, stream=None) -> None:
+        """Enqueues an encode whose length is in device memory (n_dev); the
+        stream's words go to out_words_dev (device uint64).  Capturable."""
+        _check(lib().g5_codec_encode_async(self._h, _ptr(in_dev), _ptr(n_dev), _ptr(out_dev), _ptr(out_words_dev),
+                                           mode, stream), "g5_codec_encode_async")
+
+    def decode_async(self, in_dev, words_dev, out_dev, out_cap: int, out_n_dev, mode: int = CODEC_D4,
+                     stream=None) -> None:
+        """Enqueues a decode of a stream whose length is in device memory."""
+        _check(lib().g5_codec_decode_async(self._h, _ptr(in_dev), _ptr(words_dev), _ptr(out_dev), out_cap,
+                                           _ptr(out_n_dev), mode, stream), "g5_codec_decode_async")
+
+    def status(self) -> int:
+        """Status code of the last call on this workspace (synchronous)."""
+        return lib().g5_codec_status(self._h)
 
     @staticmethod
     def batch_bound(in_off: np.ndarray) -> int:

@@ -1515,6 +1515,7 @@ g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_
     g5_status rc = G5_OK;
     if (hs.err & G5_DEVERR_LEVELS) rc = G5_ERR_TIMEOUT;
     else if (hs.err) rc = G5_ERR_CAPACITY;
+    else if (b->cfg.codec && (cscal[g5::CS_ERR] & G5_DEVERR_WAIT)) rc = G5_ERR_TIMEOUT;
     else if (b->cfg.codec && (cscal[g5::CS_ERR] & G5_DEVERR_MISMATCH)) rc = G5_ERR_MISMATCH;
     else if (b->cfg.codec && cscal[g5::CS_ERR]) rc = G5_ERR_CORRUPT_STREAM;
     if (stats) {

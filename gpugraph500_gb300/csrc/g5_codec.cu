@@ -20,13 +20,19 @@
 //   VariableByte<true> (variablebyte.h:100-161): delta from 0, 7-bit groups
 //   little-endian, high bit on the last byte, zero-padded to a word.
 //
-// GPU design: every miniblock is independent for encoding (its deltas only
-// need the input), so one warp packs one miniblock; offsets come from a
-// prefix sum of the bit widths.  Decoding needs each group's position, which
-// the stream only gives as a chain (each header says how long its group is):
-// the chain is resolved with binary lifting over all 16-byte positions
-// (group starts are always 16-byte aligned), then one warp unpacks each
-// miniblock and a prefix sum over miniblocks restores absolute values.
+// GPU design, one stream per call: every miniblock is independent for
+// encoding (its deltas only need the input), so one warp packs one
+// miniblock, a block one group, and the group's place in the stream is the
+// prefix of the groups before it, found in the same pass by a decoupled
+// look-back (one launch).  Decoding needs each group's position, which the
+// stream only gives as a chain (each header says how long its group is): a
+// first pass follows the chain inside chunks of the stream from every
+// possible entry and carries the real entries across chunks by look-back;
+// a second pass unpacks one group per block, with the running values
+// carried across groups by look-back (two launches).  The many-streams
+// calls (one launch set for k queues) resolve the chains by binary lifting
+// over all 16-byte positions (group starts are always 16-byte aligned) and
+// use separate scan passes.
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
@@ -47,7 +53,6 @@ constexpr int kTailMaxBytes = 4096;  // largest VariableByte tail decoded
 // extra scalar slots (beyond CodecScalar)
 enum { CS_NMB = 5, CS_RAW = 6, CS_NG = 7 };
 // the scalar block holds CS_COUNT entries; decode uses a few more
-enum { CS_NV = 8, CS_LIFT = 9, CS_TOTAL = 12 };
 
 __device__ __forceinline__ uint32_t bits_of(uint32_t v) { return v ? 32u - __clz(v) : 0u; }
 
@@ -58,11 +63,6 @@ struct AddU32 {
     __device__ static T id() { return 0u; }
     __device__ static T op(T a, T b) { return a + b; }
     __device__ static T shfl_up(T v, int o) { return __shfl_up_sync(0xFFFFFFFFu, v, o); }
-};
-
-struct VecFlag {
-    uint4 v;
-    uint32_t f;
 };
 
 struct ResetAdd {
@@ -205,17 +205,6 @@ __global__ void __launch_bounds__(kB) k_scan_down(const typename Op::T *in, type
 
 // ---- encoder ---------------------------------------------------------------------------
 
-__global__ void k_enc_prep(const uint64_t *n_dev, uint64_t raw_thr, uint64_t *scal)
-{
-    if (threadIdx.x) return;
-    const uint64_t n = *n_dev;
-    scal[CS_N] = n;
-    scal[CS_N1] = n / 128 * 128;
-    scal[CS_NMB] = n / 128;
-    scal[CS_RAW] = (raw_thr && n <= raw_thr) ? 1 : 0;
-    scal[CS_ERR] = 0;
-}
-
 // Lane j of a warp loads vector j of miniblock k and its predecessor vector.
 __device__ __forceinline__ void load_vectors(const uint32_t *in, uint64_t k, uint4 &cur, uint4 &prev)
 {
@@ -238,247 +227,12 @@ __device__ __forceinline__ uint4 deltas(uint4 cur, uint4 prev, int mode)
     return make_uint4(cur.x - prev.x, cur.y - prev.y, cur.z - prev.z, cur.w - prev.w);
 }
 
-__global__ void __launch_bounds__(kB) k_enc_bits(const uint32_t *in, uint64_t *scal, uint8_t *mb_bits,
-                                                 uint32_t *mb_len, int mode)
-{
-    if (scal[CS_RAW]) return;
-    const uint64_t nmb = scal[CS_NMB];
-    const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
-    const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
-    for (uint64_t k = gw; k < nmb; k += nw) {
-        uint4 cur, prev;
-        load_vectors(in, k, cur, prev);
-        uint4 d = deltas(cur, prev, mode);
-        uint32_t acc = d.x | d.y | d.z | d.w;
-#pragma unroll
-        for (int o = 16; o; o >>= 1) acc |= __shfl_xor_sync(0xFFFFFFFFu, acc, o);
-        if (g5_lane() == 0) {
-            const uint32_t b = bits_of(acc);
-            mb_bits[k] = (uint8_t)b;
-            mb_len[k] = 4 * b;
-        }
-    }
-}
-
 __device__ __forceinline__ uint32_t comp(const uint4 &v, int l)
 {
     return l == 0 ? v.x : l == 1 ? v.y : l == 2 ? v.z : v.w;
 }
 
-__global__ void __launch_bounds__(kB) k_enc_pack(const uint32_t *in, uint64_t *scal, const uint8_t *mb_bits,
-                                                 const uint32_t *mb_off, uint32_t *out, int mode)
-{
-    __shared__ uint4 s_d[kB / 32][32];
-    if (scal[CS_RAW]) {
-        const uint64_t n = scal[CS_N];
-        for (uint64_t i = (uint64_t)blockIdx.x * kB + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kB)
-            out[i] = in[i];
-        if (blockIdx.x == 0 && threadIdx.x == 0) scal[CS_WORDS] = n;
-        return;
-    }
-    const uint64_t nmb = scal[CS_NMB];
-    const int lane = g5_lane(), wib = threadIdx.x >> 5;
-    const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
-    const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
-    for (uint64_t k = gw; k < nmb; k += nw) {
-        const uint32_t b = mb_bits[k];
-        const uint64_t off = 4 + 4 * (k / 16 + 1) + (uint64_t)mb_off[k];
-        if ((k & 15) == 0 && lane < 4) {
-            uint32_t h = 0;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const uint64_t kk = k + 4 * lane + q;
-                const uint32_t bb = kk < nmb ? mb_bits[kk] : 0u;
-                h |= bb << (24 - 8 * q);
-            }
-            out[4 + 4 * (k / 16) + (uint64_t)(k == 0 ? 0 : mb_off[k]) + lane] = h;
-        }
-        uint4 cur, prev;
-        load_vectors(in, k, cur, prev);
-        if (b == 32) {
-            reinterpret_cast<uint4 *>(out + off)[lane] = cur;
-            continue;
-        }
-        if (b == 0) continue;
-        s_d[wib][lane] = deltas(cur, prev, mode);
-        __syncwarp();
-        for (uint32_t idx = lane; idx < 4 * b; idx += 32) {
-            const uint32_t w = idx >> 2, l = idx & 3;
-            const uint32_t bit0 = 32 * w;
-            const uint32_t j0 = bit0 / b, j1 = (bit0 + 31) / b;
-            uint32_t word = 0;
-            for (uint32_t j = j0; j <= j1 && j < 32; ++j) {
-                const uint32_t d = comp(s_d[wib][j], l);
-                const int sh = (int)(j * b) - (int)bit0;
-                word |= sh >= 0 ? (d << sh) : (d >> (-sh));
-            }
-            out[off + idx] = word;
-        }
-        __syncwarp();
-    }
-}
-
-// Header words and the VariableByte tail; total words -> scal[CS_WORDS].
-__global__ void k_enc_tail(const uint32_t *in, uint64_t *scal, const uint32_t *payload_total, uint32_t *out)
-{
-    __shared__ uint32_t s_val[128];
-    __shared__ uint32_t s_bytes[(128 * 5 + 3) / 4 + 1];
-    if (scal[CS_RAW]) return;
-    const uint64_t n = scal[CS_N], n1 = scal[CS_N1], nmb = scal[CS_NMB];
-    const uint64_t ngroups = (nmb + 15) / 16;
-    const uint64_t blkend = 4 + 4 * ngroups + (nmb ? (uint64_t)*payload_total : 0);
-    const int lane = threadIdx.x;
-    const uint32_t nt = (uint32_t)(n - n1);
-    for (uint32_t i = lane; i < nt; i += 32) s_val[i] = in[n1 + i];
-    for (uint32_t i = lane; i < sizeof(s_bytes) / 4; i += 32) s_bytes[i] = 0;
-    __syncwarp();
-    if (lane == 0) {
-        out[0] = (uint32_t)n1;
-        out[1] = kCookie;
-        out[2] = kCookie;
-        out[3] = kCookie;
-        uint8_t *bb = reinterpret_cast<uint8_t *>(s_bytes);
-        uint32_t p = 0, prev = 0;
-        for (uint32_t i = 0; i < nt; ++i) {
-            uint32_t v = s_val[i] - prev;
-            prev = s_val[i];
-            while (v >= 128u) {
-                bb[p++] = (uint8_t)(v & 127u);
-                v >>= 7;
-            }
-            bb[p++] = (uint8_t)(v | 128u);
-        }
-        const uint32_t tw = (p + 3) / 4;
-        s_val[0] = tw;
-        scal[CS_WORDS] = blkend + tw;
-        scal[CS_BLKEND] = blkend;
-    }
-    __syncwarp();
-    const uint32_t tw = s_val[0];
-    for (uint32_t i = lane; i < tw; i += 32) out[blkend + i] = s_bytes[i];
-}
-
 // ---- decoder ---------------------------------------------------------------------------
-
-__global__ void k_dec_prep(const uint32_t *in, const uint64_t *words_dev, uint64_t cap, uint64_t raw_thr,
-                           const uint64_t *n_expect, uint64_t *scal, int lift_levels, uint64_t max_vec,
-                           uint64_t max_mb)
-{
-    if (threadIdx.x) return;
-    const uint64_t words = *words_dev;
-    scal[CS_ERR] = 0;
-    scal[CS_WORDS] = words;
-    // plugin semantics: raw when n <= thr or the stream is as long as n
-    // (cpu_2d/compression/cpusimd.hh:169-173)
-    if (raw_thr && n_expect) {
-        const uint64_t ne = *n_expect;
-        if (ne <= raw_thr || words == ne) {
-            scal[CS_RAW] = 1;
-            scal[CS_N] = words;
-            if (words > cap) scal[CS_ERR] |= G5_DEVERR_CORRUPT;
-            return;
-        }
-    }
-    scal[CS_RAW] = 0;
-    uint64_t err = 0;
-    uint64_t n1 = 0;
-    if (words < 4) err = 1;
-    else {
-        n1 = in[0];
-        if (in[1] != kCookie || in[2] != kCookie || in[3] != kCookie) err = 1;
-        if (n1 % 128 || n1 > cap || n1 / 128 >= max_mb) err = 1;
-    }
-    const uint64_t nmb = err ? 0 : n1 / 128;
-    const uint64_t ng = (nmb + 15) / 16;
-    const uint64_t nv = words / 4;
-    if (nv > max_vec) err = 1;
-    int R = 0;
-    while (((uint64_t)1 << R) < ng + 1) ++R;
-    if (R > lift_levels) err = 1;
-    scal[CS_N1] = err ? 0 : n1;
-    scal[CS_NMB] = err ? 0 : nmb;
-    scal[CS_NG] = err ? 0 : ng;
-    scal[CS_NV] = nv;
-    scal[CS_LIFT] = R;
-    scal[CS_N] = 0;
-    if (err) scal[CS_ERR] |= G5_DEVERR_CORRUPT;
-}
-
-// jump[i] = vector index after a group whose header is vector i (16 widths).
-__global__ void __launch_bounds__(kB) k_dec_jump(const uint32_t *in, const uint64_t *scal, uint32_t *jump)
-{
-    if (scal[CS_RAW] || scal[CS_ERR] || scal[CS_NG] < 2) return;
-    const uint64_t nv = scal[CS_NV];
-    const uint32_t sink = (uint32_t)nv + 1;
-    const uint4 *v = reinterpret_cast<const uint4 *>(in);
-    for (uint64_t i = (uint64_t)blockIdx.x * kB + threadIdx.x; i <= nv + 1; i += (uint64_t)gridDim.x * kB) {
-        uint32_t j = sink;
-        if (i < nv) {
-            const uint4 h = v[i];
-            const uint32_t hw[4] = {h.x, h.y, h.z, h.w};
-            uint32_t s = 0;
-            bool ok = true;
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-#pragma unroll
-                for (int by = 0; by < 4; ++by) {
-                    const uint32_t b = (hw[q] >> (8 * by)) & 0xFF;
-                    ok &= b <= 32;
-                    s += b;
-                }
-            if (ok && i + 1 + s <= nv) j = (uint32_t)(i + 1 + s);
-        }
-        jump[i] = j;
-    }
-}
-
-__global__ void __launch_bounds__(kB) k_dec_lift(const uint64_t *scal, uint32_t *jump, uint64_t stride, int r)
-{
-    if (scal[CS_RAW] || scal[CS_ERR] || scal[CS_NG] < 2 || (uint64_t)r + 1 >= scal[CS_LIFT]) return;
-    const uint64_t nv = scal[CS_NV];
-    const uint32_t *t = jump + stride * r;
-    uint32_t *t1 = jump + stride * (r + 1);
-    for (uint64_t i = (uint64_t)blockIdx.x * kB + threadIdx.x; i <= nv + 1; i += (uint64_t)gridDim.x * kB)
-        t1[i] = t[t[i]];
-}
-
-__global__ void __launch_bounds__(kB) k_dec_pos(const uint32_t *in, uint64_t *scal, const uint32_t *jump,
-                                                uint64_t stride, uint32_t *gpos)
-{
-    if (scal[CS_RAW] || scal[CS_ERR]) return;
-    const uint64_t ng = scal[CS_NG], nv = scal[CS_NV], nmb = scal[CS_NMB];
-    const int R = (int)scal[CS_LIFT];
-    for (uint64_t g = (uint64_t)blockIdx.x * kB + threadIdx.x; g < ng; g += (uint64_t)gridDim.x * kB) {
-        uint64_t pos = 1;
-        for (int r = 0; r < R && pos < nv; ++r)
-            if ((g >> r) & 1) pos = jump[stride * r + pos];
-        if (ng < 2) pos = 1;
-        if (pos >= nv) {
-            atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_CORRUPT);
-            pos = 0;
-        }
-        gpos[g] = (uint32_t)pos;
-        if (g == ng - 1 && pos) {
-            // the last group only holds `howmany` miniblocks
-            const uint64_t howmany = nmb - 16 * g;
-            const uint4 h = reinterpret_cast<const uint4 *>(in)[pos];
-            const uint32_t hw[4] = {h.x, h.y, h.z, h.w};
-            uint64_t s = 0;
-            bool ok = true;
-            for (uint64_t i = 0; i < howmany; ++i) {
-                const uint32_t b = (hw[i / 4] >> (24 - 8 * (i % 4))) & 0xFF;
-                ok &= b <= 32;
-                s += b;
-            }
-            const uint64_t end = pos + 1 + s;
-            if (!ok || end > nv)
-                atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_CORRUPT);
-            else
-                scal[CS_BLKEND] = 4 * end;
-        }
-    }
-    if (ng == 0 && blockIdx.x == 0 && threadIdx.x == 0) scal[CS_BLKEND] = 4;
-}
 
 // Unpacks lane j's 4 deltas of miniblock k (b < 32) or raw values (b == 32).
 __device__ __forceinline__ uint4 unpack_vec(const uint32_t *in, uint64_t off_vec, uint32_t b)
@@ -519,167 +273,737 @@ __device__ __forceinline__ void mb_locate(const uint32_t *in, const uint32_t *gp
     off_vec = (uint64_t)p + 1 + s;
 }
 
-__global__ void __launch_bounds__(kB) k_dec_sum(const uint32_t *in, const uint64_t *scal, const uint32_t *gpos,
-                                                VecFlag *mb_sf, int mode)
+// ---- one-pass kernels: decoupled look-back -----------------------------------------------
+//
+// The single-stream encoder and decoder are one pass each over the stream's
+// tiles (a group of 16 miniblocks for packing and unpacking, a range of
+// stream vectors for locating groups).  Blocks claim tiles in launch order
+// from a counter, so a tile only ever waits on tiles claimed before it, whose
+// blocks are already running.  Each tile publishes its own aggregate, then
+// its inclusive prefix once known; a tile combines the nearest inclusive
+// prefix before it with the aggregates in between.  Payloads are written
+// before their status word (with a fence between); a status word holds the
+// call's epoch, so what earlier calls left reads as "not published" and
+// nothing is cleared between calls.  The last block to finish resets the
+// counter and advances the epoch.  Every wait is bounded: past kSpinLimit
+// polls the kernel records G5_DEVERR_WAIT and goes on with what it has, so
+// no launch can spin forever.
+
+constexpr int kOB = 512;                 // one-pass blocks: 16 warps, one per miniblock of a group
+constexpr uint32_t kSpinLimit = 1u << 21;
+constexpr int kLocS = 2048;              // stream vectors per locate chunk
+constexpr int kEntries = 513;            // a group spans at most 1 + 16 * 32 vectors
+constexpr uint32_t kDead = 0xFFFFu;
+enum : uint32_t { ST_NONE = 0, ST_AGG = 1, ST_INC = 2 };
+
+// scalar slots of the one-pass kernels (the scalar block holds kScalars)
+enum {
+    CS_E_CTR = 16, CS_E_DONE = 17, CS_E_EPOCH = 18, CS_E_ERR = 19,
+    CS_L_CTR = 20, CS_L_DONE = 21, CS_L_EPOCH = 22, CS_L_ERR = 23, CS_L_LAST = 24,
+    CS_U_CTR = 25, CS_U_DONE = 26, CS_U_EPOCH = 27
+};
+
+__device__ __forceinline__ uint64_t vload64(const uint64_t *p) { return *reinterpret_cast<const volatile uint64_t *>(p); }
+__device__ __forceinline__ void vstore64(uint64_t *p, uint64_t v) { *reinterpret_cast<volatile uint64_t *>(p) = v; }
+__device__ __forceinline__ uint32_t vload32(const uint32_t *p) { return *reinterpret_cast<const volatile uint32_t *>(p); }
+
+__device__ __forceinline__ uint32_t status_flag(uint64_t s, uint64_t epoch)
 {
-    if (scal[CS_RAW] || scal[CS_ERR]) return;
-    const uint64_t nmb = scal[CS_NMB];
-    const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
-    const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
-    for (uint64_t k = gw; k < nmb; k += nw) {
-        uint64_t off;
-        uint32_t b;
-        mb_locate(in, gpos, k, off, b);
-        uint4 d = unpack_vec(in, off, b);
-        VecFlag r;
-        if (b == 32) {
-            r.v.x = __shfl_sync(0xFFFFFFFFu, d.x, 31);
-            r.v.y = __shfl_sync(0xFFFFFFFFu, d.y, 31);
-            r.v.z = __shfl_sync(0xFFFFFFFFu, d.z, 31);
-            r.v.w = __shfl_sync(0xFFFFFFFFu, d.w, 31);
-            r.f = 1;
-        } else {
-            uint32_t sx = d.x, sy = d.y, sz = d.z, sw = d.w;
-#pragma unroll
-            for (int o = 16; o; o >>= 1) {
-                sx += __shfl_xor_sync(0xFFFFFFFFu, sx, o);
-                sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
-                sz += __shfl_xor_sync(0xFFFFFFFFu, sz, o);
-                sw += __shfl_xor_sync(0xFFFFFFFFu, sw, o);
-            }
-            if (mode == G5_CODEC_DM) r.v = make_uint4(sw, sw, sw, sw);
-            else r.v = make_uint4(sx, sy, sz, sw);
-            r.f = 0;
+    return (s >> 2) == epoch ? (uint32_t)(s & 3u) : ST_NONE;
+}
+
+// Plain sums of 64-bit values (encoder: words per group).
+struct SumU64 {
+    typedef uint64_t T;
+    __device__ static T id() { return 0; }
+    __device__ static T op(T a, T b) { return a + b; }
+    __device__ static T shfl_down(T v, int o) { return __shfl_down_sync(0xFFFFFFFFu, v, o); }
+    __device__ static T bcast0(T v) { return __shfl_sync(0xFFFFFFFFu, v, 0); }
+    __device__ static T load(const T *p) { return vload64(p); }
+    __device__ static void store(T *p, T v) { vstore64(p, v); }
+};
+
+// Running lane sums with resets (decoder: a raw miniblock restarts the sums).
+struct ResetAddV {
+    typedef VecFlag T;
+    __device__ static T id() { return ResetAdd::id(); }
+    __device__ static T op(T a, T b) { return ResetAdd::op(a, b); }
+    __device__ static T shfl_down(T v, int o)
+    {
+        T r;
+        r.v.x = __shfl_down_sync(0xFFFFFFFFu, v.v.x, o);
+        r.v.y = __shfl_down_sync(0xFFFFFFFFu, v.v.y, o);
+        r.v.z = __shfl_down_sync(0xFFFFFFFFu, v.v.z, o);
+        r.v.w = __shfl_down_sync(0xFFFFFFFFu, v.v.w, o);
+        r.f = __shfl_down_sync(0xFFFFFFFFu, v.f, o);
+        return r;
+    }
+    __device__ static T bcast0(const T &v)
+    {
+        T r;
+        r.v.x = __shfl_sync(0xFFFFFFFFu, v.v.x, 0);
+        r.v.y = __shfl_sync(0xFFFFFFFFu, v.v.y, 0);
+        r.v.z = __shfl_sync(0xFFFFFFFFu, v.v.z, 0);
+        r.v.w = __shfl_sync(0xFFFFFFFFu, v.v.w, 0);
+        r.f = __shfl_sync(0xFFFFFFFFu, v.f, 0);
+        return r;
+    }
+    __device__ static T load(const T *p)
+    {
+        const volatile uint32_t *q = reinterpret_cast<const volatile uint32_t *>(p);
+        T r;
+        r.v = make_uint4(q[0], q[1], q[2], q[3]);
+        r.f = q[4];
+        return r;
+    }
+    __device__ static void store(T *p, const T &v)
+    {
+        volatile uint32_t *q = reinterpret_cast<volatile uint32_t *>(p);
+        q[0] = v.v.x;
+        q[1] = v.v.y;
+        q[2] = v.v.z;
+        q[3] = v.v.w;
+        q[4] = v.f;
+    }
+};
+
+// Decoupled look-back of tile t, run by one whole warp: publishes `mine` as
+// the tile's aggregate (tile 0: as its inclusive prefix), combines the tiles
+// before it in order and publishes the inclusive prefix; returns the
+// exclusive prefix.  agg[t] / inc[t] hold the payloads, st[t] the status.
+template <class Op>
+__device__ typename Op::T lookback(uint64_t *st, typename Op::T *agg, typename Op::T *inc, uint64_t t,
+                                   uint64_t epoch, const typename Op::T &mine, uint64_t *err)
+{
+    typedef typename Op::T T;
+    const int lane = g5_lane();
+    if (t == 0) {
+        if (lane == 0) {
+            Op::store(inc, mine);
+            __threadfence();
+            vstore64(st, (epoch << 2) | ST_INC);
         }
-        if (g5_lane() == 0) mb_sf[k] = r;
+        return Op::id();
+    }
+    if (lane == 0) {
+        Op::store(agg + t, mine);
+        __threadfence();
+        vstore64(st + t, (epoch << 2) | ST_AGG);
+    }
+    T acc = Op::id();  // combination of the tiles after the current window, in order
+    int64_t j = (int64_t)t - 1;
+    uint32_t spins = 0;
+    for (;;) {
+        const int64_t idx = j - lane;  // lane 0 is the nearest tile
+        const uint32_t flag = idx >= 0 ? status_flag(vload64(st + idx), epoch) : ST_INC;
+        const unsigned incm = __ballot_sync(0xFFFFFFFFu, flag == ST_INC);
+        const unsigned ready = __ballot_sync(0xFFFFFFFFu, flag != ST_NONE);
+        const int first = incm ? __ffs(incm) - 1 : 32;
+        const unsigned need = first == 32 ? 0xFFFFFFFFu : (2u << first) - 1u;
+        if ((ready & need) != need) {
+            if (++spins > kSpinLimit) {
+                if (lane == 0) atomicOr((unsigned long long *)err, (unsigned long long)G5_DEVERR_WAIT);
+                break;
+            }
+            __nanosleep(32);
+            continue;
+        }
+        __threadfence();
+        T v = Op::id();
+        if (lane <= first && idx >= 0) v = flag == ST_INC ? Op::load(inc + idx) : Op::load(agg + idx);
+        // in-order reduction: a higher lane is an earlier tile, so each step
+        // puts the value from the higher lane first; lane 0 ends with the
+        // window's tiles combined from the earliest to the latest
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const T y = Op::shfl_down(v, o);
+            if (lane + o < 32) v = Op::op(y, v);
+        }
+        acc = Op::op(Op::bcast0(v), acc);
+        if (first < 32) break;
+        j -= 32;
+    }
+    if (lane == 0) {
+        Op::store(inc + t, Op::op(acc, mine));
+        __threadfence();
+        vstore64(st + t, (epoch << 2) | ST_INC);
+    }
+    return acc;
+}
+
+// Claims the next tile for the whole block (thread 0 draws, all read).
+__device__ __forceinline__ uint64_t claim_tile(uint64_t *ctr, uint64_t *s_t)
+{
+    __syncthreads();  // the previous tile's shared state is no longer read
+    if (threadIdx.x == 0) *s_t = atomicAdd((unsigned long long *)ctr, 1ull);
+    __syncthreads();
+    return *s_t;
+}
+
+// True in the block that finishes last (thread 0 only); it may then reset the
+// call's counters: every other block has passed its last read of them.
+__device__ __forceinline__ bool last_block(uint64_t *done)
+{
+    __syncthreads();
+    if (threadIdx.x != 0) return false;
+    __threadfence();
+    return atomicAdd((unsigned long long *)done, 1ull) == gridDim.x - 1;
+}
+
+// Stream header words and the VariableByte tail of n - n1 (< 128) values,
+// written by one warp; blkend = word after the block part.  Total words ->
+// scal[CS_WORDS].  (compositecodec.h:31-51, variablebyte.h:100-161.)
+__device__ void enc_tail_warp(const uint32_t *in, uint64_t n, uint64_t n1, uint64_t blkend, uint32_t *out,
+                              uint64_t *scal, uint32_t *s_val, uint32_t *s_bytes)
+{
+    const int lane = g5_lane();
+    const uint32_t nt = (uint32_t)(n - n1);
+    for (uint32_t i = lane; i < nt; i += 32) s_val[i] = in[n1 + i];
+    for (uint32_t i = lane; i < (128 * 5 + 3) / 4 + 1; i += 32) s_bytes[i] = 0;
+    __syncwarp();
+    if (lane == 0) {
+        out[0] = (uint32_t)n1;
+        out[1] = kCookie;
+        out[2] = kCookie;
+        out[3] = kCookie;
+        uint8_t *bb = reinterpret_cast<uint8_t *>(s_bytes);
+        uint32_t p = 0, prev = 0;
+        for (uint32_t i = 0; i < nt; ++i) {
+            uint32_t v = s_val[i] - prev;
+            prev = s_val[i];
+            while (v >= 128u) {
+                bb[p++] = (uint8_t)(v & 127u);
+                v >>= 7;
+            }
+            bb[p++] = (uint8_t)(v | 128u);
+        }
+        const uint32_t tw = (p + 3) / 4;
+        s_val[0] = tw;
+        scal[CS_WORDS] = blkend + tw;
+        scal[CS_BLKEND] = blkend;
+    }
+    __syncwarp();
+    const uint32_t tw = s_val[0];
+    for (uint32_t i = lane; i < tw; i += 32) out[blkend + i] = s_bytes[i];
+}
+
+// ---- encoder: one pass ----------------------------------------------------------------
+//
+// One tile per group of 16 miniblocks, warp w packing miniblock w: the warp
+// computes its deltas and bit width, the block adds up the group's words
+// (4 header words + 4 b per miniblock), the group's position in the stream is
+// the exclusive prefix of the groups before it (look-back), and every warp
+// packs its miniblock there.  The block with the last group writes the
+// stream header and the VariableByte tail.  n comes from device memory, so
+// the launch can sit in a CUDA graph with a fixed grid.
+__global__ void __launch_bounds__(kOB) k_enc1(const uint32_t *__restrict__ in, const uint64_t *n_dev,
+                                              uint64_t max_n, uint64_t raw_thr, uint32_t *__restrict__ out,
+                                              uint64_t *scal, uint64_t *tst, uint64_t *tagg, uint64_t *tinc, int mode)
+{
+    __shared__ uint4 s_d[16][32];
+    __shared__ uint32_t s_b[16];
+    __shared__ uint64_t s_t, s_excl;
+    __shared__ uint32_t s_val[128];
+    __shared__ uint32_t s_bytes[(128 * 5 + 3) / 4 + 1];
+    const int lane = g5_lane(), wid = threadIdx.x >> 5;
+    const uint64_t n_in = *n_dev;
+    const bool too_long = n_in > max_n;  // a device-side length past the workspace: nothing is written
+    const uint64_t n = too_long ? 0 : n_in;
+    const uint64_t epoch = scal[CS_E_EPOCH];
+    const uint64_t n1 = n / 128 * 128, nmb = n / 128, ntiles = too_long ? 0 : (nmb + 15) / 16;
+    const bool raw = raw_thr && n <= raw_thr;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        scal[CS_N] = n;
+        scal[CS_N1] = n1;
+        scal[CS_NMB] = nmb;
+        scal[CS_RAW] = raw ? 1 : 0;
+    }
+    if (raw) {
+        for (uint64_t i = (uint64_t)blockIdx.x * kOB + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kOB)
+            out[i] = in[i];
+        if (blockIdx.x == 0 && threadIdx.x == 0) scal[CS_WORDS] = n;
+    } else {
+        for (;;) {
+            const uint64_t t = claim_tile(&scal[CS_E_CTR], &s_t);
+            if (t >= ntiles) break;
+            const uint64_t k = 16 * t + wid;
+            uint4 cur = make_uint4(0, 0, 0, 0), d = make_uint4(0, 0, 0, 0);
+            uint32_t b = 0;
+            if (k < nmb) {
+                uint4 prev;
+                load_vectors(in, k, cur, prev);
+                d = deltas(cur, prev, mode);
+                uint32_t acc = d.x | d.y | d.z | d.w;
+#pragma unroll
+                for (int o = 16; o; o >>= 1) acc |= __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+                b = bits_of(acc);
+            }
+            if (lane == 0) s_b[wid] = b;
+            __syncthreads();
+            uint32_t off = 4, tw = 4;  // this miniblock's payload offset in the group; group words
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const uint32_t w4 = 4 * s_b[i];
+                off += i < wid ? w4 : 0u;
+                tw += w4;
+            }
+            if (wid == 0) {
+                const uint64_t ex = lookback<SumU64>(tst, tagg, tinc, t, epoch, (uint64_t)tw, &scal[CS_E_ERR]);
+                if (lane == 0) s_excl = ex;
+            }
+            __syncthreads();
+            const uint64_t base = 4 + s_excl;  // word of the group's header (a multiple of 4)
+            if (wid == 0 && lane < 4)
+                out[base + lane] = (s_b[4 * lane] << 24) | (s_b[4 * lane + 1] << 16) | (s_b[4 * lane + 2] << 8) |
+                                   s_b[4 * lane + 3];
+            const uint64_t po = base + off;
+            if (k < nmb && b == 32) {
+                reinterpret_cast<uint4 *>(out + po)[lane] = cur;
+            } else if (k < nmb && b) {
+                s_d[wid][lane] = d;
+                __syncwarp();
+                for (uint32_t idx = lane; idx < 4 * b; idx += 32) {
+                    const uint32_t w = idx >> 2, l = idx & 3;
+                    const uint32_t bit0 = 32 * w;
+                    const uint32_t j0 = bit0 / b, j1 = (bit0 + 31) / b;
+                    uint32_t word = 0;
+                    for (uint32_t j = j0; j <= j1 && j < 32; ++j) {
+                        const uint32_t dj = comp(s_d[wid][j], l);
+                        const int sh = (int)(j * b) - (int)bit0;
+                        word |= sh >= 0 ? (dj << sh) : (dj >> (-sh));
+                    }
+                    out[po + idx] = word;
+                }
+            }
+            if (t == ntiles - 1 && wid == 1) enc_tail_warp(in, n, n1, base + tw, out, scal, s_val, s_bytes);
+        }
+        if (too_long && blockIdx.x == 0 && threadIdx.x == 0)
+            atomicOr((unsigned long long *)&scal[CS_E_ERR], (unsigned long long)G5_DEVERR_CAPACITY);
+        else if (ntiles == 0 && blockIdx.x == 0 && wid == 0)
+            enc_tail_warp(in, n, n1, 4, out, scal, s_val, s_bytes);
+    }
+    if (last_block(&scal[CS_E_DONE])) {
+        scal[CS_ERR] = scal[CS_E_ERR];
+        scal[CS_E_ERR] = 0;
+        scal[CS_E_CTR] = 0;
+        scal[CS_E_DONE] = 0;
+        scal[CS_E_EPOCH] = epoch + 1;
+        __threadfence();
     }
 }
 
-__global__ void __launch_bounds__(kB) k_dec_out(const uint32_t *in, uint64_t *scal, const uint32_t *gpos,
-                                                const VecFlag *mb_base, uint32_t *out, const uint32_t *expect,
-                                                int mode)
+// ---- decoder: locate groups (one pass) -------------------------------------------------
+//
+// A group's position is only given by the chain of group headers before it
+// (each says how long its group is).  The stream's vectors are cut into
+// chunks of kLocS; a chunk's first group starts somewhere in its first
+// kEntries vectors (a group spans at most that many), so the block of a
+// chunk follows the chain inside the chunk (in shared memory) from every one
+// of those entries and publishes, per entry, where the chain leaves the
+// chunk and how many groups it started: the chunk's transfer table, its
+// look-back aggregate.  Its real entry comes from the nearest chunk before
+// it that knows its own (its inclusive prefix: the next chunk's entry and
+// the groups before it), carried forward through the tables in between.
+// Then the block writes its groups' positions.  Chains through vectors that
+// cannot be headers (a width above 32, a group running past the stream) are
+// marked dead; a real chain that reaches one before the last group makes
+// the stream corrupt.
+
+// Header checks every block makes alike; false if the stream is raw or bad.
+struct DecHead {
+    uint64_t words, nv, n1, nmb, ng;
+    bool raw, bad;
+};
+
+__device__ __forceinline__ DecHead dec_head(const uint32_t *in, const uint64_t *words_dev, uint64_t cap,
+                                            uint64_t raw_thr, const uint64_t *n_expect, uint64_t max_vec,
+                                            uint64_t max_mb)
 {
-    if (scal[CS_RAW]) {
-        const uint64_t n = scal[CS_N];
-        if (scal[CS_ERR]) return;
-        for (uint64_t i = (uint64_t)blockIdx.x * kB + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kB) {
-            out[i] = in[i];
-            if (expect && expect[i] != in[i])
-                atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_MISMATCH);
-        }
-        return;
+    DecHead h;
+    h.words = *words_dev;
+    h.nv = h.words / 4;
+    h.n1 = h.nmb = h.ng = 0;
+    h.bad = false;
+    // plugin semantics: raw when n <= thr or the stream is as long as n
+    // (cpu_2d/compression/cpusimd.hh:169-173)
+    h.raw = raw_thr && n_expect && (*n_expect <= raw_thr || h.words == *n_expect);
+    if (h.raw) {
+        h.bad = h.words > cap;
+        return h;
     }
-    if (scal[CS_ERR]) return;
-    const uint64_t nmb = scal[CS_NMB];
-    const int lane = g5_lane();
-    const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
-    const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
-    bool bad = false;
-    for (uint64_t k = gw; k < nmb; k += nw) {
-        uint64_t off;
-        uint32_t b;
-        mb_locate(in, gpos, k, off, b);
-        uint4 d = unpack_vec(in, off, b);
-        const uint4 base = mb_base[k].v;
-        uint4 x;
-        if (b == 32) {
-            x = d;
-        } else if (mode == G5_CODEC_DM) {
-            uint32_t c = d.w;
+    if (h.words < 4) {
+        h.bad = true;
+    } else {
+        h.n1 = in[0];
+        if (in[1] != kCookie || in[2] != kCookie || in[3] != kCookie) h.bad = true;
+        if (h.n1 % 128 || h.n1 > cap || h.n1 / 128 >= max_mb) h.bad = true;
+    }
+    if (h.nv > max_vec) h.bad = true;
+    if (h.bad) h.n1 = 0;
+    h.nmb = h.n1 / 128;
+    h.ng = (h.nmb + 15) / 16;
+    return h;
+}
+
+__device__ __forceinline__ uint32_t width_of(uint4 h, int i)
+{
+    const uint32_t w = i < 4 ? h.x : i < 8 ? h.y : i < 12 ? h.z : h.w;
+    return (w >> (24 - 8 * (i & 3))) & 0xFFu;
+}
+
+__global__ void __launch_bounds__(kOB) k_dec_locate(const uint32_t *__restrict__ in, const uint64_t *words_dev,
+                                                    uint64_t cap, uint64_t raw_thr, const uint64_t *n_expect,
+                                                    uint64_t *scal, uint64_t max_vec, uint64_t max_mb,
+                                                    uint32_t *ltab, uint64_t *lst, uint64_t *lpay, uint32_t *gpos)
+{
+    __shared__ uint16_t s_j[kLocS];
+    __shared__ uint64_t s_t;
+    __shared__ uint32_t s_entry, s_own, s_bad;
+    __shared__ uint64_t s_gbase;
+    const uint64_t epoch = scal[CS_L_EPOCH];
+    const DecHead h = dec_head(in, words_dev, cap, raw_thr, n_expect, max_vec, max_mb);
+    const uint64_t nchunks = (h.raw || h.bad || h.ng == 0) ? 0 : (h.nv - 1 + kLocS - 1) / kLocS;
+    for (;;) {
+        const uint64_t c = claim_tile(&scal[CS_L_CTR], &s_t);
+        if (c >= nchunks) break;
+        const uint64_t a = 1 + c * kLocS;  // first vector of the chunk
+        const uint4 *v = reinterpret_cast<const uint4 *>(in);
+        for (uint32_t p = threadIdx.x; p < kLocS; p += kOB) {
+            uint32_t r = kDead;
+            if (a + p < h.nv) {
+                const uint4 hv = v[a + p];
+                uint32_t s = 0;
+                bool ok = true;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t y = __shfl_up_sync(0xFFFFFFFFu, c, o);
-                if (lane >= o) c += y;
+                for (int i = 0; i < 16; ++i) {
+                    const uint32_t b = width_of(hv, i);
+                    ok &= b <= 32;
+                    s += b;
+                }
+                if (ok && a + p + 1 + s <= h.nv) r = p + 1 + s;  // <= kLocS + 512 < kDead
             }
-            c += base.w;
-            uint32_t pc = __shfl_up_sync(0xFFFFFFFFu, c, 1);
-            if (lane == 0) pc = base.w;
-            x = make_uint4(d.x + pc, d.y + pc, d.z + pc, c);
-        } else {
-            uint32_t cx = d.x, cy = d.y, cz = d.z, cw = d.w;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t yx = __shfl_up_sync(0xFFFFFFFFu, cx, o);
-                uint32_t yy = __shfl_up_sync(0xFFFFFFFFu, cy, o);
-                uint32_t yz = __shfl_up_sync(0xFFFFFFFFu, cz, o);
-                uint32_t yw = __shfl_up_sync(0xFFFFFFFFu, cw, o);
-                if (lane >= o) {
-                    cx += yx;
-                    cy += yy;
-                    cz += yz;
-                    cw += yw;
+            s_j[p] = (uint16_t)r;
+        }
+        __syncthreads();
+        // transfer table: entry e -> (exit offset in the next chunk, groups started)
+        for (uint32_t e = threadIdx.x; e < kEntries; e += kOB) {
+            uint32_t p = e, cnt = 0, exit = kDead;
+            if (a + e < h.nv) {
+                while (p < kLocS) {
+                    const uint32_t r = s_j[p];
+                    ++cnt;  // a group starts at p
+                    if (r == kDead) break;
+                    p = r;
+                }
+                if (p >= kLocS) exit = p - kLocS;
+                else --cnt;  // the dead header starts no group
+            }
+            ltab[c * kEntries + e] = (exit << 16) | cnt;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            vstore64(lst + c, (epoch << 2) | ST_AGG);
+            // the chunk's real entry and the groups before it
+            uint64_t E = 1, G = 0;
+            bool bad = false;
+            if (c > 0) {
+                int64_t j = (int64_t)c - 1;
+                uint32_t spins = 0;
+                for (;;) {
+                    const uint32_t f = status_flag(vload64(lst + j), epoch);
+                    if (f == ST_INC) break;
+                    if (f == ST_AGG) {
+                        --j;  // chunk 0 always publishes an inclusive prefix
+                        continue;
+                    }
+                    if (++spins > kSpinLimit) {
+                        atomicOr((unsigned long long *)&scal[CS_L_ERR], (unsigned long long)G5_DEVERR_WAIT);
+                        bad = true;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+                __threadfence();
+                if (!bad) {
+                    const uint64_t pay = vload64(lpay + j);
+                    E = pay & 0xFFFFFFFFull;
+                    G = pay >> 32;
+                    for (uint64_t i = (uint64_t)j + 1; i < c && G < h.ng; ++i) {
+                        const uint64_t ai = 1 + i * kLocS;
+                        if (E < ai || E - ai >= kEntries) {
+                            bad = true;
+                            break;
+                        }
+                        const uint32_t tv = vload32(ltab + i * kEntries + (E - ai));
+                        G += tv & 0xFFFFu;
+                        if (G >= h.ng) break;
+                        if ((tv >> 16) == kDead) {
+                            bad = true;
+                            break;
+                        }
+                        E = ai + kLocS + (tv >> 16);
+                    }
                 }
             }
-            x = make_uint4(cx + base.x, cy + base.y, cz + base.z, cw + base.w);
+            if (G > h.ng) G = h.ng;
+            // this chunk's own step
+            uint64_t En = 0, Gn = h.ng;
+            uint32_t own = 0;
+            if (!bad && G < h.ng) {
+                if (E < a || E - a >= kEntries) {
+                    bad = true;
+                } else {
+                    const uint32_t tv = ltab[c * kEntries + (E - a)];
+                    const uint64_t cnt = tv & 0xFFFFu;
+                    own = (uint32_t)(G + cnt >= h.ng ? h.ng - G : cnt);
+                    Gn = G + own;
+                    if (Gn < h.ng) {
+                        if ((tv >> 16) == kDead) bad = true;
+                        else En = a + kLocS + (tv >> 16);
+                    }
+                }
+            }
+            if (bad) Gn = h.ng;  // successors own nothing
+            vstore64(lpay + c, (Gn << 32) | (En & 0xFFFFFFFFull));
+            __threadfence();
+            vstore64(lst + c, (epoch << 2) | ST_INC);
+            s_entry = (uint32_t)(E - a);
+            s_gbase = G;
+            s_own = bad ? 0 : own;
+            s_bad = bad;
+            if (bad) atomicOr((unsigned long long *)&scal[CS_L_ERR], (unsigned long long)G5_DEVERR_CORRUPT);
         }
-        reinterpret_cast<uint4 *>(out)[k * 32 + lane] = x;
-        if (expect) {
-            const uint4 e = reinterpret_cast<const uint4 *>(expect)[k * 32 + lane];
-            bad |= (e.x != x.x) | (e.y != x.y) | (e.z != x.z) | (e.w != x.w);
+        __syncthreads();
+        if (threadIdx.x == 0 && s_own) {
+            uint32_t p = s_entry;
+            for (uint32_t i = 0; i < s_own; ++i) {
+                const uint64_t g = s_gbase + i;
+                gpos[g] = (uint32_t)(a + p);
+                if (g == h.ng - 1) {
+                    // the last group holds only the remaining miniblocks
+                    const uint4 hv = v[a + p];
+                    const uint64_t howmany = h.nmb - 16 * g;
+                    uint64_t s = 0;
+                    bool ok = true;
+                    for (uint64_t q = 0; q < howmany; ++q) {
+                        const uint32_t b = width_of(hv, (int)q);
+                        ok &= b <= 32;
+                        s += b;
+                    }
+                    const uint64_t end = a + p + 1 + s;
+                    if (!ok || end > h.nv) {
+                        atomicOr((unsigned long long *)&scal[CS_L_ERR], (unsigned long long)G5_DEVERR_CORRUPT);
+                    } else {
+                        scal[CS_BLKEND] = 4 * end;
+                        scal[CS_L_LAST] = epoch;  // the last group was found
+                    }
+                }
+                p = s_j[p];
+            }
+        }
+    }
+    if (last_block(&scal[CS_L_DONE])) {
+        uint64_t err = scal[CS_L_ERR] | (h.bad ? G5_DEVERR_CORRUPT : 0);
+        if (!h.raw && !h.bad && h.ng > 0 && scal[CS_L_LAST] != epoch) err |= G5_DEVERR_CORRUPT;
+        if (!h.raw && h.ng == 0) scal[CS_BLKEND] = 4;
+        scal[CS_ERR] = err;
+        scal[CS_WORDS] = h.words;
+        scal[CS_RAW] = h.raw ? 1 : 0;
+        scal[CS_N1] = h.n1;
+        scal[CS_NMB] = h.nmb;
+        scal[CS_NG] = h.ng;
+        scal[CS_N] = h.raw ? h.words : 0;
+        scal[CS_L_ERR] = 0;
+        scal[CS_L_CTR] = 0;
+        scal[CS_L_DONE] = 0;
+        scal[CS_L_EPOCH] = epoch + 1;
+        __threadfence();
+    }
+}
+
+// ---- decoder: unpack (one pass) --------------------------------------------------------
+//
+// One tile per group, warp w unpacking miniblock w at the position the
+// locator found: the warp's lane sums (or, for a raw b = 32 miniblock, its
+// last vector with a reset flag) are the miniblock's aggregate, the group's
+// aggregate goes through the look-back, and each warp adds the prefix of
+// everything before its miniblock to its deltas.  Block 0 first decodes the
+// VariableByte tail, which starts from 0 whatever the block part holds.
+// With `expect` every value is compared with the expected one (the level
+// loop's round-trip check); `acc` accumulates words and values.
+__global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__ in, uint64_t *scal,
+                                                    const uint32_t *__restrict__ gpos, uint32_t *__restrict__ out,
+                                                    uint64_t cap, const uint64_t *n_expect,
+                                                    const uint32_t *__restrict__ expect, uint64_t *acc,
+                                                    uint64_t *ust, VecFlag *uagg, VecFlag *uinc, int mode)
+{
+    __shared__ VecFlag s_vf[16];
+    __shared__ VecFlag s_base[16];
+    __shared__ uint64_t s_t;
+    __shared__ uint32_t s_b[kTailMaxBytes / 4];
+    const int lane = g5_lane(), wid = threadIdx.x >> 5;
+    const uint64_t epoch = scal[CS_U_EPOCH];
+    const uint64_t err0 = scal[CS_ERR];
+    const uint64_t words = scal[CS_WORDS];
+    bool bad = false;
+    if (scal[CS_RAW]) {
+        const uint64_t n = scal[CS_N];
+        if (!err0)
+            for (uint64_t i = (uint64_t)blockIdx.x * kOB + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kOB) {
+                out[i] = in[i];
+                bad |= expect && expect[i] != in[i];
+            }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            if (n_expect && n != *n_expect) atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_MISMATCH);
+            if (acc) {
+                acc[0] += words;
+                acc[1] += n;
+            }
+        }
+    } else if (!err0) {
+        const uint64_t nmb = scal[CS_NMB], ng = scal[CS_NG], n1 = scal[CS_N1];
+        if (blockIdx.x == 0 && wid == 0) {
+            // VariableByte tail (variablebyte.h:217-): words after the block part
+            const uint64_t blkend = scal[CS_BLKEND];
+            const uint64_t tw = words > blkend ? words - blkend : 0;
+            if (tw * 4 > kTailMaxBytes) {
+                if (lane == 0) atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_CORRUPT);
+            } else {
+                for (uint64_t i = lane; i < tw; i += 32) s_b[i] = in[blkend + i];
+                __syncwarp();
+                if (lane == 0) {
+                    const uint8_t *bb = reinterpret_cast<const uint8_t *>(s_b);
+                    uint64_t o = n1, e = 0;
+                    uint32_t prev = 0, v = 0;
+                    int shift = 0;
+                    for (uint64_t p = 0; p < tw * 4; ++p) {
+                        const uint32_t c = bb[p];
+                        v |= (c & 127u) << shift;
+                        if (c & 128u) {
+                            if (o >= cap) {
+                                e |= G5_DEVERR_CORRUPT;
+                                break;
+                            }
+                            prev += v;
+                            out[o] = prev;
+                            if (expect && expect[o] != prev) e |= G5_DEVERR_MISMATCH;
+                            ++o;
+                            v = 0;
+                            shift = 0;
+                        } else {
+                            shift += 7;
+                            if (shift > 28) {
+                                e |= G5_DEVERR_CORRUPT;
+                                break;
+                            }
+                        }
+                    }
+                    scal[CS_N] = o;
+                    if (n_expect && o != *n_expect) e |= G5_DEVERR_MISMATCH;
+                    if (e) atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)e);
+                    if (acc) {
+                        acc[0] += words;
+                        acc[1] += o;
+                    }
+                }
+            }
+        }
+        for (;;) {
+            const uint64_t t = claim_tile(&scal[CS_U_CTR], &s_t);
+            if (t >= ng) break;
+            const uint64_t k = 16 * t + wid;
+            uint4 d = make_uint4(0, 0, 0, 0);
+            uint32_t b = 0;
+            VecFlag mine = ResetAdd::id();
+            if (k < nmb) {
+                const uint32_t p = gpos[t];
+                const uint4 hv = reinterpret_cast<const uint4 *>(in)[p];
+                uint64_t off = (uint64_t)p + 1;
+                for (int i = 0; i < wid; ++i) off += width_of(hv, i);
+                b = width_of(hv, wid);
+                d = unpack_vec(in, off, b);
+                if (b == 32) {
+                    mine.v.x = __shfl_sync(0xFFFFFFFFu, d.x, 31);
+                    mine.v.y = __shfl_sync(0xFFFFFFFFu, d.y, 31);
+                    mine.v.z = __shfl_sync(0xFFFFFFFFu, d.z, 31);
+                    mine.v.w = __shfl_sync(0xFFFFFFFFu, d.w, 31);
+                    mine.f = 1;
+                } else {
+                    uint32_t sx = d.x, sy = d.y, sz = d.z, sw = d.w;
+#pragma unroll
+                    for (int o = 16; o; o >>= 1) {
+                        sx += __shfl_xor_sync(0xFFFFFFFFu, sx, o);
+                        sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
+                        sz += __shfl_xor_sync(0xFFFFFFFFu, sz, o);
+                        sw += __shfl_xor_sync(0xFFFFFFFFu, sw, o);
+                    }
+                    mine.v = mode == G5_CODEC_DM ? make_uint4(sw, sw, sw, sw) : make_uint4(sx, sy, sz, sw);
+                    mine.f = 0;
+                }
+            }
+            if (lane == 0) s_vf[wid] = mine;
+            __syncthreads();
+            if (wid == 0) {
+                VecFlag tile = ResetAdd::id();
+                for (int i = 0; i < 16; ++i) tile = ResetAdd::op(tile, s_vf[i]);
+                const VecFlag ex = lookback<ResetAddV>(ust, uagg, uinc, t, epoch, tile, &scal[CS_ERR]);
+                if (lane == 0) {
+                    VecFlag run = ex;
+                    for (int i = 0; i < 16; ++i) {
+                        s_base[i] = run;
+                        run = ResetAdd::op(run, s_vf[i]);
+                    }
+                }
+            }
+            __syncthreads();
+            if (k < nmb) {
+                const uint4 base = s_base[wid].v;
+                uint4 x;
+                if (b == 32) {
+                    x = d;
+                } else if (mode == G5_CODEC_DM) {
+                    uint32_t c = d.w;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, c, o);
+                        if (lane >= o) c += y;
+                    }
+                    c += base.w;
+                    uint32_t pc = __shfl_up_sync(0xFFFFFFFFu, c, 1);
+                    if (lane == 0) pc = base.w;
+                    x = make_uint4(d.x + pc, d.y + pc, d.z + pc, c);
+                } else {
+                    uint32_t cx = d.x, cy = d.y, cz = d.z, cw = d.w;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t yx = __shfl_up_sync(0xFFFFFFFFu, cx, o);
+                        const uint32_t yy = __shfl_up_sync(0xFFFFFFFFu, cy, o);
+                        const uint32_t yz = __shfl_up_sync(0xFFFFFFFFu, cz, o);
+                        const uint32_t yw = __shfl_up_sync(0xFFFFFFFFu, cw, o);
+                        if (lane >= o) {
+                            cx += yx;
+                            cy += yy;
+                            cz += yz;
+                            cw += yw;
+                        }
+                    }
+                    x = make_uint4(cx + base.x, cy + base.y, cz + base.z, cw + base.w);
+                }
+                reinterpret_cast<uint4 *>(out)[k * 32 + lane] = x;
+                if (expect) {
+                    const uint4 e = reinterpret_cast<const uint4 *>(expect)[k * 32 + lane];
+                    bad |= (e.x != x.x) | (e.y != x.y) | (e.z != x.z) | (e.w != x.w);
+                }
+            }
         }
     }
     if (bad) atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_MISMATCH);
-}
-
-__global__ void k_dec_tail(const uint32_t *in, uint64_t *scal, uint64_t cap, uint32_t *out,
-                           const uint64_t *n_expect, const uint32_t *expect, uint64_t *acc)
-{
-    __shared__ uint32_t s_b[kTailMaxBytes / 4];
-    const int lane = threadIdx.x;
-    if (scal[CS_RAW]) {
-        if (lane == 0) {
-            if (n_expect && scal[CS_N] != *n_expect) scal[CS_ERR] |= G5_DEVERR_MISMATCH;
-            if (acc) {
-                acc[0] += scal[CS_WORDS];
-                acc[1] += scal[CS_N];
-            }
-        }
-        return;
-    }
-    if (scal[CS_ERR]) return;
-    const uint64_t words = scal[CS_WORDS], blkend = scal[CS_BLKEND], n1 = scal[CS_N1];
-    const uint64_t tw = words > blkend ? words - blkend : 0;
-    if (tw * 4 > kTailMaxBytes) {
-        if (lane == 0) scal[CS_ERR] |= G5_DEVERR_CORRUPT;
-        return;
-    }
-    for (uint64_t i = lane; i < tw; i += 32) s_b[i] = in[blkend + i];
-    __syncwarp();
-    if (lane == 0) {
-        const uint8_t *bb = reinterpret_cast<const uint8_t *>(s_b);
-        uint64_t o = n1;
-        uint32_t prev = 0, v = 0;
-        int shift = 0;
-        uint64_t err = 0;
-        for (uint64_t p = 0; p < tw * 4; ++p) {
-            const uint32_t c = bb[p];
-            v |= (c & 127u) << shift;
-            if (c & 128u) {
-                if (o >= cap) {
-                    err |= G5_DEVERR_CORRUPT;
-                    break;
-                }
-                prev += v;
-                out[o] = prev;
-                if (expect && expect[o] != prev) err |= G5_DEVERR_MISMATCH;
-                ++o;
-                v = 0;
-                shift = 0;
-            } else {
-                shift += 7;
-                if (shift > 28) {
-                    err |= G5_DEVERR_CORRUPT;
-                    break;
-                }
-            }
-        }
-        scal[CS_N] = o;
-        if (n_expect && o != *n_expect) err |= G5_DEVERR_MISMATCH;
-        scal[CS_ERR] |= err;
-        if (acc) {
-            acc[0] += words;
-            acc[1] += o;
-        }
+    if (last_block(&scal[CS_U_DONE])) {
+        scal[CS_U_CTR] = 0;
+        scal[CS_U_DONE] = 0;
+        scal[CS_U_EPOCH] = epoch + 1;
+        __threadfence();
     }
 }
 
@@ -1110,14 +1434,6 @@ __global__ void k_bdec_tail(const uint32_t *in, BStream *bs, int k, uint32_t *ou
     }
 }
 
-int lift_levels_for(size_t max_n)
-{
-    const size_t ng = (max_n / 128 + 15) / 16;
-    int R = 0;
-    while (((size_t)1 << R) < ng + 1) ++R;
-    return R < 1 ? 1 : R;
-}
-
 }  // namespace
 
 size_t codec_bound(size_t n)
@@ -1126,50 +1442,57 @@ size_t codec_bound(size_t n)
     return 4 + 4 * (mb / 16 + 1) + mb * 128 + ((n % 128) * 5 + 3) / 4 + 8;
 }
 
+size_t codec_tiles(size_t max_n) { return (max_n / 128 + 1) / 16 + 2; }
+
+size_t codec_chunks(size_t max_n) { return (codec_bound(max_n) / 4 + 2) / kLocS + 2; }
+
+int codec_grid() { return num_sms() * 2; }
+
 g5_status codec_work_alloc(CodecWork &w, size_t max_n)
 {
     w.max_n = max_n;
     w.max_mb = max_n / 128 + 1;
     w.max_vec = codec_bound(max_n) / 4 + 2;
-    w.lift_levels = lift_levels_for(max_n);
-    w.grid = num_sms() * 4;
-    G5_CUDA(cudaMalloc(&w.mb_len, sizeof(uint32_t) * w.max_mb));
-    G5_CUDA(cudaMalloc(&w.mb_bits, w.max_mb));
-    G5_CUDA(cudaMalloc(&w.jump, sizeof(uint32_t) * (w.max_vec + 2) * (size_t)w.lift_levels));
-    G5_CUDA(cudaMalloc(&w.gpos, sizeof(uint32_t) * (w.max_mb / 16 + 2)));
-    G5_CUDA(cudaMalloc(&w.mb_sum, sizeof(VecFlag) * w.max_mb));
-    G5_CUDA(cudaMalloc(&w.mb_base, sizeof(VecFlag) * w.max_mb));
-    w.mb_flag = nullptr;
-    G5_CUDA(cudaMalloc(&w.part, sizeof(VecFlag) * (size_t)(w.grid + 1)));
-    G5_CUDA(cudaMalloc(&w.scal, sizeof(uint64_t) * 16));
-    G5_CUDA(cudaMemset(w.scal, 0, sizeof(uint64_t) * 16));
+    w.grid = codec_grid();
+    const size_t T = codec_tiles(max_n), C = codec_chunks(max_n);
+    G5_CUDA(cudaMalloc(&w.scal, sizeof(uint64_t) * kScalars));
+    G5_CUDA(cudaMalloc(&w.gpos, sizeof(uint32_t) * T));
+    G5_CUDA(cudaMalloc(&w.est, sizeof(uint64_t) * 3 * T));
+    w.eagg = w.est + T;
+    w.einc = w.est + 2 * T;
+    G5_CUDA(cudaMalloc(&w.ltab, sizeof(uint32_t) * kEntries * C));
+    G5_CUDA(cudaMalloc(&w.lst, sizeof(uint64_t) * 2 * C));
+    w.lpay = w.lst + C;
+    G5_CUDA(cudaMalloc(&w.ust, sizeof(uint64_t) * T));
+    G5_CUDA(cudaMalloc(&w.uagg, sizeof(VecFlag) * 2 * T));
+    w.uinc = w.uagg + T;
+    // epochs start at 1, so zeroed status words read as "not published"
+    G5_CUDA(cudaMemset(w.scal, 0, sizeof(uint64_t) * kScalars));
+    G5_CUDA(cudaMemset(w.est, 0, sizeof(uint64_t) * 3 * T));
+    G5_CUDA(cudaMemset(w.lst, 0, sizeof(uint64_t) * 2 * C));
+    G5_CUDA(cudaMemset(w.ust, 0, sizeof(uint64_t) * T));
+    const uint64_t one = 1;
+    for (int e : {CS_E_EPOCH, CS_L_EPOCH, CS_U_EPOCH})
+        G5_CUDA(cudaMemcpy(w.scal + e, &one, sizeof one, cudaMemcpyHostToDevice));
     return G5_OK;
 }
 
 void codec_work_free(CodecWork &w)
 {
-    cudaFree(w.mb_len);
-    cudaFree(w.mb_bits);
-    cudaFree(w.jump);
-    cudaFree(w.gpos);
-    cudaFree(w.mb_sum);
-    cudaFree(w.mb_base);
-    cudaFree(w.part);
     cudaFree(w.scal);
+    cudaFree(w.gpos);
+    cudaFree(w.est);
+    cudaFree(w.ltab);
+    cudaFree(w.lst);
+    cudaFree(w.ust);
+    cudaFree(w.uagg);
     w = CodecWork();
 }
 
 void codec_encode_launch(CodecWork &w, const uint32_t *in, const uint64_t *n_dev, uint32_t *out, int mode,
                          uint64_t raw_threshold, cudaStream_t s)
 {
-    k_enc_prep<<<1, 32, 0, s>>>(n_dev, raw_threshold, w.scal);
-    k_enc_bits<<<w.grid, kB, 0, s>>>(in, w.scal, w.mb_bits, w.mb_len, mode);
-    uint32_t *part = reinterpret_cast<uint32_t *>(w.part);
-    k_scan_red<AddU32><<<w.grid, kB, 0, s>>>(w.mb_len, w.scal + CS_NMB, part);
-    k_scan_top<AddU32><<<1, kB, 0, s>>>(part, w.grid, part + w.grid);
-    k_scan_down<AddU32><<<w.grid, kB, 0, s>>>(w.mb_len, w.mb_len, w.scal + CS_NMB, part);
-    k_enc_pack<<<w.grid, kB, 0, s>>>(in, w.scal, w.mb_bits, w.mb_len, out, mode);
-    k_enc_tail<<<1, 32, 0, s>>>(in, w.scal, part + w.grid, out);
+    k_enc1<<<w.grid, kOB, 0, s>>>(in, n_dev, w.max_n, raw_threshold, out, w.scal, w.est, w.eagg, w.einc, mode);
 }
 
 void codec_decode_launch(CodecWork &w, const uint32_t *in, const uint64_t *words_dev, uint32_t *out, size_t cap,
@@ -1183,21 +1506,10 @@ void decode_launch_acc(CodecWork &w, const uint32_t *in, const uint64_t *words_d
                        int mode, uint64_t raw_threshold, const uint64_t *n_expect_dev, const uint32_t *expect,
                        uint64_t *acc, cudaStream_t s)
 {
-    const uint64_t stride = w.max_vec + 2;
-    k_dec_prep<<<1, 32, 0, s>>>(in, words_dev, cap, raw_threshold, n_expect_dev, w.scal, w.lift_levels,
-                                 w.max_vec, w.max_mb);
-    k_dec_jump<<<w.grid, kB, 0, s>>>(in, w.scal, w.jump);
-    for (int r = 0; r + 1 < w.lift_levels; ++r) k_dec_lift<<<w.grid, kB, 0, s>>>(w.scal, w.jump, stride, r);
-    k_dec_pos<<<w.grid, kB, 0, s>>>(in, w.scal, w.jump, stride, w.gpos);
-    VecFlag *sf = reinterpret_cast<VecFlag *>(w.mb_sum);
-    VecFlag *base = reinterpret_cast<VecFlag *>(w.mb_base);
-    VecFlag *part = reinterpret_cast<VecFlag *>(w.part);
-    k_dec_sum<<<w.grid, kB, 0, s>>>(in, w.scal, w.gpos, sf, mode);
-    k_scan_red<ResetAdd><<<w.grid, kB, 0, s>>>(sf, w.scal + CS_NMB, part);
-    k_scan_top<ResetAdd><<<1, kB, 0, s>>>(part, w.grid, nullptr);
-    k_scan_down<ResetAdd><<<w.grid, kB, 0, s>>>(sf, base, w.scal + CS_NMB, part);
-    k_dec_out<<<w.grid, kB, 0, s>>>(in, w.scal, w.gpos, base, out, expect, mode);
-    k_dec_tail<<<1, 32, 0, s>>>(in, w.scal, cap, out, n_expect_dev, expect, acc);
+    k_dec_locate<<<w.grid, kOB, 0, s>>>(in, words_dev, cap, raw_threshold, n_expect_dev, w.scal, w.max_vec,
+                                        w.max_mb, w.ltab, w.lst, w.lpay, w.gpos);
+    k_dec_unpack<<<w.grid, kOB, 0, s>>>(in, w.scal, w.gpos, out, cap, n_expect_dev, expect, acc, w.ust, w.uagg,
+                                        w.uinc, mode);
 }
 
 }  // namespace g5
@@ -1291,6 +1603,8 @@ g5_status g5_codec_encode(g5_codec *c, const uint32_t *in_dev, size_t n, uint32_
     G5_CUDA(cudaGetLastError());
     G5_CUDA(cudaMemcpyAsync(c->h_scal, c->w.scal, sizeof(uint64_t) * 8, cudaMemcpyDeviceToHost, s));
     G5_CUDA(cudaStreamSynchronize(s));
+    if (c->h_scal[g5::CS_ERR] & G5_DEVERR_WAIT) return G5_ERR_TIMEOUT;
+    if (c->h_scal[g5::CS_ERR]) return G5_ERR_CAPACITY;
     *out_words = (size_t)c->h_scal[g5::CS_WORDS];
     return G5_OK;
 }
@@ -1309,8 +1623,46 @@ g5_status g5_codec_decode(g5_codec *c, const uint32_t *in_dev, size_t words, uin
     G5_CUDA(cudaGetLastError());
     G5_CUDA(cudaMemcpyAsync(c->h_scal, c->w.scal, sizeof(uint64_t) * 8, cudaMemcpyDeviceToHost, s));
     G5_CUDA(cudaStreamSynchronize(s));
+    if (c->h_scal[g5::CS_ERR] & G5_DEVERR_WAIT) return G5_ERR_TIMEOUT;
     if (c->h_scal[g5::CS_ERR]) return G5_ERR_CORRUPT_STREAM;
     *out_n = (size_t)c->h_scal[g5::CS_N];
+    return G5_OK;
+}
+
+g5_status g5_codec_encode_async(g5_codec *c, const uint32_t *in_dev, const uint64_t *n_dev, uint32_t *out_dev,
+                                uint64_t *out_words_dev, int mode, void *stream)
+{
+    if (!c || !in_dev || !n_dev || !out_dev || !out_words_dev) return G5_ERR_INVALID_ARG;
+    if (mode != G5_CODEC_D4 && mode != G5_CODEC_DM) return G5_ERR_INVALID_ARG;
+    if (((uintptr_t)in_dev | (uintptr_t)out_dev) & 15) return G5_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    g5::codec_encode_launch(c->w, in_dev, n_dev, out_dev, mode, 0, s);
+    G5_CUDA(cudaGetLastError());
+    G5_CUDA(cudaMemcpyAsync(out_words_dev, c->w.scal + g5::CS_WORDS, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+    return G5_OK;
+}
+
+g5_status g5_codec_decode_async(g5_codec *c, const uint32_t *in_dev, const uint64_t *words_dev, uint32_t *out_dev,
+                                size_t out_cap, uint64_t *out_n_dev, int mode, void *stream)
+{
+    if (!c || !in_dev || !words_dev || !out_dev || !out_n_dev) return G5_ERR_INVALID_ARG;
+    if (mode != G5_CODEC_D4 && mode != G5_CODEC_DM) return G5_ERR_INVALID_ARG;
+    if (((uintptr_t)in_dev | (uintptr_t)out_dev) & 15) return G5_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    g5::codec_decode_launch(c->w, in_dev, words_dev, out_dev, out_cap, mode, 0, nullptr, nullptr, s);
+    G5_CUDA(cudaGetLastError());
+    G5_CUDA(cudaMemcpyAsync(out_n_dev, c->w.scal + g5::CS_N, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+    return G5_OK;
+}
+
+g5_status g5_codec_status(g5_codec *c)
+{
+    if (!c) return G5_ERR_INVALID_ARG;
+    uint64_t err = 0;
+    G5_CUDA(cudaMemcpy(&err, c->w.scal + g5::CS_ERR, sizeof err, cudaMemcpyDeviceToHost));
+    if (err & G5_DEVERR_WAIT) return G5_ERR_TIMEOUT;
+    if (err & G5_DEVERR_CAPACITY) return G5_ERR_CAPACITY;
+    if (err) return G5_ERR_CORRUPT_STREAM;
     return G5_OK;
 }
 
@@ -1352,7 +1704,7 @@ g5_status g5_codec_encode_batch(g5_codec *c, const uint32_t *in_dev, const uint6
     }
     mb0[k] = total_mb;
     BatchWs &w = c->bw;
-    const int grid = c->w.grid;
+    const int grid = g5::num_sms() * 4;
     G5_TRY(w.grow(BatchWs::BS, sizeof(g5::BStream) * (size_t)k));
     G5_TRY(w.grow(BatchWs::IDX, sizeof(uint64_t) * ((size_t)k + 1)));
     G5_TRY(w.grow(BatchWs::BITS, total_mb + 1));
@@ -1427,7 +1779,7 @@ g5_status g5_codec_decode_batch(g5_codec *c, const uint32_t *in_dev, const uint6
     while (((uint64_t)1 << R) < (uint64_t)max_ng + 1) ++R;
     const uint64_t stride = total_v + 1;
     BatchWs &w = c->bw;
-    const int grid = c->w.grid;
+    const int grid = g5::num_sms() * 4;
     G5_TRY(w.grow(BatchWs::BS, sizeof(g5::BStream) * (size_t)k));
     G5_TRY(w.grow(BatchWs::IDX, sizeof(uint64_t) * 3 * ((size_t)k + 1)));
     G5_TRY(w.grow(BatchWs::JUMP, sizeof(uint32_t) * stride * (size_t)R));
@@ -1486,21 +1838,25 @@ g5_status g5_codec_decode_batch(g5_codec *c, const uint32_t *in_dev, const uint6
 // that may not block on (or fragment) device memory between requests, or a
 // host process whose device memory is owned by another allocator (a
 // framework's caching pool) with no headroom for cudaMalloc.  The encoder's
-// scratch (bit widths, payload offsets, scan partials, length scalars) lives
-// in the file-scope array below instead of a g5_codec workspace: 57,741
-// bytes (about 56 KiB, kNoAllocBytes) that every GPU which loads the library
-// holds until the process exits.  The array's device address is looked up
+// scratch (its scalars and tile counter, the length, and the look-back words
+// of every group) lives in the file-scope array below instead of a g5_codec
+// workspace: 12,608 bytes (about 12 KiB, kNoAllocBytes) that every GPU which
+// loads the library holds until the process exits.  Nothing in it needs
+// clearing between calls: the look-back words carry the call's epoch, and
+// the last block of each call resets the tile counter and advances the
+// epoch (the array starts zeroed).  The array's device address is looked up
 // once per device and cached for the life of the process, so the entry point
 // must not be used again on a device after cudaDeviceReset in the same
 // process (the reset frees the module that holds the array).
 
 namespace {
 
-constexpr size_t kNoAllocMaxValues = (size_t)1 << 20;          // values per call
-constexpr size_t kNoAllocMb = kNoAllocMaxValues / 128 + 1;       // miniblocks
-constexpr size_t kNoAllocParts = 4096;                           // scan partials
-constexpr size_t kNoAllocBytes = 128 + 8 + kNoAllocMb * 4 + kNoAllocMb + kNoAllocParts * 4 + 256;
-static_assert(kNoAllocBytes == 57741, "the documented size of the scratch array");
+constexpr size_t kNoAllocMaxValues = (size_t)1 << 20;             // values per call
+constexpr size_t kNoAllocMb = kNoAllocMaxValues / 128 + 1;          // miniblocks
+constexpr size_t kNoAllocTiles = kNoAllocMb / 16 + 2;               // look-back groups
+constexpr size_t kNoAllocScal = sizeof(uint64_t) * g5::kScalars;    // scalars
+constexpr size_t kNoAllocBytes = kNoAllocScal + 16 + 3 * sizeof(uint64_t) * kNoAllocTiles;
+static_assert(kNoAllocBytes == 12608, "the documented size of the scratch array");
 
 // In host code this name is only a host-side stand-in for the device array;
 // kernels receive the device address fetched with cudaGetSymbolAddress.
@@ -1540,25 +1896,23 @@ extern "C" g5_status g5_codec_encode_noalloc(const uint32_t *in_dev, size_t n, u
     g5::CodecWork w;
     w.max_n = kNoAllocMaxValues;
     w.max_mb = kNoAllocMb;
-    w.grid = std::min(g5::num_sms() * 4, (int)kNoAllocParts - 1);
-    w.scal = reinterpret_cast<uint64_t *>(b);                        // 16 scalars
-    uint64_t *n_dev = reinterpret_cast<uint64_t *>(b + 128);
-    w.mb_len = reinterpret_cast<uint32_t *>(b + 136);
-    w.mb_bits = reinterpret_cast<uint8_t *>(b + 136 + kNoAllocMb * 4);
-    const size_t off_part = (136 + 5 * kNoAllocMb + 7) & ~(size_t)7;
-    static_assert(((136 + 5 * kNoAllocMb + 7) & ~(size_t)7) + kNoAllocParts * 4 <= kNoAllocBytes,
+    w.grid = g5::codec_grid();
+    w.scal = reinterpret_cast<uint64_t *>(b);
+    uint64_t *n_dev = reinterpret_cast<uint64_t *>(b + kNoAllocScal);
+    w.est = reinterpret_cast<uint64_t *>(b + kNoAllocScal + 16);
+    w.eagg = w.est + kNoAllocTiles;
+    w.einc = w.est + 2 * kNoAllocTiles;
+    static_assert(kNoAllocScal + 16 + 3 * sizeof(uint64_t) * kNoAllocTiles <= kNoAllocBytes,
                   "scratch layout exceeds the static array");
-    w.part = reinterpret_cast<uint64_t *>(b + off_part);
     cudaStream_t s = (cudaStream_t)stream;
     uint64_t hn = n;
-    // every scratch word the encoder reads is written earlier in the same
-    // call (k_enc_prep resets the scalars), so nothing needs clearing here
     G5_CUDA(cudaMemcpyAsync(n_dev, &hn, sizeof hn, cudaMemcpyHostToDevice, s));
     g5::codec_encode_launch(w, in_dev, n_dev, out_dev, mode, 0, s);
     G5_CUDA(cudaGetLastError());
-    uint64_t words = 0;
-    G5_CUDA(cudaMemcpyAsync(&words, w.scal + g5::CS_WORDS, sizeof words, cudaMemcpyDeviceToHost, s));
+    uint64_t sc[3] = {0, 0, 0};  // CS_N, CS_WORDS, CS_ERR
+    G5_CUDA(cudaMemcpyAsync(sc, w.scal, sizeof sc, cudaMemcpyDeviceToHost, s));
     G5_CUDA(cudaStreamSynchronize(s));
-    *out_words = (size_t)words;
+    if (sc[g5::CS_ERR]) return G5_ERR_TIMEOUT;
+    *out_words = (size_t)sc[g5::CS_WORDS];
     return G5_OK;
 }

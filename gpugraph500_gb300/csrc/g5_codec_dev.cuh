@@ -9,24 +9,27 @@
 
 namespace g5 {
 
+// Four running lane sums and a reset flag (a raw miniblock restarts the sums).
+struct VecFlag {
+    uint4 v;
+    uint32_t f;
+};
+
 struct CodecWork {
     size_t max_n = 0;        // capacity in values
     size_t max_mb = 0;       // miniblocks
     size_t max_vec = 0;      // 16-byte vectors of the largest stream
-    int lift_levels = 0;     // binary-lifting tables
     int grid = 0;            // blocks of the fixed grid
-    // encoder
-    uint32_t *mb_len = nullptr;    // 4*b per miniblock, then exclusive prefix
-    uint8_t *mb_bits = nullptr;    // b per miniblock
-    // decoder
-    uint32_t *jump = nullptr;      // lift_levels tables of max_vec + 1 entries
-    uint32_t *gpos = nullptr;      // vector index of each group header
-    uint4 *mb_sum = nullptr;       // per miniblock lane sums (or raw last vector)
-    uint32_t *mb_flag = nullptr;   // 1 if the miniblock is raw (b == 32)
-    uint4 *mb_base = nullptr;      // scanned base vector of each miniblock
-    // scan partials and device scalars
-    uint64_t *part = nullptr;      // grid * 8 words
-    uint64_t *scal = nullptr;      // device scalars, see CodecScalar
+    uint64_t *scal = nullptr;  // device scalars (kScalars), see CodecScalar
+    uint32_t *gpos = nullptr;  // decoder: vector index of each group header
+    // encoder look-back: status, aggregate and inclusive words per group
+    uint64_t *est = nullptr, *eagg = nullptr, *einc = nullptr;
+    // decoder group locator: per chunk a transfer table, status and payload
+    uint32_t *ltab = nullptr;
+    uint64_t *lst = nullptr, *lpay = nullptr;
+    // decoder unpacker look-back: status, aggregate and inclusive lane sums per group
+    uint64_t *ust = nullptr;
+    VecFlag *uagg = nullptr, *uinc = nullptr;
 };
 
 enum CodecScalar {
@@ -37,6 +40,14 @@ enum CodecScalar {
     CS_BLKEND = 4,  // word index where the block part ends
     CS_COUNT = 8
 };
+
+constexpr int kScalars = 32;  // scalar slots of a CodecWork
+
+// Look-back status groups and locate chunks a workspace for max_n values
+// needs, and the fixed grid of the codec kernels.
+size_t codec_tiles(size_t max_n);
+size_t codec_chunks(size_t max_n);
+int codec_grid();
 
 size_t codec_bound(size_t n);
 g5_status codec_work_alloc(CodecWork &w, size_t max_n);

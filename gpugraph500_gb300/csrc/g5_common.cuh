@@ -76,6 +76,7 @@ enum : uint32_t {
     G5_DEVERR_CORRUPT = 2u,
     G5_DEVERR_MISMATCH = 4u,
     G5_DEVERR_LEVELS = 8u,
+    G5_DEVERR_WAIT = 16u,  // a bounded device wait ran out
 };
 
 __device__ __forceinline__ int g5_lane() { return threadIdx.x & 31; }

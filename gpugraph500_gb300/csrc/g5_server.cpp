@@ -52,6 +52,8 @@ constexpr int64_t kAutoLevelsVertices = int64_t(1) << 25;
 // ones (whose one-root searches are short) stream workspaces.
 constexpr int64_t kCohortVertices = int64_t(1) << 21;
 constexpr int kCohortWorkspaces = 2;  // batch workspaces per cohort graph
+constexpr int kCohortPlain = 2;       // one-root workspaces per cohort graph
+constexpr size_t kCohortMin = 3;      // queued queries that start a cohort while a one-root workspace is free
 
 // One batch workspace of a cohort graph and the queries it runs.
 struct Cohort {
@@ -69,7 +71,8 @@ struct Query {
     int graph = 0;
     int64_t root = 0;
     int slot = -1;
-    int cohort = -1;  // cohort graphs: workspace index (slot = root index in it)
+    int cohort = -1;  // cohort graphs: batch workspace index (slot = root index in it), or -1 for a
+                      // one-root workspace (slot = its index)
     int state = 0;  // 0 queued, 1 running, 2 done, 3 released
     Clock::time_point t_submit, t_start, t_done;
 };
@@ -84,6 +87,7 @@ struct g5_server {
     std::vector<int> bidx;                  // per graph: index in the batch (-1 if none)
     std::vector<std::vector<g5_bfs *>> ws;  // streams mode: workspaces per graph
     std::vector<std::vector<Cohort>> cohorts;  // cohort graphs: batch workspaces
+    std::vector<std::vector<uint64_t>> plain_query;  // cohort graphs: ticket per one-root workspace (0 free)
     uint32_t *col_buf = nullptr;          // one root's uint32 parents, gathered for a result
     std::vector<uint32_t> col_host;
     std::mutex result_mu;                 // guards col_buf / col_host
@@ -282,6 +286,8 @@ void worker_cohorts(g5_server *sv)
     cudaSetDevice(sv->graphs[0]->device);
     const int ng = (int)sv->graphs.size();
     int nrun = 0;
+    std::vector<std::vector<int>> plain_run(ng);
+    for (int g = 0; g < ng; ++g) plain_run[g].assign(sv->plain_query[g].size(), 0);
     auto fail = [&](g5_status st) {
         sv->error = st;
         sv->stop.store(true);
@@ -292,7 +298,28 @@ void worker_cohorts(g5_server *sv)
             std::unique_lock<std::mutex> lk(sv->mu);
             for (int g = 0; g < ng; ++g) {
                 if (sv->kind[g] != G5_SERVE_COHORTS) continue;
+                // a short queue runs on one-root workspaces (a lone query
+                // finishes sooner alone than as a batch); a longer one, or one
+                // with no such workspace free, starts a cohort
+                for (int s = 0; s < (int)sv->plain_query[g].size(); ++s) {
+                    if (sv->queue[g].empty() || sv->queue[g].size() >= kCohortMin) break;
+                    if (sv->plain_query[g][s] != 0) continue;
+                    const uint64_t t = sv->queue[g].front();
+                    sv->queue[g].pop_front();
+                    Query &q = sv->queries[t];
+                    q.cohort = -1;
+                    q.slot = s;
+                    q.state = 1;
+                    q.t_start = Clock::now();
+                    sv->plain_query[g][s] = t;
+                    const g5_status st = g5_bfs_launch(sv->ws[g][s], q.root);
+                    if (st != G5_OK) return fail(st);
+                    plain_run[g][s] = 1;
+                    ++nrun;
+                }
+                const bool have_plain = !sv->plain_query[g].empty();
                 for (int w = 0; w < (int)sv->cohorts[g].size() && !sv->queue[g].empty(); ++w) {
+                    if (have_plain && sv->queue[g].size() < kCohortMin) break;  // wait for a one-root workspace
                     Cohort &c = sv->cohorts[g][w];
                     if (c.state != 0) continue;
                     c.tickets.clear();
@@ -324,6 +351,25 @@ void worker_cohorts(g5_server *sv)
         bool any_done = false;
         for (int g = 0; g < ng; ++g) {
             if (sv->kind[g] != G5_SERVE_COHORTS) continue;
+            for (int s = 0; s < (int)plain_run[g].size(); ++s) {
+                if (!plain_run[g][s]) continue;
+                int done = 0;
+                double ms = 0;
+                const g5_status st = g5_bfs_poll(sv->ws[g][s], &done, &ms);
+                if (!done) continue;
+                plain_run[g][s] = 0;
+                --nrun;
+                any_done = true;
+                std::lock_guard<std::mutex> lk(sv->mu);
+                if (st != G5_OK) return fail(st);
+                sv->steps += 1;
+                sv->device_ms += ms;
+                Query &q = sv->queries[sv->plain_query[g][s]];
+                q.state = sv->keep_results ? 2 : 3;
+                q.t_done = Clock::now();
+                sv->completed += 1;
+                if (!sv->keep_results) sv->plain_query[g][s] = 0;
+            }
             for (Cohort &c : sv->cohorts[g]) {
                 if (c.state != 1) continue;
                 int done = 0;
@@ -408,6 +454,7 @@ g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t me
         if (sv->kind[i] == G5_SERVE_COHORTS) cohort_n += (uint64_t)graphs[i]->n;
     sv->ws.resize(ngraphs);
     sv->cohorts.resize(ngraphs);
+    sv->plain_query.resize(ngraphs);
     sv->pred_base.assign(ngraphs, 0);
     sv->bidx.assign(ngraphs, -1);
     std::vector<g5_graph *> bgraphs;
@@ -454,7 +501,8 @@ g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t me
         const uint64_t n = (uint64_t)graphs[i]->n;
         col_n = std::max(col_n, n);
         const uint64_t gshare = (uint64_t)((double)left * (double)n / (double)cohort_n);
-        const uint64_t fixed = g5::batch_copy_bytes(graphs[i]);
+        const uint64_t per_plain = 48ull * n + (uint64_t)graphs[i]->nnz / 64 + (1u << 20);
+        const uint64_t fixed = g5::batch_copy_bytes(graphs[i]) + kCohortPlain * per_plain;
         const uint64_t per_ws = g5::batch_workspace_bytes(graphs[i]);
         // as many workspaces (up to kCohortWorkspaces) as leave room for at
         // least 8 root slots each, and every workspace the slots that fit
@@ -468,6 +516,13 @@ g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t me
         if (nw < 1 || cap < 1) return fail(G5_ERR_OOM);
         cap = std::min<uint64_t>(64, cap);
         sv->slots[i] = (int)cap * nw;
+        for (int p = 0; p < kCohortPlain; ++p) {
+            g5_bfs *b = nullptr;
+            const g5_status st = g5_bfs_create(graphs[i], &cfg, &b);
+            if (st != G5_OK) return fail(st);
+            sv->ws[i].push_back(b);
+        }
+        sv->plain_query[i].assign(kCohortPlain, 0);
         for (int w = 0; w < nw; ++w) {
             Cohort c;
             c.cap = (int)cap;
@@ -588,7 +643,9 @@ g5_status g5_server_result(g5_server *sv, uint64_t ticket, int64_t *pred_host, d
     if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(q.t_done - q.t_submit).count();
     if (queue_ms) *queue_ms = std::chrono::duration<double, std::milli>(q.t_start - q.t_submit).count();
     g5_status rc = G5_OK;
-    if (q.state == 2 && pred_host && sv->kind[q.graph] == G5_SERVE_STREAMS) {
+    const bool one_root = sv->kind[q.graph] == G5_SERVE_STREAMS ||
+                          (sv->kind[q.graph] == G5_SERVE_COHORTS && q.cohort < 0);
+    if (q.state == 2 && pred_host && one_root) {
         const int64_t n = sv->graphs[q.graph]->n;
         const int64_t *src = nullptr;
         g5_bfs_device_pred(sv->ws[q.graph][q.slot], &src);
@@ -629,7 +686,9 @@ g5_status g5_server_result(g5_server *sv, uint64_t ticket, int64_t *pred_host, d
     if (rc != G5_OK) return rc;
     Query &qq = sv->queries[ticket];
     if (qq.state == 2) {
-        if (sv->kind[qq.graph] == G5_SERVE_COHORTS) {
+        if (sv->kind[qq.graph] == G5_SERVE_COHORTS && qq.cohort < 0) {
+            sv->plain_query[qq.graph][qq.slot] = 0;
+        } else if (sv->kind[qq.graph] == G5_SERVE_COHORTS) {
             Cohort &c = sv->cohorts[qq.graph][qq.cohort];
             if (c.held > 0 && --c.held == 0) c.state = 0;
         } else {

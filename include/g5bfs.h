@@ -339,15 +339,17 @@ g5_status g5_batch_serve_step(g5_batch *bt, const int32_t *adm_graph, const int3
  *     smaller ones by stream workspaces; each kind has its own worker.
  *   mode G5_SERVE_COHORTS: graphs of 2^21 vertices or more are served by
  *     cohorts, the smaller ones by stream workspaces.  A cohort graph holds
- *     up to two batch workspaces (g5_batch, sharing one degree-ordered copy
- *     of the graph); whenever one is free, the graph's queued queries, up to
- *     its root slots (at most 64), start together as one batched search, so
- *     cohorts are small under light load and grow to share each adjacency
- *     read among up to 64 queries under heavy load.  Cohort graphs get the
+ *     two one-root workspaces and up to two batch workspaces (g5_batch,
+ *     sharing one degree-ordered copy of the graph).  While fewer than three
+ *     of its queries wait, they run alone on the one-root workspaces (a lone
+ *     query finishes sooner alone); from three on, whenever a batch
+ *     workspace is free, the queued queries, up to its root slots (at most
+ *     64), start together as one batched search, so under heavy load each
+ *     adjacency read is shared by up to 64 queries.  Cohort graphs get the
  *     budget the other graphs leave, in proportion to their vertex counts
  *     (4 bytes per vertex and root slot, plus the workspaces and the copy).
- *     With keep_results a workspace is reused once every query of its
- *     cohort has been released by g5_server_result.
+ *     With keep_results a workspace is reused once every query on it has
+ *     been released by g5_server_result.
  * Queries beyond the free slots wait in a FIFO per graph (memory-based
  * admission).  keep_results = 0 frees a slot as soon as its query finishes
  * (results are discarded). */
@@ -402,6 +404,21 @@ g5_status g5_codec_encode(g5_codec *c, const uint32_t *in_dev, size_t n, uint32_
 g5_status g5_codec_decode(g5_codec *c, const uint32_t *in_dev, size_t words, uint32_t *out_dev,
                           size_t out_cap, size_t *out_n, int mode, void *stream);
 
+/* Asynchronous forms with the lengths in device memory, for callers that
+ * keep a queue's length on the device (a level loop does) and for capture
+ * in a CUDA graph: nothing is read back and the call returns after
+ * enqueueing.  encode_async: n_dev (device, one uint64, at most the
+ * workspace's max_n, else nothing is written and the workspace status is
+ * G5_ERR_CAPACITY); the stream's words go to out_words_dev (device, one
+ * uint64).  decode_async: words_dev (device) gives the stream's length;
+ * the decoded count goes to out_n_dev (device).  g5_codec_status (a
+ * synchronous read) gives the status of the last call on the workspace. */
+g5_status g5_codec_encode_async(g5_codec *c, const uint32_t *in_dev, const uint64_t *n_dev, uint32_t *out_dev,
+                                uint64_t *out_words_dev, int mode, void *stream);
+g5_status g5_codec_decode_async(g5_codec *c, const uint32_t *in_dev, const uint64_t *words_dev, uint32_t *out_dev,
+                                size_t out_cap, uint64_t *out_n_dev, int mode, void *stream);
+g5_status g5_codec_status(g5_codec *c);
+
 /* Many queues per call, one launch set for all of them (the reference's
  * compress/decompress run once per queue, vreduce.hpp:192-528,
  * globalbfs.hh:853-938; a level's queues or a microbench's queue set go
@@ -435,8 +452,8 @@ g5_status g5_codec_decode_batch(g5_codec *c, const uint32_t *in_dev, const uint6
  * memory: a serving loop that must never block on or fragment the CUDA
  * allocator between requests, or a process whose device memory belongs to
  * another allocator (a framework's caching pool) with nothing left for
- * cudaMalloc.  It needs no g5_codec: its scratch is a fixed array of 57,741
- * bytes (about 56 KiB) in the library's device image, held on every GPU that
+ * cudaMalloc.  It needs no g5_codec: its scratch is a fixed array of 12,608
+ * bytes (about 12 KiB) in the library's device image, held on every GPU that
  * loads the library until the process exits, and it calls no allocating
  * function.  At most 1,048,576 values per call (more gives
  * G5_ERR_CAPACITY).  The first call on a device looks up that device's copy

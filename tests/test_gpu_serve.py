@@ -107,11 +107,13 @@ def test_bad_queries(graphs):
 
 
 def _cohort_bytes(g, slots, workspaces):
-    """Device bytes of a cohort graph: the shared degree-ordered copy, the
-    batch workspaces and 4 bytes per vertex and root slot."""
+    """Device bytes of a cohort graph: the shared degree-ordered copy, two
+    one-root workspaces, the batch workspaces and 4 bytes per vertex and root
+    slot."""
     copy = 28 * g.n + 4 * g.nnz + (1 << 20)
+    plain = 2 * (48 * g.n + g.nnz // 64 + (1 << 20))
     ws = 48 * g.n + g.nnz // 64 + (1 << 20)
-    return copy + workspaces * ws + workspaces * slots * 4 * g.n
+    return copy + plain + workspaces * ws + workspaces * slots * 4 * g.n
 
 
 def test_cohort_admission_and_reuse(graphs):
@@ -134,7 +136,30 @@ def test_cohort_admission_and_reuse(graphs):
             assert np.array_equal(pred[:g.n], want), (rep, int(r))
         assert queued >= 1
     st = sv.stats()
-    assert st["completed"] == 24 and st["steps"] >= 4  # at most 3 queries per cohort
+    assert st["completed"] == 24 and st["steps"] >= 8  # at most 3 queries per search
+    sv.close()
+
+
+def test_cohorts_mixed_with_lone_queries(graphs):
+    """Queries trickling in one at a time run on the one-root workspaces, a
+    burst forms cohorts; all parents equal the oracle's."""
+    g = graphs[2]
+    sv = g5.Server([g], mem_budget=_cohort_bytes(g, 16, 2), modes=[g5.Server.COHORTS])
+    ro, col = g.csr()
+    roots = g5.select_roots(g, 40)
+    got = {}
+    for r in roots[:5]:  # one at a time
+        t = sv.submit(0, int(r))
+        assert sv.wait(t, 60.0)
+        got[int(r)] = sv.result(t)[0]
+    tickets = [(sv.submit(0, int(r)), int(r)) for r in roots[5:]]  # a burst
+    for t, r in tickets:
+        assert sv.wait(t, 60.0)
+        got[r] = sv.result(t)[0]
+    for r, p in got.items():
+        assert np.array_equal(p[:g.n], orc.bfs(ro, col, r)[0]), r
+    st = sv.stats()
+    assert st["completed"] == 40 and st["steps"] < 40  # the burst shared searches
     sv.close()
 
 
