@@ -57,10 +57,13 @@ def parse():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-codec", action="store_true")
-    ap.add_argument("--no-c2", action="store_true", help="skip the scale-22 search with the codec in the level loop")
-    ap.add_argument("--c2-scale", type=int, default=22)
-    ap.add_argument("--big-scale", type=int, default=28,
-                    help="also compare plain and batched search on a second, larger graph (e.g. 28)")
+    ap.add_argument("--no-c2", action="store_true", help="skip the search with the codec in the level loop")
+    ap.add_argument("--c2-scale", type=int, default=-1,
+                    help="scale of the search with the codec in the level loop (default: 22 when --scale is 26, "
+                         "else none; 0: none)")
+    ap.add_argument("--big-scale", type=int, default=-1,
+                    help="also compare plain and batched search on a second, larger graph (default: 28 when "
+                         "--scale is 26, else none; 0: none)")
     ap.add_argument("--serve-rates", default="1000,5000,20000")
     ap.add_argument("--serve-modes", default="streams,cohorts",
                     help="comma list of server slot kinds to measure: streams, levels, auto, cohorts")
@@ -322,6 +325,12 @@ def reference_arm(args):
 
 def main():
     args = parse()
+    # the default workload (scale 26) also runs the scale-28 plain-vs-batched
+    # leg and the scale-22 codec-in-loop leg; other scales only when asked
+    if args.big_scale < 0:
+        args.big_scale = 28 if args.scale == 26 else 0
+    if args.c2_scale < 0:
+        args.c2_scale = 22 if args.scale == 26 else 0
     if args.impl == "reference":
         return reference_arm(args)
     rank, ws, dist = dist_init(args)
@@ -445,7 +454,7 @@ def main():
 
     serve = mixed = codec = c2 = None
     torch.cuda.empty_cache()  # the batched leg's output goes back to the device
-    if rank == 0 and not args.no_c2:
+    if rank == 0 and not args.no_c2 and args.c2_scale:
         c2 = bench_c2(g5, args)
     if rank == 0 and not args.no_serve:
         serve = bench_serve(g5, g, args)
