@@ -713,10 +713,12 @@ __global__ void __launch_bounds__(kOB) k_dec_locate(const uint32_t *__restrict__
                 for (;;) {
                     const uint32_t f = status_flag(vload64(lst + j), epoch);
                     if (f == ST_INC) break;
-                    if (f == ST_AGG) {
-                        --j;  // chunk 0 always publishes an inclusive prefix
+                    if (f == ST_AGG && j > 0) {
+                        --j;
                         continue;
                     }
+                    // not yet published, or chunk 0 (whose inclusive prefix
+                    // always follows its table): wait
                     if (++spins > kSpinLimit) {
                         atomicOr((unsigned long long *)&scal[CS_L_ERR], (unsigned long long)G5_DEVERR_WAIT);
                         bad = true;
