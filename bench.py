@@ -70,6 +70,9 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--profile-batch", action="store_true",
                     help="only the batched search, host-driven with per-kernel CUDA events (for ncu)")
+    ap.add_argument("--profile-codec", action="store_true",
+                    help="only the codec: the largest level queue of one search at --scale, encoded and "
+                         "decoded three times (for ncu)")
     ap.add_argument("--host-loop", action="store_true",
                     help="host-driven level loop (same kernels, one launch each; for ncu, which "
                          "cannot profile kernels inside graphs with conditional nodes)")
@@ -345,6 +348,9 @@ def main():
     from gpugraph500_gb300 import replicas
     roots = replicas.shard_roots(g5.select_roots(g, args.roots * ws), args.roots, rank, ws)
     nr = len(roots)
+    if args.profile_codec:
+        print(json.dumps(profile_codec(g5, torch, g, roots)))
+        return 0
     if args.profile_batch:
         bt = g5.Batch([g])
         out = torch.empty(nr * g.n, dtype=torch.int32, device="cuda")
@@ -797,6 +803,29 @@ def plain_vs_batched(g5, torch, g, args, tune, ab):
     bfs.close()
     return {"plain_hmean_gteps": plain, "plain_mean_ms": statistics.mean(ms), "batched": batched,
             "batched_over_plain": batched["aggregate_gteps"] / plain if plain else None}
+
+
+def profile_codec(g5, torch, g, roots):
+    """The largest level queue of the first root's search, encoded and decoded
+    three times with s4-bp128-d4 (one-stream calls); checks the round trip."""
+    b = g5.CudaBFS(g, want_levels=True)
+    b.runBFS(int(roots[0]))
+    lev = b.getLevels()
+    b.close()
+    L = int(np.bincount(lev[lev >= 0]).argmax())
+    q = np.nonzero(lev == L)[0].astype(np.uint32)
+    n = len(q)
+    c = g5.Codec(n + 256)
+    din = torch.from_numpy(q.view(np.int32)).cuda()
+    dout = torch.zeros(g5.Codec.bound(n) + 64, dtype=torch.int32, device="cuda")
+    back = torch.zeros(n + 256, dtype=torch.int32, device="cuda")
+    w = m = 0
+    for _ in range(3):
+        w = c.encode(din, n, dout, g5.CODEC_D4)
+        m = c.decode(dout, w, back, n + 256, g5.CODEC_D4)
+    ok = m == n and bool(torch.equal(back[:n], din))
+    c.close()
+    return {"profile_codec": {"level": L, "values": n, "words": w, "round_trip": ok}}
 
 
 def bench_c2(g5, args):

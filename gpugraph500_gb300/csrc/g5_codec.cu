@@ -291,7 +291,7 @@ __device__ __forceinline__ void mb_locate(const uint32_t *in, const uint32_t *gp
 
 constexpr int kOB = 512;                 // one-pass blocks: 16 warps, one per miniblock of a group
 constexpr uint32_t kSpinLimit = 1u << 21;
-constexpr int kLocS = 2048;              // stream vectors per locate chunk
+constexpr int kLocS = 16384;             // stream vectors per locate chunk
 constexpr int kEntries = 513;            // a group spans at most 1 + 16 * 32 vectors
 constexpr uint32_t kDead = 0xFFFFu;
 enum : uint32_t { ST_NONE = 0, ST_AGG = 1, ST_INC = 2 };
@@ -489,19 +489,46 @@ __device__ void enc_tail_warp(const uint32_t *in, uint64_t n, uint64_t n1, uint6
 
 // ---- encoder: one pass ----------------------------------------------------------------
 //
-// One tile per group of 16 miniblocks, warp w packing miniblock w: the warp
-// computes its deltas and bit width, the block adds up the group's words
-// (4 header words + 4 b per miniblock), the group's position in the stream is
-// the exclusive prefix of the groups before it (look-back), and every warp
-// packs its miniblock there.  The block with the last group writes the
-// stream header and the VariableByte tail.  n comes from device memory, so
-// the launch can sit in a CUDA graph with a fixed grid.
+// One tile per kTG groups of 16 miniblocks (64 miniblocks), warp w handling
+// miniblocks w, w + 16, w + 32 and w + 48 of the tile: first every warp
+// computes its miniblocks' bit widths (their loads issued together), the
+// block adds up the tile's words (4 header words per group + 4 b per
+// miniblock), the tile's position in the stream is the exclusive prefix of
+// the tiles before it (look-back), then the warps pack their miniblocks there
+// from a second read of the input (the tile's 32 KB are still in L1 / L2).
+// The block with the last group writes the stream header and the
+// VariableByte tail.  n comes from device memory, so the launch can sit in a
+// CUDA graph with a fixed grid.
+constexpr int kTG = 4;               // groups per encoder / unpacker tile
+constexpr int kTM = 16 * kTG;        // miniblocks per tile
+
+// Packs the deltas of one miniblock (already in s_d) with width b at out + po.
+__device__ __forceinline__ void pack_mb(const uint4 (&s_dw)[32], uint32_t b, uint32_t *out, uint64_t po)
+{
+    const int lane = g5_lane();
+    for (uint32_t idx = lane; idx < 4 * b; idx += 32) {
+        const uint32_t w = idx >> 2, l = idx & 3;
+        const uint32_t bit0 = 32 * w;
+        const uint32_t j0 = bit0 / b, j1 = (bit0 + 31) / b;
+        uint32_t word = 0;
+        for (uint32_t j = j0; j <= j1 && j < 32; ++j) {
+            const uint32_t dj = comp(s_dw[j], l);
+            const int sh = (int)(j * b) - (int)bit0;
+            word |= sh >= 0 ? (dj << sh) : (dj >> (-sh));
+        }
+        out[po + idx] = word;
+    }
+}
+
 __global__ void __launch_bounds__(kOB) k_enc1(const uint32_t *__restrict__ in, const uint64_t *n_dev,
                                               uint64_t max_n, uint64_t raw_thr, uint32_t *__restrict__ out,
                                               uint64_t *scal, uint64_t *tst, uint64_t *tagg, uint64_t *tinc, int mode)
 {
     __shared__ uint4 s_d[16][32];
-    __shared__ uint32_t s_b[16];
+    __shared__ uint32_t s_b[kTM];
+    __shared__ uint32_t s_off[kTM];  // payload word offset of each miniblock in the tile
+    __shared__ uint32_t s_goff[kTG]; // header word offset of each group in the tile
+    __shared__ uint32_t s_tw;        // words of the tile
     __shared__ uint64_t s_t, s_excl;
     __shared__ uint32_t s_val[128];
     __shared__ uint32_t s_bytes[(128 * 5 + 3) / 4 + 1];
@@ -510,7 +537,8 @@ __global__ void __launch_bounds__(kOB) k_enc1(const uint32_t *__restrict__ in, c
     const bool too_long = n_in > max_n;  // a device-side length past the workspace: nothing is written
     const uint64_t n = too_long ? 0 : n_in;
     const uint64_t epoch = scal[CS_E_EPOCH];
-    const uint64_t n1 = n / 128 * 128, nmb = n / 128, ntiles = too_long ? 0 : (nmb + 15) / 16;
+    const uint64_t n1 = n / 128 * 128, nmb = n / 128, ngroups = (nmb + 15) / 16;
+    const uint64_t ntiles = too_long ? 0 : (ngroups + kTG - 1) / kTG;
     const bool raw = raw_thr && n <= raw_thr;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         scal[CS_N] = n;
@@ -526,56 +554,71 @@ __global__ void __launch_bounds__(kOB) k_enc1(const uint32_t *__restrict__ in, c
         for (;;) {
             const uint64_t t = claim_tile(&scal[CS_E_CTR], &s_t);
             if (t >= ntiles) break;
-            const uint64_t k = 16 * t + wid;
-            uint4 cur = make_uint4(0, 0, 0, 0), d = make_uint4(0, 0, 0, 0);
-            uint32_t b = 0;
-            if (k < nmb) {
-                uint4 prev;
-                load_vectors(in, k, cur, prev);
-                d = deltas(cur, prev, mode);
-                uint32_t acc = d.x | d.y | d.z | d.w;
+            const uint64_t k0 = (uint64_t)kTM * t;
+            // widths: all of the warp's loads first
+            uint4 cur[kTG], prev[kTG];
 #pragma unroll
-                for (int o = 16; o; o >>= 1) acc |= __shfl_xor_sync(0xFFFFFFFFu, acc, o);
-                b = bits_of(acc);
+            for (int i = 0; i < kTG; ++i) {
+                const uint64_t k = k0 + 16 * i + wid;
+                if (k < nmb) load_vectors(in, k, cur[i], prev[i]);
             }
-            if (lane == 0) s_b[wid] = b;
+#pragma unroll
+            for (int i = 0; i < kTG; ++i) {
+                const uint64_t k = k0 + 16 * i + wid;
+                uint32_t b = 0;
+                if (k < nmb) {
+                    const uint4 d = deltas(cur[i], prev[i], mode);
+                    uint32_t acc = d.x | d.y | d.z | d.w;
+#pragma unroll
+                    for (int o = 16; o; o >>= 1) acc |= __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+                    b = bits_of(acc);
+                }
+                if (lane == 0) s_b[16 * i + wid] = b;
+            }
             __syncthreads();
-            uint32_t off = 4, tw = 4;  // this miniblock's payload offset in the group; group words
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                const uint32_t w4 = 4 * s_b[i];
-                off += i < wid ? w4 : 0u;
-                tw += w4;
+            if (threadIdx.x == 0) {
+                uint32_t o = 0;
+                for (int g = 0; g < kTG; ++g) {
+                    if ((uint64_t)kTG * t + g >= ngroups) break;  // no header past the last group
+                    s_goff[g] = o;
+                    o += 4;
+                    for (int i = 0; i < 16; ++i) {
+                        s_off[16 * g + i] = o;
+                        o += 4 * s_b[16 * g + i];
+                    }
+                }
+                s_tw = o;
             }
+            __syncthreads();
             if (wid == 0) {
-                const uint64_t ex = lookback<SumU64>(tst, tagg, tinc, t, epoch, (uint64_t)tw, &scal[CS_E_ERR]);
+                const uint64_t ex = lookback<SumU64>(tst, tagg, tinc, t, epoch, (uint64_t)s_tw, &scal[CS_E_ERR]);
                 if (lane == 0) s_excl = ex;
             }
             __syncthreads();
-            const uint64_t base = 4 + s_excl;  // word of the group's header (a multiple of 4)
-            if (wid == 0 && lane < 4)
-                out[base + lane] = (s_b[4 * lane] << 24) | (s_b[4 * lane + 1] << 16) | (s_b[4 * lane + 2] << 8) |
-                                   s_b[4 * lane + 3];
-            const uint64_t po = base + off;
-            if (k < nmb && b == 32) {
-                reinterpret_cast<uint4 *>(out + po)[lane] = cur;
-            } else if (k < nmb && b) {
-                s_d[wid][lane] = d;
-                __syncwarp();
-                for (uint32_t idx = lane; idx < 4 * b; idx += 32) {
-                    const uint32_t w = idx >> 2, l = idx & 3;
-                    const uint32_t bit0 = 32 * w;
-                    const uint32_t j0 = bit0 / b, j1 = (bit0 + 31) / b;
-                    uint32_t word = 0;
-                    for (uint32_t j = j0; j <= j1 && j < 32; ++j) {
-                        const uint32_t dj = comp(s_d[wid][j], l);
-                        const int sh = (int)(j * b) - (int)bit0;
-                        word |= sh >= 0 ? (dj << sh) : (dj >> (-sh));
-                    }
-                    out[po + idx] = word;
+            const uint64_t base = 4 + s_excl;  // word of the tile's first header (a multiple of 4)
+            if (wid == 0 && lane < 4 * kTG && (uint64_t)kTG * t + lane / 4 < ngroups) {
+                const int g = lane / 4, q = lane & 3;
+                const uint32_t *bw = s_b + 16 * g + 4 * q;
+                out[base + s_goff[g] + q] = (bw[0] << 24) | (bw[1] << 16) | (bw[2] << 8) | bw[3];
+            }
+#pragma unroll 1
+            for (int i = 0; i < kTG; ++i) {
+                const uint64_t k = k0 + 16 * i + wid;
+                if (k >= nmb) break;
+                const uint32_t b = s_b[16 * i + wid];
+                const uint64_t po = base + s_off[16 * i + wid];
+                uint4 c, pv;
+                load_vectors(in, k, c, pv);
+                if (b == 32) {
+                    reinterpret_cast<uint4 *>(out + po)[lane] = c;
+                } else if (b) {
+                    s_d[wid][lane] = deltas(c, pv, mode);
+                    __syncwarp();
+                    pack_mb(s_d[wid], b, out, po);
+                    __syncwarp();
                 }
             }
-            if (t == ntiles - 1 && wid == 1) enc_tail_warp(in, n, n1, base + tw, out, scal, s_val, s_bytes);
+            if (t == ntiles - 1 && wid == 1) enc_tail_warp(in, n, n1, base + s_tw, out, scal, s_val, s_bytes);
         }
         if (too_long && blockIdx.x == 0 && threadIdx.x == 0)
             atomicOr((unsigned long long *)&scal[CS_E_ERR], (unsigned long long)G5_DEVERR_CAPACITY);
@@ -826,22 +869,94 @@ __global__ void __launch_bounds__(kOB) k_dec_locate(const uint32_t *__restrict__
 
 // ---- decoder: unpack (one pass) --------------------------------------------------------
 //
-// One tile per group, warp w unpacking miniblock w at the position the
-// locator found: the warp's lane sums (or, for a raw b = 32 miniblock, its
-// last vector with a reset flag) are the miniblock's aggregate, the group's
-// aggregate goes through the look-back, and each warp adds the prefix of
-// everything before its miniblock to its deltas.  Block 0 first decodes the
-// VariableByte tail, which starts from 0 whatever the block part holds.
-// With `expect` every value is compared with the expected one (the level
-// loop's round-trip check); `acc` accumulates words and values.
+// One tile per kTG groups, warp w unpacking miniblocks w, w + 16, w + 32 and
+// w + 48 of the tile at the positions the locator found: first every warp
+// unpacks its miniblocks and forms their aggregates (the lane sums, or for a
+// raw b = 32 miniblock its last vector with a reset flag), the tile's
+// aggregate goes through the look-back, then each warp unpacks its
+// miniblocks again (from L1 / L2) and adds the prefix of everything before
+// them.  Block 0 first decodes the VariableByte tail, which starts from 0
+// whatever the block part holds.  With `expect` every value is compared with
+// the expected one (the level loop's round-trip check); `acc` accumulates
+// words and values.
+
+// Stream position (16-byte vectors) and width of miniblock i of the group
+// whose header is at vector p.
+__device__ __forceinline__ void mb_at(const uint32_t *in, uint32_t p, int i, uint64_t &off, uint32_t &b)
+{
+    const uint4 hv = reinterpret_cast<const uint4 *>(in)[p];
+    uint64_t o = (uint64_t)p + 1;
+    for (int q = 0; q < i; ++q) o += width_of(hv, q);
+    off = o;
+    b = width_of(hv, i);
+}
+
+__device__ __forceinline__ VecFlag mb_aggregate(const uint4 &d, uint32_t b, int mode)
+{
+    VecFlag r;
+    if (b == 32) {
+        r.v.x = __shfl_sync(0xFFFFFFFFu, d.x, 31);
+        r.v.y = __shfl_sync(0xFFFFFFFFu, d.y, 31);
+        r.v.z = __shfl_sync(0xFFFFFFFFu, d.z, 31);
+        r.v.w = __shfl_sync(0xFFFFFFFFu, d.w, 31);
+        r.f = 1;
+        return r;
+    }
+    uint32_t sx = d.x, sy = d.y, sz = d.z, sw = d.w;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        sx += __shfl_xor_sync(0xFFFFFFFFu, sx, o);
+        sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
+        sz += __shfl_xor_sync(0xFFFFFFFFu, sz, o);
+        sw += __shfl_xor_sync(0xFFFFFFFFu, sw, o);
+    }
+    r.v = mode == G5_CODEC_DM ? make_uint4(sw, sw, sw, sw) : make_uint4(sx, sy, sz, sw);
+    r.f = 0;
+    return r;
+}
+
+// Absolute values of a miniblock from its deltas (or raw vector) and base.
+__device__ __forceinline__ uint4 mb_values(const uint4 &d, uint32_t b, const uint4 &base, int mode)
+{
+    const int lane = g5_lane();
+    if (b == 32) return d;
+    if (mode == G5_CODEC_DM) {
+        uint32_t c = d.w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, c, o);
+            if (lane >= o) c += y;
+        }
+        c += base.w;
+        uint32_t pc = __shfl_up_sync(0xFFFFFFFFu, c, 1);
+        if (lane == 0) pc = base.w;
+        return make_uint4(d.x + pc, d.y + pc, d.z + pc, c);
+    }
+    uint32_t cx = d.x, cy = d.y, cz = d.z, cw = d.w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t yx = __shfl_up_sync(0xFFFFFFFFu, cx, o);
+        const uint32_t yy = __shfl_up_sync(0xFFFFFFFFu, cy, o);
+        const uint32_t yz = __shfl_up_sync(0xFFFFFFFFu, cz, o);
+        const uint32_t yw = __shfl_up_sync(0xFFFFFFFFu, cw, o);
+        if (lane >= o) {
+            cx += yx;
+            cy += yy;
+            cz += yz;
+            cw += yw;
+        }
+    }
+    return make_uint4(cx + base.x, cy + base.y, cz + base.z, cw + base.w);
+}
+
 __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__ in, uint64_t *scal,
                                                     const uint32_t *__restrict__ gpos, uint32_t *__restrict__ out,
                                                     uint64_t cap, const uint64_t *n_expect,
                                                     const uint32_t *__restrict__ expect, uint64_t *acc,
                                                     uint64_t *ust, VecFlag *uagg, VecFlag *uinc, int mode)
 {
-    __shared__ VecFlag s_vf[16];
-    __shared__ VecFlag s_base[16];
+    __shared__ VecFlag s_vf[kTM];
+    __shared__ VecFlag s_base[kTM];
     __shared__ uint64_t s_t;
     __shared__ uint32_t s_b[kTailMaxBytes / 4];
     const int lane = g5_lane(), wid = threadIdx.x >> 5;
@@ -857,7 +972,8 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
                 bad |= expect && expect[i] != in[i];
             }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
-            if (n_expect && n != *n_expect) atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_MISMATCH);
+            if (n_expect && n != *n_expect)
+                atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_MISMATCH);
             if (acc) {
                 acc[0] += words;
                 acc[1] += n;
@@ -865,6 +981,7 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
         }
     } else if (!err0) {
         const uint64_t nmb = scal[CS_NMB], ng = scal[CS_NG], n1 = scal[CS_N1];
+        const uint64_t ntiles = (ng + kTG - 1) / kTG;
         if (blockIdx.x == 0 && wid == 0) {
             // VariableByte tail (variablebyte.h:217-): words after the block part
             const uint64_t blkend = scal[CS_BLKEND];
@@ -913,85 +1030,51 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
         }
         for (;;) {
             const uint64_t t = claim_tile(&scal[CS_U_CTR], &s_t);
-            if (t >= ng) break;
-            const uint64_t k = 16 * t + wid;
-            uint4 d = make_uint4(0, 0, 0, 0);
-            uint32_t b = 0;
-            VecFlag mine = ResetAdd::id();
-            if (k < nmb) {
-                const uint32_t p = gpos[t];
-                const uint4 hv = reinterpret_cast<const uint4 *>(in)[p];
-                uint64_t off = (uint64_t)p + 1;
-                for (int i = 0; i < wid; ++i) off += width_of(hv, i);
-                b = width_of(hv, wid);
-                d = unpack_vec(in, off, b);
-                if (b == 32) {
-                    mine.v.x = __shfl_sync(0xFFFFFFFFu, d.x, 31);
-                    mine.v.y = __shfl_sync(0xFFFFFFFFu, d.y, 31);
-                    mine.v.z = __shfl_sync(0xFFFFFFFFu, d.z, 31);
-                    mine.v.w = __shfl_sync(0xFFFFFFFFu, d.w, 31);
-                    mine.f = 1;
-                } else {
-                    uint32_t sx = d.x, sy = d.y, sz = d.z, sw = d.w;
+            if (t >= ntiles) break;
+            const uint64_t k0 = (uint64_t)kTM * t;
+            // aggregates: the warp's positions and loads first
+            uint4 d[kTG];
+            uint32_t b[kTG];
 #pragma unroll
-                    for (int o = 16; o; o >>= 1) {
-                        sx += __shfl_xor_sync(0xFFFFFFFFu, sx, o);
-                        sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
-                        sz += __shfl_xor_sync(0xFFFFFFFFu, sz, o);
-                        sw += __shfl_xor_sync(0xFFFFFFFFu, sw, o);
-                    }
-                    mine.v = mode == G5_CODEC_DM ? make_uint4(sw, sw, sw, sw) : make_uint4(sx, sy, sz, sw);
-                    mine.f = 0;
+            for (int i = 0; i < kTG; ++i) {
+                const uint64_t k = k0 + 16 * i + wid;
+                d[i] = make_uint4(0, 0, 0, 0);
+                b[i] = 0;
+                if (k < nmb) {
+                    uint64_t off;
+                    mb_at(in, gpos[k / 16], wid, off, b[i]);
+                    d[i] = unpack_vec(in, off, b[i]);
                 }
             }
-            if (lane == 0) s_vf[wid] = mine;
+#pragma unroll
+            for (int i = 0; i < kTG; ++i) {
+                const uint64_t k = k0 + 16 * i + wid;
+                const VecFlag m = k < nmb ? mb_aggregate(d[i], b[i], mode) : ResetAdd::id();
+                if (lane == 0) s_vf[16 * i + wid] = m;
+            }
             __syncthreads();
             if (wid == 0) {
                 VecFlag tile = ResetAdd::id();
-                for (int i = 0; i < 16; ++i) tile = ResetAdd::op(tile, s_vf[i]);
+                for (int i = 0; i < kTM; ++i) tile = ResetAdd::op(tile, s_vf[i]);
                 const VecFlag ex = lookback<ResetAddV>(ust, uagg, uinc, t, epoch, tile, &scal[CS_ERR]);
                 if (lane == 0) {
                     VecFlag run = ex;
-                    for (int i = 0; i < 16; ++i) {
+                    for (int i = 0; i < kTM; ++i) {
                         s_base[i] = run;
                         run = ResetAdd::op(run, s_vf[i]);
                     }
                 }
             }
             __syncthreads();
-            if (k < nmb) {
-                const uint4 base = s_base[wid].v;
-                uint4 x;
-                if (b == 32) {
-                    x = d;
-                } else if (mode == G5_CODEC_DM) {
-                    uint32_t c = d.w;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, c, o);
-                        if (lane >= o) c += y;
-                    }
-                    c += base.w;
-                    uint32_t pc = __shfl_up_sync(0xFFFFFFFFu, c, 1);
-                    if (lane == 0) pc = base.w;
-                    x = make_uint4(d.x + pc, d.y + pc, d.z + pc, c);
-                } else {
-                    uint32_t cx = d.x, cy = d.y, cz = d.z, cw = d.w;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint32_t yx = __shfl_up_sync(0xFFFFFFFFu, cx, o);
-                        const uint32_t yy = __shfl_up_sync(0xFFFFFFFFu, cy, o);
-                        const uint32_t yz = __shfl_up_sync(0xFFFFFFFFu, cz, o);
-                        const uint32_t yw = __shfl_up_sync(0xFFFFFFFFu, cw, o);
-                        if (lane >= o) {
-                            cx += yx;
-                            cy += yy;
-                            cz += yz;
-                            cw += yw;
-                        }
-                    }
-                    x = make_uint4(cx + base.x, cy + base.y, cz + base.z, cw + base.w);
-                }
+#pragma unroll 1
+            for (int i = 0; i < kTG; ++i) {
+                const uint64_t k = k0 + 16 * i + wid;
+                if (k >= nmb) break;
+                uint64_t off;
+                uint32_t bi;
+                mb_at(in, gpos[k / 16], wid, off, bi);
+                const uint4 dd = unpack_vec(in, off, bi);
+                const uint4 x = mb_values(dd, bi, s_base[16 * i + wid].v, mode);
                 reinterpret_cast<uint4 *>(out)[k * 32 + lane] = x;
                 if (expect) {
                     const uint4 e = reinterpret_cast<const uint4 *>(expect)[k * 32 + lane];
