@@ -112,6 +112,7 @@ SIGNATURES = {
     "g5_server_create": (_I, [_P, _I, _SZ, _I, _I, C.POINTER(_P)]),
     "g5_server_create_modes": (_I, [_P, _I, _SZ, _I, _P, C.POINTER(_P)]),
     "g5_server_slots": (_I, [_P, _P]),
+    "g5_server_cohort_policy": (_I, [_P, _I, C.c_double]),
     "g5_server_submit": (_I, [_P, _I, _I64, C.POINTER(_U64)]),
     "g5_server_wait": (_I, [_P, _U64, C.c_double, C.POINTER(_I)]),
     "g5_server_result": (_I, [_P, _U64, _P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -616,6 +617,10 @@ class Server:
             _check(lib().g5_server_create(arr, len(self.graphs), int(mem_budget), int(keep_results), int(mode),
                                           C.byref(h)), "g5_server_create")
         self._h = h
+
+    def cohort_policy(self, min_roots: int, max_wait_ms: float) -> None:
+        """Cohort graphs: start a cohort at min_roots waiting queries or after max_wait_ms."""
+        _check(lib().g5_server_cohort_policy(self._h, int(min_roots), float(max_wait_ms)), "g5_server_cohort_policy")
 
     def slots(self) -> list:
         out = np.zeros(len(self.graphs), np.int32)

@@ -53,7 +53,15 @@ constexpr int64_t kAutoLevelsVertices = int64_t(1) << 25;
 constexpr int64_t kCohortVertices = int64_t(1) << 21;
 constexpr int kCohortWorkspaces = 2;  // batch workspaces per cohort graph
 constexpr int kCohortPlain = 2;       // one-root workspaces per cohort graph
-constexpr size_t kCohortMin = 3;      // queued queries that start a cohort while a one-root workspace is free
+// Cohort policy (defaults; g5_server_cohort_policy changes them): a batched
+// search of a few roots costs several one-root searches (at scale 26 one
+// root alone takes 4x, 16 roots 13x, 64 roots 17x a one-root search), so a
+// cohort starts once kCohortMin queries wait or the oldest has waited
+// kCohortWaitMs; a query runs alone on a one-root workspace while fewer than
+// kPlainMax wait and no cohort of its graph is running.
+constexpr int kCohortMinDefault = 16;
+constexpr double kCohortWaitMsDefault = 10.0;
+constexpr size_t kPlainMax = 4;
 
 // One batch workspace of a cohort graph and the queries it runs.
 struct Cohort {
@@ -88,6 +96,8 @@ struct g5_server {
     std::vector<std::vector<g5_bfs *>> ws;  // streams mode: workspaces per graph
     std::vector<std::vector<Cohort>> cohorts;  // cohort graphs: batch workspaces
     std::vector<std::vector<uint64_t>> plain_query;  // cohort graphs: ticket per one-root workspace (0 free)
+    int cohort_min = kCohortMinDefault;      // queued queries that start a cohort at once
+    double cohort_wait_ms = kCohortWaitMsDefault;  // ... or the oldest query's wait that does
     uint32_t *col_buf = nullptr;          // one root's uint32 parents, gathered for a result
     std::vector<uint32_t> col_host;
     std::mutex result_mu;                 // guards col_buf / col_host
@@ -298,11 +308,13 @@ void worker_cohorts(g5_server *sv)
             std::unique_lock<std::mutex> lk(sv->mu);
             for (int g = 0; g < ng; ++g) {
                 if (sv->kind[g] != G5_SERVE_COHORTS) continue;
-                // a short queue runs on one-root workspaces (a lone query
-                // finishes sooner alone than as a batch); a longer one, or one
-                // with no such workspace free, starts a cohort
+                // a short queue runs on one-root workspaces while no cohort
+                // of the graph runs (a lone query finishes sooner alone than
+                // as a batch); otherwise queries gather into cohorts
+                bool cohort_running = false;
+                for (const Cohort &c : sv->cohorts[g]) cohort_running |= c.state == 1;
                 for (int s = 0; s < (int)sv->plain_query[g].size(); ++s) {
-                    if (sv->queue[g].empty() || sv->queue[g].size() >= kCohortMin) break;
+                    if (sv->queue[g].empty() || sv->queue[g].size() >= kPlainMax || cohort_running) break;
                     if (sv->plain_query[g][s] != 0) continue;
                     const uint64_t t = sv->queue[g].front();
                     sv->queue[g].pop_front();
@@ -317,9 +329,14 @@ void worker_cohorts(g5_server *sv)
                     plain_run[g][s] = 1;
                     ++nrun;
                 }
-                const bool have_plain = !sv->plain_query[g].empty();
-                for (int w = 0; w < (int)sv->cohorts[g].size() && !sv->queue[g].empty(); ++w) {
-                    if (have_plain && sv->queue[g].size() < kCohortMin) break;  // wait for a one-root workspace
+                bool start = !sv->queue[g].empty();
+                if (start && (int)sv->queue[g].size() < sv->cohort_min) {
+                    // too few to share well: wait for more, up to the oldest's deadline
+                    const Query &oldest = sv->queries[sv->queue[g].front()];
+                    const double waited = std::chrono::duration<double, std::milli>(Clock::now() - oldest.t_submit).count();
+                    start = waited >= sv->cohort_wait_ms;
+                }
+                for (int w = 0; w < (int)sv->cohorts[g].size() && start && !sv->queue[g].empty(); ++w) {
                     Cohort &c = sv->cohorts[g][w];
                     if (c.state != 0) continue;
                     c.tickets.clear();
@@ -588,6 +605,16 @@ g5_status g5_server_create(g5_graph *const *graphs, int ngraphs, size_t mem_budg
     g5_status st = g5_server_create_modes(graphs, ngraphs, mem_budget, keep_results, modes.data(), out);
     if (st == G5_OK) (*out)->mode = mode;
     return st;
+}
+
+g5_status g5_server_cohort_policy(g5_server *sv, int min_roots, double max_wait_ms)
+{
+    if (!sv || min_roots < 1 || min_roots > 64 || !(max_wait_ms >= 0)) return G5_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->cohort_min = min_roots;
+    sv->cohort_wait_ms = max_wait_ms;
+    sv->cv_work.notify_all();
+    return G5_OK;
 }
 
 g5_status g5_server_slots(g5_server *sv, int *slots)
