@@ -291,7 +291,6 @@ __device__ __forceinline__ void mb_locate(const uint32_t *in, const uint32_t *gp
 
 constexpr int kOB = 512;                 // one-pass blocks: 16 warps, one per miniblock of a group
 constexpr uint32_t kSpinLimit = 1u << 21;
-constexpr int kLocS = 16384;             // stream vectors per locate chunk
 constexpr int kEntries = 513;            // a group spans at most 1 + 16 * 32 vectors
 constexpr uint32_t kDead = 0xFFFFu;
 enum : uint32_t { ST_NONE = 0, ST_AGG = 1, ST_INC = 2 };
@@ -299,7 +298,7 @@ enum : uint32_t { ST_NONE = 0, ST_AGG = 1, ST_INC = 2 };
 // scalar slots of the one-pass kernels (the scalar block holds kScalars)
 enum {
     CS_E_CTR = 16, CS_E_DONE = 17, CS_E_EPOCH = 18, CS_E_ERR = 19,
-    CS_L_CTR = 20, CS_L_DONE = 21, CS_L_EPOCH = 22, CS_L_ERR = 23, CS_L_LAST = 24,
+    CS_L_CTR = 20, CS_L_DONE = 21, CS_L_EPOCH = 22,
     CS_U_CTR = 25, CS_U_DONE = 26, CS_U_EPOCH = 27
 };
 
@@ -525,6 +524,7 @@ __global__ void __launch_bounds__(kOB) k_enc1(const uint32_t *__restrict__ in, c
                                               uint64_t *scal, uint64_t *tst, uint64_t *tagg, uint64_t *tinc, int mode)
 {
     __shared__ uint4 s_d[16][32];
+    __shared__ __align__(16) uint32_t s_out[kTG * (4 + 16 * 128)];  // the tile's words, packed before its place is known
     __shared__ uint32_t s_b[kTM];
     __shared__ uint32_t s_off[kTM];  // payload word offset of each miniblock in the tile
     __shared__ uint32_t s_goff[kTG]; // header word offset of each group in the tile
@@ -590,33 +590,41 @@ __global__ void __launch_bounds__(kOB) k_enc1(const uint32_t *__restrict__ in, c
                 s_tw = o;
             }
             __syncthreads();
+            // warp 0 finds the tile's place (look-back) first, so that later
+            // tiles see its aggregate early; the other warps pack meanwhile
+            // into shared memory, the tile's words relative to its start
             if (wid == 0) {
                 const uint64_t ex = lookback<SumU64>(tst, tagg, tinc, t, epoch, (uint64_t)s_tw, &scal[CS_E_ERR]);
                 if (lane == 0) s_excl = ex;
-            }
-            __syncthreads();
-            const uint64_t base = 4 + s_excl;  // word of the tile's first header (a multiple of 4)
-            if (wid == 0 && lane < 4 * kTG && (uint64_t)kTG * t + lane / 4 < ngroups) {
-                const int g = lane / 4, q = lane & 3;
-                const uint32_t *bw = s_b + 16 * g + 4 * q;
-                out[base + s_goff[g] + q] = (bw[0] << 24) | (bw[1] << 16) | (bw[2] << 8) | bw[3];
+                if (lane < 4 * kTG && (uint64_t)kTG * t + lane / 4 < ngroups) {
+                    const int g = lane / 4, q = lane & 3;
+                    const uint32_t *bw = s_b + 16 * g + 4 * q;
+                    s_out[s_goff[g] + q] = (bw[0] << 24) | (bw[1] << 16) | (bw[2] << 8) | bw[3];
+                }
             }
 #pragma unroll 1
             for (int i = 0; i < kTG; ++i) {
                 const uint64_t k = k0 + 16 * i + wid;
                 if (k >= nmb) break;
                 const uint32_t b = s_b[16 * i + wid];
-                const uint64_t po = base + s_off[16 * i + wid];
+                const uint32_t po = s_off[16 * i + wid];
                 uint4 c, pv;
                 load_vectors(in, k, c, pv);
                 if (b == 32) {
-                    reinterpret_cast<uint4 *>(out + po)[lane] = c;
+                    reinterpret_cast<uint4 *>(s_out + po)[lane] = c;
                 } else if (b) {
                     s_d[wid][lane] = deltas(c, pv, mode);
                     __syncwarp();
-                    pack_mb(s_d[wid], b, out, po);
+                    pack_mb(s_d[wid], b, s_out, po);
                     __syncwarp();
                 }
+            }
+            __syncthreads();
+            const uint64_t base = 4 + s_excl;  // word of the tile's first header (a multiple of 4)
+            {
+                uint4 *dst = reinterpret_cast<uint4 *>(out + base);
+                const uint4 *src = reinterpret_cast<const uint4 *>(s_out);
+                for (uint32_t i = threadIdx.x; i < s_tw / 4; i += kOB) dst[i] = src[i];
             }
             if (t == ntiles - 1 && wid == 1) enc_tail_warp(in, n, n1, base + s_tw, out, scal, s_val, s_bytes);
         }
@@ -635,22 +643,24 @@ __global__ void __launch_bounds__(kOB) k_enc1(const uint32_t *__restrict__ in, c
     }
 }
 
-// ---- decoder: locate groups (one pass) -------------------------------------------------
+// ---- decoder: locate groups ----------------------------------------------------------
 //
 // A group's position is only given by the chain of group headers before it
 // (each says how long its group is).  The stream's vectors are cut into
-// chunks of kLocS; a chunk's first group starts somewhere in its first
-// kEntries vectors (a group spans at most that many), so the block of a
-// chunk follows the chain inside the chunk (in shared memory) from every one
-// of those entries and publishes, per entry, where the chain leaves the
-// chunk and how many groups it started: the chunk's transfer table, its
-// look-back aggregate.  Its real entry comes from the nearest chunk before
-// it that knows its own (its inclusive prefix: the next chunk's entry and
-// the groups before it), carried forward through the tables in between.
-// Then the block writes its groups' positions.  Chains through vectors that
-// cannot be headers (a width above 32, a group running past the stream) are
-// marked dead; a real chain that reaches one before the last group makes
-// the stream corrupt.
+// chunks of S (a power of two from kLocMin to kLocMax, chosen so that there
+// are at most kLocFit chunks); a chunk's first group starts somewhere in its
+// first kEntries vectors (a group spans at most that many).
+//   k_loc_tables  (one block per chunk) follows the chain inside the chunk
+//                 from every possible entry and writes, per entry, where the
+//                 chain leaves the chunk and how many groups it started (the
+//                 chunk's transfer table), and each vector's jump
+//   k_loc_walk    (one block) carries the real entry from chunk to chunk
+//                 through the tables, held in shared memory
+//   k_loc_pos     (one block per chunk) follows the chain from the chunk's
+//                 real entry and writes its groups' positions
+// Chains through vectors that cannot be headers (a width above 32, a group
+// running past the stream) are marked dead; a real chain that reaches one
+// before the last group makes the stream corrupt.
 
 // Header checks every block makes alike; false if the stream is raw or bad.
 struct DecHead {
@@ -694,36 +704,48 @@ __device__ __forceinline__ uint32_t width_of(uint4 h, int i)
     return (w >> (24 - 8 * (i & 3))) & 0xFFu;
 }
 
-__global__ void __launch_bounds__(kOB) k_dec_locate(const uint32_t *__restrict__ in, const uint64_t *words_dev,
+constexpr int kLocMin = 2048, kLocMax = 16384;  // chunk sizes in vectors
+constexpr int kLocFit = 96;                     // chunks whose tables the walk holds in shared memory
+constexpr int kWalkThreads = 1024;
+
+// Chunk size for a stream of nv vectors (the same in all three kernels).
+__device__ __forceinline__ uint32_t loc_chunk(uint64_t nv)
+{
+    uint32_t S = kLocMin;
+    while (S < kLocMax && (nv + S - 1) / S > (uint64_t)kLocFit) S <<= 1;
+    return S;
+}
+
+__global__ void __launch_bounds__(kOB) k_loc_tables(const uint32_t *__restrict__ in, const uint64_t *words_dev,
                                                     uint64_t cap, uint64_t raw_thr, const uint64_t *n_expect,
                                                     uint64_t *scal, uint64_t max_vec, uint64_t max_mb,
-                                                    uint32_t *ltab, uint64_t *lst, uint64_t *lpay, uint32_t *gpos)
+                                                    uint32_t *ltab, uint16_t *ljump)
 {
-    __shared__ uint16_t s_j[kLocS];
+    __shared__ uint16_t s_j[kLocMax];
     __shared__ uint64_t s_t;
-    __shared__ uint32_t s_entry, s_own, s_bad;
-    __shared__ uint64_t s_gbase;
-    const uint64_t epoch = scal[CS_L_EPOCH];
     const DecHead h = dec_head(in, words_dev, cap, raw_thr, n_expect, max_vec, max_mb);
-    const uint64_t nchunks = (h.raw || h.bad || h.ng == 0) ? 0 : (h.nv - 1 + kLocS - 1) / kLocS;
+    const uint32_t S = loc_chunk(h.nv);
+    const uint64_t nchunks = (h.raw || h.bad || h.ng == 0) ? 0 : (h.nv - 1 + S - 1) / S;
+    const uint64_t epoch = scal[CS_L_EPOCH];
     for (;;) {
         const uint64_t c = claim_tile(&scal[CS_L_CTR], &s_t);
         if (c >= nchunks) break;
-        const uint64_t a = 1 + c * kLocS;  // first vector of the chunk
+        const uint64_t a = 1 + c * S;  // first vector of the chunk
         const uint4 *v = reinterpret_cast<const uint4 *>(in);
-        for (uint32_t p = threadIdx.x; p < kLocS; p += kOB) {
+        for (uint32_t p = threadIdx.x; p < S; p += kOB) {
             uint32_t r = kDead;
             if (a + p < h.nv) {
                 const uint4 hv = v[a + p];
-                uint32_t s = 0;
+                uint32_t sum = 0;
                 bool ok = true;
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
                     const uint32_t b = width_of(hv, i);
                     ok &= b <= 32;
-                    s += b;
+                    sum += b;
                 }
-                if (ok && a + p + 1 + s <= h.nv) r = p + 1 + s;  // <= kLocS + 512 < kDead
+                if (ok && a + p + 1 + sum <= h.nv) r = p + 1 + sum;  // <= S + 512 < kDead
+                ljump[a + p] = (uint16_t)r;
             }
             s_j[p] = (uint16_t)r;
         }
@@ -732,138 +754,125 @@ __global__ void __launch_bounds__(kOB) k_dec_locate(const uint32_t *__restrict__
         for (uint32_t e = threadIdx.x; e < kEntries; e += kOB) {
             uint32_t p = e, cnt = 0, exit = kDead;
             if (a + e < h.nv) {
-                while (p < kLocS) {
+                while (p < S) {
                     const uint32_t r = s_j[p];
                     ++cnt;  // a group starts at p
                     if (r == kDead) break;
                     p = r;
                 }
-                if (p >= kLocS) exit = p - kLocS;
+                if (p >= S) exit = p - S;
                 else --cnt;  // the dead header starts no group
             }
             ltab[c * kEntries + e] = (exit << 16) | cnt;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            vstore64(lst + c, (epoch << 2) | ST_AGG);
-            // the chunk's real entry and the groups before it
-            uint64_t E = 1, G = 0;
-            bool bad = false;
-            if (c > 0) {
-                int64_t j = (int64_t)c - 1;
-                uint32_t spins = 0;
-                for (;;) {
-                    const uint32_t f = status_flag(vload64(lst + j), epoch);
-                    if (f == ST_INC) break;
-                    if (f == ST_AGG && j > 0) {
-                        --j;
-                        continue;
-                    }
-                    // not yet published, or chunk 0 (whose inclusive prefix
-                    // always follows its table): wait
-                    if (++spins > kSpinLimit) {
-                        atomicOr((unsigned long long *)&scal[CS_L_ERR], (unsigned long long)G5_DEVERR_WAIT);
-                        bad = true;
-                        break;
-                    }
-                    __nanosleep(32);
-                }
-                __threadfence();
-                if (!bad) {
-                    const uint64_t pay = vload64(lpay + j);
-                    E = pay & 0xFFFFFFFFull;
-                    G = pay >> 32;
-                    for (uint64_t i = (uint64_t)j + 1; i < c && G < h.ng; ++i) {
-                        const uint64_t ai = 1 + i * kLocS;
-                        if (E < ai || E - ai >= kEntries) {
-                            bad = true;
-                            break;
-                        }
-                        const uint32_t tv = vload32(ltab + i * kEntries + (E - ai));
-                        G += tv & 0xFFFFu;
-                        if (G >= h.ng) break;
-                        if ((tv >> 16) == kDead) {
-                            bad = true;
-                            break;
-                        }
-                        E = ai + kLocS + (tv >> 16);
-                    }
-                }
-            }
-            if (G > h.ng) G = h.ng;
-            // this chunk's own step
-            uint64_t En = 0, Gn = h.ng;
-            uint32_t own = 0;
-            if (!bad && G < h.ng) {
-                if (E < a || E - a >= kEntries) {
-                    bad = true;
-                } else {
-                    const uint32_t tv = ltab[c * kEntries + (E - a)];
-                    const uint64_t cnt = tv & 0xFFFFu;
-                    own = (uint32_t)(G + cnt >= h.ng ? h.ng - G : cnt);
-                    Gn = G + own;
-                    if (Gn < h.ng) {
-                        if ((tv >> 16) == kDead) bad = true;
-                        else En = a + kLocS + (tv >> 16);
-                    }
-                }
-            }
-            if (bad) Gn = h.ng;  // successors own nothing
-            vstore64(lpay + c, (Gn << 32) | (En & 0xFFFFFFFFull));
-            __threadfence();
-            vstore64(lst + c, (epoch << 2) | ST_INC);
-            s_entry = (uint32_t)(E - a);
-            s_gbase = G;
-            s_own = bad ? 0 : own;
-            s_bad = bad;
-            if (bad) atomicOr((unsigned long long *)&scal[CS_L_ERR], (unsigned long long)G5_DEVERR_CORRUPT);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0 && s_own) {
-            uint32_t p = s_entry;
-            for (uint32_t i = 0; i < s_own; ++i) {
-                const uint64_t g = s_gbase + i;
-                gpos[g] = (uint32_t)(a + p);
-                if (g == h.ng - 1) {
-                    // the last group holds only the remaining miniblocks
-                    const uint4 hv = v[a + p];
-                    const uint64_t howmany = h.nmb - 16 * g;
-                    uint64_t s = 0;
-                    bool ok = true;
-                    for (uint64_t q = 0; q < howmany; ++q) {
-                        const uint32_t b = width_of(hv, (int)q);
-                        ok &= b <= 32;
-                        s += b;
-                    }
-                    const uint64_t end = a + p + 1 + s;
-                    if (!ok || end > h.nv) {
-                        atomicOr((unsigned long long *)&scal[CS_L_ERR], (unsigned long long)G5_DEVERR_CORRUPT);
-                    } else {
-                        scal[CS_BLKEND] = 4 * end;
-                        scal[CS_L_LAST] = epoch;  // the last group was found
-                    }
-                }
-                p = s_j[p];
-            }
-        }
     }
     if (last_block(&scal[CS_L_DONE])) {
-        uint64_t err = scal[CS_L_ERR] | (h.bad ? G5_DEVERR_CORRUPT : 0);
-        if (!h.raw && !h.bad && h.ng > 0 && scal[CS_L_LAST] != epoch) err |= G5_DEVERR_CORRUPT;
-        if (!h.raw && h.ng == 0) scal[CS_BLKEND] = 4;
-        scal[CS_ERR] = err;
-        scal[CS_WORDS] = h.words;
-        scal[CS_RAW] = h.raw ? 1 : 0;
-        scal[CS_N1] = h.n1;
-        scal[CS_NMB] = h.nmb;
-        scal[CS_NG] = h.ng;
-        scal[CS_N] = h.raw ? h.words : 0;
-        scal[CS_L_ERR] = 0;
         scal[CS_L_CTR] = 0;
         scal[CS_L_DONE] = 0;
         scal[CS_L_EPOCH] = epoch + 1;
         __threadfence();
+    }
+}
+
+// One block: the real entry E_c and groups before it G_c of every chunk,
+// chained through the tables (in shared memory when they fit); writes
+// lent[c] = E_c | G_c << 32 and the stream's scalars.
+__global__ void __launch_bounds__(kWalkThreads) k_loc_walk(const uint32_t *__restrict__ in, const uint64_t *words_dev,
+                                                           uint64_t cap, uint64_t raw_thr, const uint64_t *n_expect,
+                                                           uint64_t *scal, uint64_t max_vec, uint64_t max_mb,
+                                                           const uint32_t *ltab, uint64_t *lent)
+{
+    extern __shared__ uint32_t s_tab[];
+    const DecHead h = dec_head(in, words_dev, cap, raw_thr, n_expect, max_vec, max_mb);
+    const uint32_t S = loc_chunk(h.nv);
+    const uint64_t nchunks = (h.raw || h.bad || h.ng == 0) ? 0 : (h.nv - 1 + S - 1) / S;
+    const bool fit = nchunks <= (uint64_t)kLocFit;
+    if (fit)
+        for (uint64_t i = threadIdx.x; i < nchunks * kEntries; i += blockDim.x) s_tab[i] = ltab[i];
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    uint64_t err = h.bad ? G5_DEVERR_CORRUPT : 0;
+    uint64_t E = 1, G = 0;
+    for (uint64_t c = 0; c < nchunks; ++c) {
+        const uint64_t a = 1 + c * S;
+        lent[c] = (E & 0xFFFFFFFFull) | (G << 32);
+        if (G >= h.ng) continue;  // the chain has ended: this chunk owns nothing
+        if (E < a || E - a >= kEntries) {
+            err |= G5_DEVERR_CORRUPT;
+            G = h.ng;
+            continue;
+        }
+        const uint32_t tv = fit ? s_tab[c * kEntries + (E - a)] : ltab[c * kEntries + (E - a)];
+        G += tv & 0xFFFFu;
+        if (G >= h.ng) {
+            G = h.ng;
+            continue;
+        }
+        if ((tv >> 16) == kDead) {  // the chain dies before the last group
+            err |= G5_DEVERR_CORRUPT;
+            G = h.ng;
+            continue;
+        }
+        E = a + S + (tv >> 16);
+    }
+    if (!h.raw && !h.bad && h.ng > 0 && G < h.ng) err |= G5_DEVERR_CORRUPT;
+    if (!h.raw && h.ng == 0) scal[CS_BLKEND] = 4;
+    scal[CS_ERR] = err;
+    scal[CS_WORDS] = h.words;
+    scal[CS_RAW] = h.raw ? 1 : 0;
+    scal[CS_N1] = h.n1;
+    scal[CS_NMB] = h.nmb;
+    scal[CS_NG] = h.ng;
+    scal[CS_N] = h.raw ? h.words : 0;
+}
+
+// One block per chunk: the positions of the chunk's own groups, from its
+// real entry along the stored jumps; the block with the last group also
+// checks it and sets the end of the block part.
+__global__ void __launch_bounds__(kOB) k_loc_pos(const uint32_t *__restrict__ in, uint64_t *scal,
+                                                 const uint16_t *ljump, const uint64_t *lent, uint32_t *gpos)
+{
+    if (scal[CS_RAW] || scal[CS_ERR]) return;
+    const uint64_t ng = scal[CS_NG], nmb = scal[CS_NMB];
+    const uint64_t nv = scal[CS_WORDS] / 4;
+    const uint32_t S = loc_chunk(nv);
+    const uint64_t nchunks = ng == 0 ? 0 : (nv - 1 + S - 1) / S;
+    const uint4 *v = reinterpret_cast<const uint4 *>(in);
+    // one warp per chunk, its lane 0 walking
+    const uint64_t gw = ((uint64_t)blockIdx.x * kOB + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * kOB) >> 5;
+    if (g5_lane() != 0) return;
+    for (uint64_t c = gw; c < nchunks; c += nw) {
+        const uint64_t a = 1 + c * S;
+        const uint64_t en = lent[c];
+        uint64_t p = en & 0xFFFFFFFFull, g = en >> 32;
+        const uint64_t gnext = c + 1 < nchunks ? (lent[c + 1] >> 32) : ng;
+        for (; g < gnext; ++g) {
+            gpos[g] = (uint32_t)p;
+            if (g == ng - 1) {
+                // the last group holds only the remaining miniblocks
+                const uint4 hv = v[p];
+                const uint64_t howmany = nmb - 16 * g;
+                uint64_t sum = 0;
+                bool ok = true;
+                for (uint64_t q = 0; q < howmany; ++q) {
+                    const uint32_t b = width_of(hv, (int)q);
+                    ok &= b <= 32;
+                    sum += b;
+                }
+                const uint64_t end = p + 1 + sum;
+                if (!ok || end > nv) atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_CORRUPT);
+                else scal[CS_BLKEND] = 4 * end;
+                break;
+            }
+            if (g + 1 == gnext) break;  // the next group starts in the next chunk
+            const uint32_t r = ljump[p];
+            if (r == kDead) {  // the walk's tables rule this out; kept as a guard
+                atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_CORRUPT);
+                break;
+            }
+            p = a + r;
+        }
     }
 }
 
@@ -956,7 +965,10 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
                                                     uint64_t *ust, VecFlag *uagg, VecFlag *uinc, int mode)
 {
     __shared__ VecFlag s_vf[kTM];
-    __shared__ VecFlag s_base[kTM];
+    __shared__ VecFlag s_base[kTM];     // each miniblock's prefix from the tile's start
+    __shared__ VecFlag s_ex;            // the tile's exclusive prefix (look-back)
+    __shared__ uint8_t s_abs[kTM];      // 1: the miniblock's values need no tile prefix
+    __shared__ __align__(16) uint32_t s_val[kTM * 128];  // the tile's values before the tile prefix
     __shared__ uint64_t s_t;
     __shared__ uint32_t s_b[kTailMaxBytes / 4];
     const int lane = g5_lane(), wid = threadIdx.x >> 5;
@@ -1053,32 +1065,57 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
                 if (lane == 0) s_vf[16 * i + wid] = m;
             }
             __syncthreads();
-            if (wid == 0) {
-                VecFlag tile = ResetAdd::id();
-                for (int i = 0; i < kTM; ++i) tile = ResetAdd::op(tile, s_vf[i]);
-                const VecFlag ex = lookback<ResetAddV>(ust, uagg, uinc, t, epoch, tile, &scal[CS_ERR]);
-                if (lane == 0) {
-                    VecFlag run = ex;
-                    for (int i = 0; i < kTM; ++i) {
-                        s_base[i] = run;
-                        run = ResetAdd::op(run, s_vf[i]);
-                    }
+            if (threadIdx.x == 0) {
+                // prefixes from the tile's start (a reset inside the tile
+                // makes the rest absolute)
+                VecFlag run = ResetAdd::id();
+                for (int i = 0; i < kTM; ++i) {
+                    s_base[i] = run;
+                    s_abs[i] = (uint8_t)(run.f | s_vf[i].f);
+                    run = ResetAdd::op(run, s_vf[i]);
                 }
+                s_ex = run;  // the tile's aggregate, until warp 0 replaces it
             }
             __syncthreads();
-#pragma unroll 1
+            // warp 0 finds the tile's prefix (look-back) while the warps turn
+            // their deltas into values relative to the tile's start
+            if (wid == 0) {
+                const VecFlag ex = lookback<ResetAddV>(ust, uagg, uinc, t, epoch, s_ex, &scal[CS_ERR]);
+                __syncwarp();
+                if (lane == 0) s_ex = ex;
+            }
+#pragma unroll
             for (int i = 0; i < kTG; ++i) {
                 const uint64_t k = k0 + 16 * i + wid;
-                if (k >= nmb) break;
-                uint64_t off;
-                uint32_t bi;
-                mb_at(in, gpos[k / 16], wid, off, bi);
-                const uint4 dd = unpack_vec(in, off, bi);
-                const uint4 x = mb_values(dd, bi, s_base[16 * i + wid].v, mode);
-                reinterpret_cast<uint4 *>(out)[k * 32 + lane] = x;
-                if (expect) {
-                    const uint4 e = reinterpret_cast<const uint4 *>(expect)[k * 32 + lane];
-                    bad |= (e.x != x.x) | (e.y != x.y) | (e.z != x.z) | (e.w != x.w);
+                if (k < nmb)
+                    reinterpret_cast<uint4 *>(s_val)[(16 * i + wid) * 32 + lane] =
+                        mb_values(d[i], b[i], s_base[16 * i + wid].v, mode);
+            }
+            __syncthreads();
+            {
+                const VecFlag ex = s_ex;
+                const uint64_t kn = min((uint64_t)kTM, nmb - k0);  // miniblocks in this tile
+                for (uint32_t q = threadIdx.x; q < kn * 32; q += kOB) {
+                    const uint32_t m = q >> 5;  // miniblock of this 16-byte vector
+                    uint4 x = reinterpret_cast<const uint4 *>(s_val)[q];
+                    if (!s_abs[m]) {
+                        if (mode == G5_CODEC_DM) {
+                            x.x += ex.v.w;
+                            x.y += ex.v.w;
+                            x.z += ex.v.w;
+                            x.w += ex.v.w;
+                        } else {
+                            x.x += ex.v.x;
+                            x.y += ex.v.y;
+                            x.z += ex.v.z;
+                            x.w += ex.v.w;
+                        }
+                    }
+                    reinterpret_cast<uint4 *>(out)[k0 * 32 + q] = x;
+                    if (expect) {
+                        const uint4 e = reinterpret_cast<const uint4 *>(expect)[k0 * 32 + q];
+                        bad |= (e.x != x.x) | (e.y != x.y) | (e.z != x.z) | (e.w != x.w);
+                    }
                 }
             }
         }
@@ -1529,7 +1566,7 @@ size_t codec_bound(size_t n)
 
 size_t codec_tiles(size_t max_n) { return (max_n / 128 + 1) / 16 + 2; }
 
-size_t codec_chunks(size_t max_n) { return (codec_bound(max_n) / 4 + 2) / kLocS + 2; }
+size_t codec_chunks(size_t max_n) { return (codec_bound(max_n) / 4 + 2) / kLocMin + 2; }
 
 int codec_grid() { return num_sms() * 2; }
 
@@ -1546,15 +1583,17 @@ g5_status codec_work_alloc(CodecWork &w, size_t max_n)
     w.eagg = w.est + T;
     w.einc = w.est + 2 * T;
     G5_CUDA(cudaMalloc(&w.ltab, sizeof(uint32_t) * kEntries * C));
-    G5_CUDA(cudaMalloc(&w.lst, sizeof(uint64_t) * 2 * C));
-    w.lpay = w.lst + C;
+    G5_CUDA(cudaMalloc(&w.lent, sizeof(uint64_t) * C));
+    G5_CUDA(cudaMalloc(&w.ljump, sizeof(uint16_t) * (w.max_vec + 2)));
+    // the walk's table cache needs more than 48 KB of shared memory (set per device)
+    G5_CUDA(cudaFuncSetAttribute(k_loc_walk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(uint32_t) * kEntries * kLocFit)));
     G5_CUDA(cudaMalloc(&w.ust, sizeof(uint64_t) * T));
     G5_CUDA(cudaMalloc(&w.uagg, sizeof(VecFlag) * 2 * T));
     w.uinc = w.uagg + T;
     // epochs start at 1, so zeroed status words read as "not published"
     G5_CUDA(cudaMemset(w.scal, 0, sizeof(uint64_t) * kScalars));
     G5_CUDA(cudaMemset(w.est, 0, sizeof(uint64_t) * 3 * T));
-    G5_CUDA(cudaMemset(w.lst, 0, sizeof(uint64_t) * 2 * C));
     G5_CUDA(cudaMemset(w.ust, 0, sizeof(uint64_t) * T));
     const uint64_t one = 1;
     for (int e : {CS_E_EPOCH, CS_L_EPOCH, CS_U_EPOCH})
@@ -1568,7 +1607,8 @@ void codec_work_free(CodecWork &w)
     cudaFree(w.gpos);
     cudaFree(w.est);
     cudaFree(w.ltab);
-    cudaFree(w.lst);
+    cudaFree(w.lent);
+    cudaFree(w.ljump);
     cudaFree(w.ust);
     cudaFree(w.uagg);
     w = CodecWork();
@@ -1591,8 +1631,11 @@ void decode_launch_acc(CodecWork &w, const uint32_t *in, const uint64_t *words_d
                        int mode, uint64_t raw_threshold, const uint64_t *n_expect_dev, const uint32_t *expect,
                        uint64_t *acc, cudaStream_t s)
 {
-    k_dec_locate<<<w.grid, kOB, 0, s>>>(in, words_dev, cap, raw_threshold, n_expect_dev, w.scal, w.max_vec,
-                                        w.max_mb, w.ltab, w.lst, w.lpay, w.gpos);
+    k_loc_tables<<<w.grid, kOB, 0, s>>>(in, words_dev, cap, raw_threshold, n_expect_dev, w.scal, w.max_vec,
+                                        w.max_mb, w.ltab, w.ljump);
+    k_loc_walk<<<1, kWalkThreads, sizeof(uint32_t) * kEntries * kLocFit, s>>>(
+        in, words_dev, cap, raw_threshold, n_expect_dev, w.scal, w.max_vec, w.max_mb, w.ltab, w.lent);
+    k_loc_pos<<<w.grid, kOB, 0, s>>>(in, w.scal, w.ljump, w.lent, w.gpos);
     k_dec_unpack<<<w.grid, kOB, 0, s>>>(in, w.scal, w.gpos, out, cap, n_expect_dev, expect, acc, w.ust, w.uagg,
                                         w.uinc, mode);
 }

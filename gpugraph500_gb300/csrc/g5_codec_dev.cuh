@@ -24,9 +24,11 @@ struct CodecWork {
     uint32_t *gpos = nullptr;  // decoder: vector index of each group header
     // encoder look-back: status, aggregate and inclusive words per group
     uint64_t *est = nullptr, *eagg = nullptr, *einc = nullptr;
-    // decoder group locator: per chunk a transfer table, status and payload
+    // decoder group locator: per chunk a transfer table and the real entry,
+    // per stream vector its jump
     uint32_t *ltab = nullptr;
-    uint64_t *lst = nullptr, *lpay = nullptr;
+    uint64_t *lent = nullptr;
+    uint16_t *ljump = nullptr;
     // decoder unpacker look-back: status, aggregate and inclusive lane sums per group
     uint64_t *ust = nullptr;
     VecFlag *uagg = nullptr, *uinc = nullptr;
