@@ -115,6 +115,18 @@ public:
     }
     int64_t *getPredecessor() { return pred_.data(); }
     const std::vector<int64_t> &parents() const { return pred_; }
+    // every root, root i's parents into outs[i] (host or device, n entries;
+    // nullptr skips it) while root i + 1 runs; pinned host buffers overlap
+    void runMany(const std::vector<int64_t> &roots, const std::vector<int64_t *> &outs,
+                 std::vector<double> *device_ms = nullptr)
+    {
+        if (!outs.empty() && outs.size() != roots.size()) throw Error(G5_ERR_INVALID_ARG, "runMany");
+        if (device_ms) device_ms->assign(roots.size(), 0.0);
+        check(g5_bfs_run_many(b_, roots.data(), (int)roots.size(), outs.empty() ? nullptr : outs.data(),
+                              device_ms ? device_ms->data() : nullptr),
+              "g5_bfs_run_many");
+        if (!roots.empty()) root_ = roots.back();
+    }
     // Graph500 validation of the last search on the device
     bool validate(bool *min_parent = nullptr)
     {
@@ -191,6 +203,11 @@ public:
         }
         check(g5_server_create(gs.data(), (int)gs.size(), mem_budget, keep_results ? 1 : 0, mode, &sv_),
               "g5_server_create");
+    }
+    // cohort mode: a cohort starts at min_roots waiting queries or after max_wait_ms
+    void cohortPolicy(int min_roots, double max_wait_ms)
+    {
+        check(g5_server_cohort_policy(sv_, min_roots, max_wait_ms), "g5_server_cohort_policy");
     }
     uint64_t submit(int graph, int64_t root)
     {

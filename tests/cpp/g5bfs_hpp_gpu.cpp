@@ -41,12 +41,24 @@ static int run(int argc, char **argv)
     std::vector<int64_t> roots;
     for (int i = 3; i < argc; ++i) roots.push_back(std::atoll(argv[i]));
     g5::CudaBFS bfs(g);
+    std::vector<std::vector<int64_t>> alone;
     for (int64_t root : roots) {
         bfs.runBFS(root);
         bool minp = false;
         if (!bfs.validate(&minp) || !minp) return 1;
         if (bfs.getPredecessor()[root] != root) return 2;
         if (std::fwrite(bfs.getPredecessor(), sizeof(int64_t), n, f) != n) return 3;
+        alone.push_back(bfs.parents());
+    }
+    // all roots in one pipelined call: the same parents
+    {
+        std::vector<std::vector<int64_t>> many(roots.size(), std::vector<int64_t>(n, 7));
+        std::vector<int64_t *> outs;
+        for (auto &m : many) outs.push_back(m.data());
+        std::vector<double> ms;
+        bfs.runMany(roots, outs, &ms);
+        for (size_t i = 0; i < roots.size(); ++i)
+            if (many[i] != alone[i] || !(ms[i] > 0)) return 7;
     }
 
     g5::Batch bt({&g});
@@ -69,6 +81,17 @@ static int run(int argc, char **argv)
             const std::vector<int64_t> p = sv.result(t, 0, &lat);
             if (p.size() != n || lat < 0) return 31;
             if (std::fwrite(p.data(), sizeof(int64_t), n, f) != n) return 32;
+        }
+    }
+    {
+        // cohort mode on the same graph: every query's parents as alone
+        g5::Server sv({&g}, (size_t)1 << 30, G5_SERVE_COHORTS);
+        sv.cohortPolicy(2, 1.0);
+        std::vector<uint64_t> tickets;
+        for (int64_t root : roots) tickets.push_back(sv.submit(0, root));
+        for (size_t i = 0; i < tickets.size(); ++i) {
+            if (!sv.wait(tickets[i], 60.0)) return 33;
+            if (sv.result(tickets[i], 0) != alone[i]) return 34;
         }
     }
     std::fclose(f);
