@@ -106,7 +106,7 @@ struct BfsArgs {
     const uint32_t *heavy; // one bit per vertex of degree > kHeavy
     const uint32_t *ro32;  // row offsets as uint32 when nnz < 2^32, else null
     uint32_t *multi;       // vertices a top-down level reached more than once
-    uint32_t *wdeg;        // per word: degree sum of the vertices bottom-up added
+    uint32_t *wdeg;        // per word: degree sum of the vertices the expansion added
     unsigned *done;        // blocks of k_count finished (reset by the last one)
     uint32_t *ulist;       // sorted unvisited vertices for a bottom-up level
     uint64_t *chunk_u;     // per chunk: unvisited vertices after the level
@@ -196,6 +196,17 @@ __global__ void k_init(BfsArgs a)
 
 // ---- expansion ----------------------------------------------------------------
 
+// Sets v's bit in the next frontier; the thread that sets it adds v's degree
+// to its bitmap word's degree sum, so the counting pass reads one sum per
+// word instead of the degree of every new vertex.  Returns the word's bits
+// before the call.
+__device__ __forceinline__ uint32_t set_next(const BfsArgs &a, uint32_t v, uint32_t bit)
+{
+    const uint32_t old = atomicOr(a.next + (v >> 5), bit);
+    if (!(old & bit)) atomicAdd(a.wdeg + (v >> 5), __ldg(a.deg + v));
+    return old;
+}
+
 __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
 {
     __shared__ uint64_t s_q[kWarps][32];
@@ -248,13 +259,13 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
                             // value <= u (even a stale one) makes the atomic moot
                             if ((unsigned long long)a.pred[v] > u)
                                 atomicMin((unsigned long long *)(a.pred + v), u);
-                            if (!(a.next[v >> 5] & bit)) atomicOr(a.next + (v >> 5), bit);
+                            if (!(a.next[v >> 5] & bit)) set_next(a, v, bit);
                         } else if (a.parent_mode == 1) {
-                            if (!(a.next[v >> 5] & bit)) atomicOr(a.next + (v >> 5), bit);
+                            if (!(a.next[v >> 5] & bit)) set_next(a, v, bit);
                         } else {
                             // first discoverer writes its parent; a vertex
                             // reached again is left to the fix-up sweep
-                            const uint32_t old = (a.next[v >> 5] & bit) ? bit : atomicOr(a.next + (v >> 5), bit);
+                            const uint32_t old = (a.next[v >> 5] & bit) ? bit : set_next(a, v, bit);
                             if (!(old & bit)) atomicMin((unsigned long long *)(a.pred + v), u);
                             else if (!(a.multi[v >> 5] & bit)) atomicOr(a.multi + (v >> 5), bit);
                         }
@@ -665,22 +676,14 @@ __global__ void __launch_bounds__(kBlock) k_count(BfsArgs a)
 {
     const uint32_t c = blockIdx.x;
     const uint64_t w0 = (uint64_t)c * kChunkWords + (uint64_t)threadIdx.x * kWordsPerThread;
-    const bool bu = a.st->dir == DIR_BU;  // bottom-up levels leave per-word degree sums
+    // both expansions leave per-word degree sums of the vertices they add
     uint64_t cn = 0, cm = 0, cu = 0;
 #pragma unroll
     for (int k = 0; k < kWordsPerThread; ++k) {
-        uint32_t x = (w0 + k < a.nwords) ? a.next[w0 + k] : 0u;
+        const uint32_t x = (w0 + k < a.nwords) ? a.next[w0 + k] : 0u;
         if (a.st->dir == DIR_BU && w0 + k < a.nwords) cu += __popc(~(a.visited[w0 + k] | x));
         cn += __popc(x);
-        if (bu) {
-            if (x) cm += a.wdeg[w0 + k];
-            continue;
-        }
-        while (x) {
-            const int b = __ffs(x) - 1;
-            x &= x - 1;
-            cm += __ldg(a.deg + (w0 + k) * 32 + b);
-        }
+        if (x) cm += a.wdeg[w0 + k];
     }
     cn = warp_sum_u64(cn);
     cm = warp_sum_u64(cm);
@@ -1123,7 +1126,7 @@ struct g5_bfs {
     uint32_t *ro32 = nullptr;     // uint32 copy of the row offsets (nnz < 2^32)
     uint32_t *first = nullptr;    // first neighbour of each vertex (dense, coalesced)
     uint32_t *multi = nullptr;    // reached more than once in a top-down level
-    uint32_t *wdeg = nullptr;     // per-word degree sums written by bottom-up
+    uint32_t *wdeg = nullptr;     // per-word degree sums written by the expansion
     uint32_t *ulist = nullptr;    // sorted unvisited vertices (n entries)
     unsigned *done = nullptr;     // k_count's finished-block counter
     int64_t *pred = nullptr;
@@ -1172,6 +1175,9 @@ void enqueue_prologue(g5_bfs *b, const BfsArgs &a, cudaStream_t s)
     // bottom-up sweeps skip them (the root is set again by k_init)
     cudaMemcpyAsync(b->bitmaps, b->isolated, sizeof(uint32_t) * a.nwords, cudaMemcpyDeviceToDevice, s);
     cudaMemsetAsync(b->bitmaps + a.nwords, 0, sizeof(uint32_t) * 2 * a.nwords, s);
+    // per-word degree sums start at zero (a search stopped by an error can
+    // leave some behind)
+    cudaMemsetAsync(b->wdeg, 0, sizeof(uint32_t) * a.nwords, s);
     cudaMemsetAsync(a.pred, 0xFF, sizeof(int64_t) * (size_t)a.n, s);
     if (b->level) cudaMemsetAsync(b->level, 0xFF, sizeof(int32_t) * (size_t)a.n, s);
     k_init<<<1, kBlock, 0, s>>>(a);
