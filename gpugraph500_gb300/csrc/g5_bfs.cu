@@ -599,6 +599,7 @@ __device__ __forceinline__ void add_examined(const BfsArgs &a, uint64_t examined
 // Top-down expansion of the level (no-op when the level is bottom-up).
 __global__ void __launch_bounds__(kBlock, 8) k_td(BfsArgs a)
 {
+    g5_pdl_sync();
     if (a.st->err || a.st->dir != DIR_TD) return;
     uint64_t examined = 0;
     expand_td(a, examined);
@@ -610,6 +611,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_td(BfsArgs a)
 template <typename Off>
 __global__ void __launch_bounds__(kBlock, 8) k_bu(BfsArgs a)
 {
+    g5_pdl_sync();
     if (a.st->err || a.st->dir != DIR_BU) return;
     uint64_t examined = 0;
     if (a.st->list_mode) bottom_up_list<Off>(a, examined);
@@ -620,6 +622,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_bu(BfsArgs a)
 // Parents of the vertices a top-down level discovered (no-op after bottom-up).
 __global__ void __launch_bounds__(kBlock) k_fixup(BfsArgs a)
 {
+    g5_pdl_sync();
     if (a.st->err || a.st->dir != DIR_TD || a.parent_mode == 0) return;
     uint64_t examined = 0;
     if (a.ro32) sweep<true, uint32_t>(a, examined);
@@ -674,6 +677,7 @@ __device__ void scan_and_decide(const BfsArgs &a);
 
 __global__ void __launch_bounds__(kBlock) k_count(BfsArgs a)
 {
+    g5_pdl_sync();
     const uint32_t c = blockIdx.x;
     const uint64_t w0 = (uint64_t)c * kChunkWords + (uint64_t)threadIdx.x * kWordsPerThread;
     // both expansions leave per-word degree sums of the vertices they add
@@ -822,6 +826,7 @@ __device__ void scan_and_decide(const BfsArgs &a)
 
 __global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
 {
+    g5_pdl_sync();
     const uint32_t c = blockIdx.x;
     const int lane = g5_lane(), wid = threadIdx.x >> 5;
     const uint64_t wbeg = (uint64_t)c * kChunkWords + (uint64_t)wid * kWordsPerWarp;
@@ -1163,6 +1168,7 @@ struct g5_bfs {
     int64_t *cur_pred = nullptr;    // parent array of the last search
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     Prof prof;
+    bool pdl = true;  // level kernels as programmatic dependent launches
     bool ran = false;
     int64_t last_root = -1;
 };
@@ -1187,16 +1193,19 @@ void enqueue_level(g5_bfs *b, const BfsArgs &a, cudaStream_t s, Prof *pf = nullp
 {
     Prof dummy;
     Prof &p = pf ? *pf : dummy;
+    // the level's kernels follow one another as programmatic dependent
+    // launches (each sets up while the one before drains)
+    const bool pdl = b->pdl;
     p.mark(KP_EXPAND, s);
-    k_td<<<g5::grid_for(8), kBlock, 0, s>>>(a);
-    if (a.ro32) k_bu<uint32_t><<<g5::grid_for(8), kBlock, 0, s>>>(a);
-    else k_bu<int64_t><<<g5::grid_for(8), kBlock, 0, s>>>(a);
+    g5::launch(pdl, k_td, g5::grid_for(8), kBlock, s, a);
+    if (a.ro32) g5::launch(pdl, k_bu<uint32_t>, g5::grid_for(8), kBlock, s, a);
+    else g5::launch(pdl, k_bu<int64_t>, g5::grid_for(8), kBlock, s, a);
     p.mark(KP_FIXUP, s);
-    if (a.parent_mode != 0) k_fixup<<<g5::grid_for(8), kBlock, 0, s>>>(a);
+    if (a.parent_mode != 0) g5::launch(pdl, k_fixup, g5::grid_for(8), kBlock, s, a);
     p.mark(KP_COUNT, s);
-    k_count<<<a.nchunks, kBlock, 0, s>>>(a);
+    g5::launch(pdl, k_count, a.nchunks, kBlock, s, a);
     p.mark(KP_WRITE, s);
-    k_write<<<a.nchunks, kBlock, 0, s>>>(a);
+    g5::launch(pdl, k_write, a.nchunks, kBlock, s, a);
     p.mark(KP_CODEC, s);
     if (a.codec) {
         g5::codec_encode_launch(b->cw, b->queue, &b->st->nf, b->codec_stream, a.codec,
@@ -1467,7 +1476,16 @@ g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
     k_degrees<<<g5::grid_for(8), kBlock, 0, b->stream>>>(g->row_off, g->col, g->n, b->deg, b->isolated,
                                                           b->heavy, b->ro32, b->first);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
-    if (b->cfg.use_graph && (st = build_graph(b, b->pred, &b->exec, &b->graph)) != G5_OK) return fail(st);
+    if (b->cfg.use_graph && (st = build_graph(b, b->pred, &b->exec, &b->graph)) != G5_OK) {
+        // a driver that cannot capture programmatic dependent launches into
+        // the loop's body: the same graph with ordinary launches
+        cudaGetLastError();
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+        b->exec = nullptr;
+        b->pdl = false;
+        if ((st = build_graph(b, b->pred, &b->exec, &b->graph)) != G5_OK) return fail(st);
+    }
     b->cur_pred = b->pred;
     *out = b;
     return G5_OK;

@@ -24,12 +24,7 @@ struct Srcs {
 template <int K, int V>
 __global__ void __launch_bounds__(256) k_or_vec(ulonglong2 *__restrict__ dst, Srcs s, uint64_t nvec)
 {
-    // launched as a programmatic dependent of the previous kernel on the
-    // stream: wait until that grid has finished and its writes are visible,
-    // then let the next launch start setting up while this one streams (both
-    // are no-ops for an ordinary launch)
-    asm volatile("griddepcontrol.wait;\n" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+    g5_pdl_sync();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < nvec; i0 += stride * V) {
         ulonglong2 acc[V];
@@ -74,19 +69,10 @@ void launch_or(ulonglong2 *dst, const Srcs &s, uint64_t nvec, cudaStream_t st)
     const uint64_t want = (nvec + per_block - 1) / per_block;
     const uint64_t cap = (uint64_t)g5::grid_for(8);
     const int grid = (int)(want < cap ? want : cap);
-    // programmatic stream serialization: the launch may begin while the
-    // previous kernel on the stream drains; the kernel's griddepcontrol.wait
-    // keeps the data dependence
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(256);
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, k_or_vec<K, kVec>, dst, s, nvec);
+    // a programmatic dependent launch: it may begin while the previous
+    // kernel on the stream drains; the kernel's first instruction keeps the
+    // data dependence
+    g5::launch(true, k_or_vec<K, kVec>, grid, 256, st, dst, s, nvec);
 }
 
 void dispatch_or(ulonglong2 *dst, const Srcs &s, int k, uint64_t nvec, cudaStream_t st)

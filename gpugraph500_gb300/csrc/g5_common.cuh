@@ -68,6 +68,23 @@ struct DevBuf {
     }
 };
 
+// Launches kern on s; with pdl, as a programmatic dependent of the kernel
+// before it on the stream (the kernel must call g5_pdl_sync first).
+template <typename... KArgs, typename... Args>
+cudaError_t launch(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 }  // namespace g5
 
 // Device-side error flags (bit set in a status word).
@@ -80,6 +97,16 @@ enum : uint32_t {
 };
 
 __device__ __forceinline__ int g5_lane() { return threadIdx.x & 31; }
+
+// Programmatic dependent launch: waits until the kernel before this one on
+// the stream has finished and its writes are visible, then lets the next
+// launch start setting up while this one runs.  Both are no-ops for an
+// ordinary launch; a kernel calls this before it reads anything.
+__device__ __forceinline__ void g5_pdl_sync()
+{
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
 __device__ __forceinline__ unsigned g5_lanemask_lt()
 {
     unsigned m;
