@@ -576,18 +576,37 @@ __global__ void __launch_bounds__(kOB) k_enc1(const uint32_t *__restrict__ in, c
                 if (lane == 0) s_b[16 * i + wid] = b;
             }
             __syncthreads();
-            if (threadIdx.x == 0) {
-                uint32_t o = 0;
-                for (int g = 0; g < kTG; ++g) {
-                    if ((uint64_t)kTG * t + g >= ngroups) break;  // no header past the last group
-                    s_goff[g] = o;
-                    o += 4;
-                    for (int i = 0; i < 16; ++i) {
-                        s_off[16 * g + i] = o;
-                        o += 4 * s_b[16 * g + i];
-                    }
+            if (wid == 0) {
+                // words of miniblock i, plus its group's 4 header words at the
+                // group's first miniblock (no header past the last group);
+                // exclusive scan over the 64, two per lane
+                uint32_t e[2], x = 0;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int i = 2 * lane + h;
+                    const bool head = (i & 15) == 0 && (uint64_t)kTG * t + i / 16 < ngroups;
+                    e[h] = 4 * s_b[i] + (head ? 4u : 0u);
+                    x += e[h];
                 }
-                s_tw = o;
+                uint32_t inc = x;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+                    if (lane >= o) inc += y;
+                }
+                uint32_t pos = inc - x;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int i = 2 * lane + h;
+                    if ((i & 15) == 0) {
+                        s_goff[i / 16] = pos;
+                        s_off[i] = pos + 4;
+                    } else {
+                        s_off[i] = pos;
+                    }
+                    pos += e[h];
+                }
+                if (lane == 31) s_tw = inc;
             }
             __syncthreads();
             // warp 0 finds the tile's place (look-back) first, so that later
@@ -787,8 +806,23 @@ __global__ void __launch_bounds__(kWalkThreads) k_loc_walk(const uint32_t *__res
     const uint32_t S = loc_chunk(h.nv);
     const uint64_t nchunks = (h.raw || h.bad || h.ng == 0) ? 0 : (h.nv - 1 + S - 1) / S;
     const bool fit = nchunks <= (uint64_t)kLocFit;
-    if (fit)
-        for (uint64_t i = threadIdx.x; i < nchunks * kEntries; i += blockDim.x) s_tab[i] = ltab[i];
+    if (fit) {
+        // eight loads per thread in flight at a time
+        const uint64_t tot = nchunks * kEntries;
+        for (uint64_t i0 = threadIdx.x; i0 < tot; i0 += 8ull * blockDim.x) {
+            uint32_t r[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const uint64_t i = i0 + (uint64_t)k * blockDim.x;
+                r[k] = i < tot ? ltab[i] : 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const uint64_t i = i0 + (uint64_t)k * blockDim.x;
+                if (i < tot) s_tab[i] = r[k];
+            }
+        }
+    }
     __syncthreads();
     if (threadIdx.x != 0) return;
     uint64_t err = h.bad ? G5_DEVERR_CORRUPT : 0;
@@ -827,27 +861,30 @@ __global__ void __launch_bounds__(kWalkThreads) k_loc_walk(const uint32_t *__res
 }
 
 // One block per chunk: the positions of the chunk's own groups, from its
-// real entry along the stored jumps; the block with the last group also
-// checks it and sets the end of the block part.
+// real entry along the jumps (staged in shared memory); the block with the
+// last group also checks it and sets the end of the block part.
 __global__ void __launch_bounds__(kOB) k_loc_pos(const uint32_t *__restrict__ in, uint64_t *scal,
                                                  const uint16_t *ljump, const uint64_t *lent, uint32_t *gpos)
 {
+    __shared__ uint16_t s_j[kLocMax];
     if (scal[CS_RAW] || scal[CS_ERR]) return;
     const uint64_t ng = scal[CS_NG], nmb = scal[CS_NMB];
     const uint64_t nv = scal[CS_WORDS] / 4;
     const uint32_t S = loc_chunk(nv);
     const uint64_t nchunks = ng == 0 ? 0 : (nv - 1 + S - 1) / S;
     const uint4 *v = reinterpret_cast<const uint4 *>(in);
-    // one warp per chunk, its lane 0 walking
-    const uint64_t gw = ((uint64_t)blockIdx.x * kOB + threadIdx.x) >> 5;
-    const uint64_t nw = ((uint64_t)gridDim.x * kOB) >> 5;
-    if (g5_lane() != 0) return;
-    for (uint64_t c = gw; c < nchunks; c += nw) {
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const uint64_t a = 1 + c * S;
         const uint64_t en = lent[c];
-        uint64_t p = en & 0xFFFFFFFFull, g = en >> 32;
+        const uint64_t g0 = en >> 32;
         const uint64_t gnext = c + 1 < nchunks ? (lent[c + 1] >> 32) : ng;
-        for (; g < gnext; ++g) {
+        if (g0 >= gnext) continue;  // uniform over the block
+        __syncthreads();            // the previous chunk's jumps are no longer read
+        for (uint32_t p = threadIdx.x; p < S && a + p < nv; p += kOB) s_j[p] = ljump[a + p];
+        __syncthreads();
+        if (threadIdx.x != 0) continue;
+        uint64_t p = en & 0xFFFFFFFFull;
+        for (uint64_t g = g0; g < gnext; ++g) {
             gpos[g] = (uint32_t)p;
             if (g == ng - 1) {
                 // the last group holds only the remaining miniblocks
@@ -866,7 +903,7 @@ __global__ void __launch_bounds__(kOB) k_loc_pos(const uint32_t *__restrict__ in
                 break;
             }
             if (g + 1 == gnext) break;  // the next group starts in the next chunk
-            const uint32_t r = ljump[p];
+            const uint32_t r = s_j[p - a];
             if (r == kDead) {  // the walk's tables rule this out; kept as a guard
                 atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_CORRUPT);
                 break;
@@ -1065,16 +1102,25 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
                 if (lane == 0) s_vf[16 * i + wid] = m;
             }
             __syncthreads();
-            if (threadIdx.x == 0) {
-                // prefixes from the tile's start (a reset inside the tile
-                // makes the rest absolute)
-                VecFlag run = ResetAdd::id();
-                for (int i = 0; i < kTM; ++i) {
-                    s_base[i] = run;
-                    s_abs[i] = (uint8_t)(run.f | s_vf[i].f);
-                    run = ResetAdd::op(run, s_vf[i]);
+            if (wid == 0) {
+                // prefixes from the tile's start, two miniblocks per lane (a
+                // reset inside the tile makes the rest absolute)
+                const VecFlag v0 = s_vf[2 * lane], v1 = s_vf[2 * lane + 1];
+                const VecFlag c = ResetAdd::op(v0, v1);
+                VecFlag inc = c;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const VecFlag y = ResetAdd::shfl_up(inc, o);
+                    if (lane >= o) inc = ResetAdd::op(y, inc);
                 }
-                s_ex = run;  // the tile's aggregate, until warp 0 replaces it
+                VecFlag ex = ResetAdd::shfl_up(inc, 1);
+                if (lane == 0) ex = ResetAdd::id();
+                s_base[2 * lane] = ex;
+                s_abs[2 * lane] = (uint8_t)(ex.f | v0.f);
+                const VecFlag e1 = ResetAdd::op(ex, v0);
+                s_base[2 * lane + 1] = e1;
+                s_abs[2 * lane + 1] = (uint8_t)(e1.f | v1.f);
+                if (lane == 31) s_ex = inc;  // the tile's aggregate, until the look-back replaces it
             }
             __syncthreads();
             // warp 0 finds the tile's prefix (look-back) while the warps turn
