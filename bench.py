@@ -618,14 +618,26 @@ def dram_measured(kernel, scale, peak, gteps=None, edges_per_search=None):
 
 def kernel_roofline(g5, g, roots, alpha, beta, peak, sizes=None):
     """Per-kernel times of the plain search (profile mode) and the
-    algorithmic-bytes roofline of the dominant expansion kernel.  Per launch:
-    bottom-up 8(N+1) + 4 E_bu + 3N/8 (offset stream, adjacency read until the
-    first hit, frontier/visited/next bitmaps); top-down 20|F| + 4 E_td + N/8
-    (queue and row-offset pair, adjacency, visited bitmap)."""
+    algorithmic-bytes roofline of each expansion launch kind, the dominant
+    one as the headline.  C = candidates of a bottom-up level (vertices with
+    edges not yet visited), off = bytes of a row offset (4 while nnz < 2^32).
+    Per launch:
+      k_bu word sweep (first bottom-up level): N/8 visited words + (off + 4) C
+        (each candidate's row start and its first neighbour from the dense
+        copy; the row end is the next start) + 4 E_bu (adjacency read until
+        the first hit) + N/8 frontier probes + N/8 next words
+      k_bu list sweep (later bottom-up levels): 4 C (the unvisited list) +
+        (2 off + 4) C (row bounds and first neighbour of each listed vertex)
+        + 4 E_bu + N/8 frontier probes
+      k_td: 20 |F| (queue entry, edge offset, row base) + 4 E_td + N/8 visited."""
     pb = g5.CudaBFS(g, alpha=alpha, beta=beta, use_graph=False, profile=True, **(sizes or {}))
     n = g.n
+    off = 4 if g.nnz < (1 << 32) - 64 else 8
+    ro = g.row_offsets()
+    with_edges = int(np.count_nonzero(np.diff(ro)))
+    del ro
     tot = {}
-    acc = {"bu": [0.0, 0.0, 0], "td": [0.0, 0.0, 0]}  # bytes, ms, launches
+    acc = {k: [0.0, 0.0, 0] for k in ("bu_sweep", "bu_list", "td")}  # bytes, ms, launches
     for r in roots:
         code = pb.run(int(r), None, None, stats=True)
         if code != 0:
@@ -634,32 +646,46 @@ def kernel_roofline(g5, g, roots, alpha, beta, peak, sizes=None):
         for k, ms in log:
             tot[k] = tot.get(k, 0.0) + ms
         exp = [ms for k, ms in log if k == "expand"]
+        seen = 0      # vertices visited up to and including the level
+        prev_bu = False
         for lvl, row in enumerate(pb.level_log()):
             if lvl >= len(exp):
                 break
             d, nf, _, read = (int(x) for x in row)
-            if d == 1:
-                b = 8 * (n + 1) + 4 * read + 3 * n / 8
-                key = "bu"
+            seen += nf
+            cand = max(with_edges - seen, 0)
+            if d == 1 and not prev_bu:
+                b = 3 * n / 8 + (off + 4) * cand + 4 * read
+                key = "bu_sweep"
+            elif d == 1:
+                b = (4 + 2 * off + 4) * cand + 4 * read + n / 8
+                key = "bu_list"
             else:
                 b = 20 * nf + 4 * read + n / 8
                 key = "td"
+            prev_bu = d == 1
             acc[key][0] += b
             acc[key][1] += exp[lvl]
             acc[key][2] += 1
     pb.close()
     total_ms = sum(tot.values())
-    key = "bu" if acc["bu"][1] >= acc["td"][1] else "td"
-    b, ms, cnt = acc[key]
-    name = BU_KERNEL if key == "bu" else TD_KERNEL
-    ach = b / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
-    return {"name": name, "launches": cnt, "ms_per_launch": ms / max(cnt, 1),
-            "bytes_per_launch": b / max(cnt, 1), "achieved": ach,
-            "share_of_search": ms / total_ms if total_ms else None,
-            "traffic": ncu_traffic(name, g.scale),
-            "kernel_ms_per_search": {k: v / len(roots) for k, v in tot.items()},
-            "other_expand": {"name": TD_KERNEL if key == "bu" else BU_KERNEL, "launches": acc["td" if key == "bu" else "bu"][2],
-                             "ms_total": acc["td" if key == "bu" else "bu"][1]}}
+    kinds = {}
+    for key, (b, ms, cnt) in acc.items():
+        if cnt:
+            kinds[key] = {"launches": cnt, "ms_per_launch": ms / cnt, "bytes_per_launch": b / cnt,
+                          "achieved": b / (ms * 1e-3) / 1e9 if ms > 0 else 0.0,
+                          "frac": (b / (ms * 1e-3) / 1e9 / peak) if ms > 0 else 0.0,
+                          "share_of_search": ms / total_ms if total_ms else None}
+    key = max(kinds, key=lambda k: acc[k][1])
+    name = TD_KERNEL if key == "td" else BU_KERNEL
+    head = kinds[key]
+    return {"name": name, "kind": key, "launches": head["launches"], "ms_per_launch": head["ms_per_launch"],
+            "bytes_per_launch": head["bytes_per_launch"], "achieved": head["achieved"],
+            "share_of_search": head["share_of_search"],
+            "traffic": ncu_traffic(name, g.scale) if key != "td" else ncu_traffic(TD_KERNEL, g.scale),
+            "traffic_scope": "ncu DRAM bytes per working k_bu launch, both sweep kinds together",
+            "kinds": kinds, "offset_bytes": off, "vertices_with_edges": with_edges,
+            "kernel_ms_per_search": {k: v / len(roots) for k, v in tot.items()}}
 
 
 class _DevArray:

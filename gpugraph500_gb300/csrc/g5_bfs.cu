@@ -1169,6 +1169,7 @@ struct g5_bfs {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     Prof prof;
     bool pdl = true;  // level kernels as programmatic dependent launches
+    int64_t with_edges = 0;  // vertices of degree > 0
     bool ran = false;
     int64_t last_root = -1;
 };
@@ -1411,19 +1412,32 @@ void free_ws(g5_bfs *b)
     if (b->stream) cudaStreamDestroy(b->stream);
 }
 
-// Algorithmic HBM bytes of one search from the level log (per level:
-// top-down 4|F| + 16|F| + 4 E_td + N/8 + 4|F'| + 9|F'|; bottom-up
-// 8(N+1) + 4 E_bu + 3N/8 + 9|F'|).
-int64_t alg_bytes(const LevelRec *log, int nlev, int64_t n)
+// Algorithmic HBM bytes of one search from the level log.  With C the
+// candidates of a bottom-up level (vertices with edges not yet visited) and
+// off the bytes of a row offset, per level: top-down 20|F| + 4 E_td + N/8
+// (queue entry, edge offset and row base per frontier vertex, adjacency,
+// visited bitmap); the first bottom-up level of a run 3N/8 + (off + 4) C +
+// 4 E_bu (visited, frontier and next bitmaps, each candidate's row start and
+// dense first neighbour, adjacency until the first hit); a later one
+// (2 off + 8) C + 4 E_bu + N/8 (the unvisited list, row bounds and first
+// neighbour of each listed vertex, adjacency, frontier); plus 4 + 9 bytes
+// per vertex the level adds (queue, parent, level) after top-down and 9
+// after bottom-up.
+int64_t alg_bytes(const LevelRec *log, int nlev, int64_t n, int64_t with_edges, int off)
 {
-    double B = 0;
+    double B = 0, seen = 0;
     for (int L = 0; L < nlev; ++L) {
         const double nf = (double)log[L].nf;
         const double nf1 = (L + 1 < nlev) ? (double)log[L + 1].nf : 0.0;
+        seen += nf;
+        const double cand = std::max(0.0, (double)with_edges - seen);
+        const double E = 4.0 * (double)log[L].examined;
         if (log[L].dir == DIR_TD)
-            B += 20.0 * nf + 4.0 * (double)log[L].examined + (double)n / 8.0 + 13.0 * nf1;
+            B += 20.0 * nf + E + (double)n / 8.0 + 13.0 * nf1;
+        else if (L == 0 || log[L - 1].dir != DIR_BU)
+            B += 3.0 * (double)n / 8.0 + (off + 4.0) * cand + E + 9.0 * nf1;
         else
-            B += 8.0 * (double)(n + 1) + 4.0 * (double)log[L].examined + 3.0 * (double)n / 8.0 + 9.0 * nf1;
+            B += (2.0 * off + 8.0) * cand + E + (double)n / 8.0 + 9.0 * nf1;
     }
     return (int64_t)B;
 }
@@ -1476,6 +1490,16 @@ g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
     k_degrees<<<g5::grid_for(8), kBlock, 0, b->stream>>>(g->row_off, g->col, g->n, b->deg, b->isolated,
                                                           b->heavy, b->ro32, b->first);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(G5_ERR_CUDA);
+    {
+        // vertices with edges (for the algorithmic byte count): n minus the
+        // isolated bits
+        std::vector<uint32_t> iso((size_t)b->args.nwords);
+        if (cudaMemcpy(iso.data(), b->isolated, sizeof(uint32_t) * iso.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return fail(G5_ERR_CUDA);
+        int64_t isolated = 0;
+        for (uint32_t w : iso) isolated += __builtin_popcount(w);
+        b->with_edges = g->n - isolated;
+    }
     if (b->cfg.use_graph && (st = build_graph(b, b->pred, &b->exec, &b->graph)) != G5_OK) {
         // a driver that cannot capture programmatic dependent launches into
         // the loop's body: the same graph with ordinary launches
@@ -1559,7 +1583,7 @@ g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_
         }
         stats->codec_words = (int64_t)hs.codec_acc[0];
         stats->codec_values = (int64_t)hs.codec_acc[1];
-        stats->alg_bytes = alg_bytes(b->h_log, nlev, b->g->n);
+        stats->alg_bytes = alg_bytes(b->h_log, nlev, b->g->n, b->with_edges, b->ro32 ? 4 : 8);
         float ms = 0;
         cudaEventElapsedTime(&ms, b->ev0, b->ev1);
         stats->device_ms = ms;
