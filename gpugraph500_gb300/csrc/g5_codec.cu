@@ -501,21 +501,25 @@ __device__ void enc_tail_warp(const uint32_t *in, uint64_t n, uint64_t n1, uint6
 constexpr int kTG = 4;               // groups per encoder / unpacker tile
 constexpr int kTM = 16 * kTG;        // miniblocks per tile
 
-// Packs the deltas of one miniblock (already in s_d) with width b at out + po.
-__device__ __forceinline__ void pack_mb(const uint4 (&s_dw)[32], uint32_t b, uint32_t *out, uint64_t po)
+// Packs a miniblock's deltas (lane j holds vector j) with width b (1..31)
+// into shared memory at s + po: value j of lane l occupies bits j b .. of
+// lane l's bit stream, whose word w is s[po + 4 w + l]
+// (ipackwithoutmask<b>, simdintegratedbitpacking.cpp:875).  Each lane ORs
+// its four values into place (a value that straddles two words into both)
+// after the words are cleared: no division, no loop over values.
+__device__ __forceinline__ void pack_mb_smem(const uint4 &d, uint32_t b, uint32_t *s, uint32_t po)
 {
     const int lane = g5_lane();
-    for (uint32_t idx = lane; idx < 4 * b; idx += 32) {
-        const uint32_t w = idx >> 2, l = idx & 3;
-        const uint32_t bit0 = 32 * w;
-        const uint32_t j0 = bit0 / b, j1 = (bit0 + 31) / b;
-        uint32_t word = 0;
-        for (uint32_t j = j0; j <= j1 && j < 32; ++j) {
-            const uint32_t dj = comp(s_dw[j], l);
-            const int sh = (int)(j * b) - (int)bit0;
-            word |= sh >= 0 ? (dj << sh) : (dj >> (-sh));
-        }
-        out[po + idx] = word;
+    for (uint32_t idx = lane; idx < 4 * b; idx += 32) s[po + idx] = 0;
+    __syncwarp();
+    const uint32_t bit = (uint32_t)lane * b, w = bit >> 5, sh = bit & 31;
+    const bool spill = sh + b > 32;
+    uint32_t *p = s + po + 4 * w;
+    const uint32_t v[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        atomicOr(p + l, v[l] << sh);
+        if (spill) atomicOr(p + 4 + l, v[l] >> (32 - sh));
     }
 }
 
@@ -523,7 +527,6 @@ __global__ void __launch_bounds__(kOB) k_enc1(const uint32_t *__restrict__ in, c
                                               uint64_t max_n, uint64_t raw_thr, uint32_t *__restrict__ out,
                                               uint64_t *scal, uint64_t *tst, uint64_t *tagg, uint64_t *tinc, int mode)
 {
-    __shared__ uint4 s_d[16][32];
     __shared__ __align__(16) uint32_t s_out[kTG * (4 + 16 * 128)];  // the tile's words, packed before its place is known
     __shared__ uint32_t s_b[kTM];
     __shared__ uint32_t s_off[kTM];  // payload word offset of each miniblock in the tile
@@ -629,14 +632,8 @@ __global__ void __launch_bounds__(kOB) k_enc1(const uint32_t *__restrict__ in, c
                 const uint32_t po = s_off[16 * i + wid];
                 uint4 c, pv;
                 load_vectors(in, k, c, pv);
-                if (b == 32) {
-                    reinterpret_cast<uint4 *>(s_out + po)[lane] = c;
-                } else if (b) {
-                    s_d[wid][lane] = deltas(c, pv, mode);
-                    __syncwarp();
-                    pack_mb(s_d[wid], b, s_out, po);
-                    __syncwarp();
-                }
+                if (b == 32) reinterpret_cast<uint4 *>(s_out + po)[lane] = c;
+                else if (b) pack_mb_smem(deltas(c, pv, mode), b, s_out, po);
             }
             __syncthreads();
             const uint64_t base = 4 + s_excl;  // word of the tile's first header (a multiple of 4)
