@@ -561,7 +561,8 @@ def ncu_summary(kernel, scale):
             for ln in f:
                 k, sep, v = ln.partition(":")
                 if sep and k in ("dram_bytes_per_launch", "ncu_mean_us", "search_dram_gbs_ncu",
-                                 "search_dram_bytes_per_search"):
+                                 "search_dram_bytes_per_search", "sweep_dram_bytes_per_launch",
+                                 "list_dram_bytes_per_launch"):
                     out[k] = float(v)
                 elif sep and k == "settings":
                     # "alpha=14 beta=2000 tile_edges=128 bu_serial=8"
@@ -569,6 +570,14 @@ def ncu_summary(kernel, scale):
     except (OSError, ValueError, IndexError):
         pass
     return out
+
+
+def kind_traffic(kind, scale):
+    """DRAM bytes per launch of one k_bu launch kind ("bu_sweep" or
+    "bu_list") from the committed summary profiles/k_bu_kinds_scale<s>.txt,
+    or None."""
+    key = {"bu_sweep": "sweep_dram_bytes_per_launch", "bu_list": "list_dram_bytes_per_launch"}.get(kind)
+    return ncu_summary("k_bu_kinds", scale).get(key) if key else None
 
 
 def ncu_traffic(kernel, scale):
@@ -675,15 +684,16 @@ def kernel_roofline(g5, g, roots, alpha, beta, peak, sizes=None):
             kinds[key] = {"launches": cnt, "ms_per_launch": ms / cnt, "bytes_per_launch": b / cnt,
                           "achieved": b / (ms * 1e-3) / 1e9 if ms > 0 else 0.0,
                           "frac": (b / (ms * 1e-3) / 1e9 / peak) if ms > 0 else 0.0,
-                          "share_of_search": ms / total_ms if total_ms else None}
+                          "share_of_search": ms / total_ms if total_ms else None,
+                          "traffic": kind_traffic(key, g.scale)}
     key = max(kinds, key=lambda k: acc[k][1])
     name = TD_KERNEL if key == "td" else BU_KERNEL
     head = kinds[key]
     return {"name": name, "kind": key, "launches": head["launches"], "ms_per_launch": head["ms_per_launch"],
             "bytes_per_launch": head["bytes_per_launch"], "achieved": head["achieved"],
             "share_of_search": head["share_of_search"],
-            "traffic": ncu_traffic(name, g.scale) if key != "td" else ncu_traffic(TD_KERNEL, g.scale),
-            "traffic_scope": "ncu DRAM bytes per working k_bu launch, both sweep kinds together",
+            "traffic": kind_traffic(key, g.scale),
+            "traffic_source": f"profiles/k_bu_kinds_scale{g.scale}.txt (DRAM bytes per launch of this kind)",
             "kinds": kinds, "offset_bytes": off, "vertices_with_edges": with_edges,
             "kernel_ms_per_search": {k: v / len(roots) for k, v in tot.items()}}
 
