@@ -106,7 +106,7 @@ struct BfsArgs {
     const uint32_t *heavy; // one bit per vertex of degree > kHeavy
     const uint32_t *ro32;  // row offsets as uint32 when nnz < 2^32, else null
     uint32_t *multi;       // vertices a top-down level reached more than once
-    uint32_t *wdeg;        // per word: degree sum of the vertices the expansion added
+    uint32_t *wdeg;        // per word: degree sum of the vertices bottom-up added
     unsigned *done;        // blocks of k_count finished (reset by the last one)
     uint32_t *ulist;       // sorted unvisited vertices for a bottom-up level
     uint64_t *chunk_u;     // per chunk: unvisited vertices after the level
@@ -196,17 +196,6 @@ __global__ void k_init(BfsArgs a)
 
 // ---- expansion ----------------------------------------------------------------
 
-// Sets v's bit in the next frontier; the thread that sets it adds v's degree
-// to its bitmap word's degree sum, so the counting pass reads one sum per
-// word instead of the degree of every new vertex.  Returns the word's bits
-// before the call.
-__device__ __forceinline__ uint32_t set_next(const BfsArgs &a, uint32_t v, uint32_t bit)
-{
-    const uint32_t old = atomicOr(a.next + (v >> 5), bit);
-    if (!(old & bit)) atomicAdd(a.wdeg + (v >> 5), __ldg(a.deg + v));
-    return old;
-}
-
 __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
 {
     __shared__ uint64_t s_q[kWarps][32];
@@ -259,13 +248,13 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
                             // value <= u (even a stale one) makes the atomic moot
                             if ((unsigned long long)a.pred[v] > u)
                                 atomicMin((unsigned long long *)(a.pred + v), u);
-                            if (!(a.next[v >> 5] & bit)) set_next(a, v, bit);
+                            if (!(a.next[v >> 5] & bit)) atomicOr(a.next + (v >> 5), bit);
                         } else if (a.parent_mode == 1) {
-                            if (!(a.next[v >> 5] & bit)) set_next(a, v, bit);
+                            if (!(a.next[v >> 5] & bit)) atomicOr(a.next + (v >> 5), bit);
                         } else {
                             // first discoverer writes its parent; a vertex
                             // reached again is left to the fix-up sweep
-                            const uint32_t old = (a.next[v >> 5] & bit) ? bit : set_next(a, v, bit);
+                            const uint32_t old = (a.next[v >> 5] & bit) ? bit : atomicOr(a.next + (v >> 5), bit);
                             if (!(old & bit)) atomicMin((unsigned long long *)(a.pred + v), u);
                             else if (!(a.multi[v >> 5] & bit)) atomicOr(a.multi + (v >> 5), bit);
                         }
@@ -599,7 +588,6 @@ __device__ __forceinline__ void add_examined(const BfsArgs &a, uint64_t examined
 // Top-down expansion of the level (no-op when the level is bottom-up).
 __global__ void __launch_bounds__(kBlock, 8) k_td(BfsArgs a)
 {
-    g5_pdl_sync();
     if (a.st->err || a.st->dir != DIR_TD) return;
     uint64_t examined = 0;
     expand_td(a, examined);
@@ -611,7 +599,6 @@ __global__ void __launch_bounds__(kBlock, 8) k_td(BfsArgs a)
 template <typename Off>
 __global__ void __launch_bounds__(kBlock, 8) k_bu(BfsArgs a)
 {
-    g5_pdl_sync();
     if (a.st->err || a.st->dir != DIR_BU) return;
     uint64_t examined = 0;
     if (a.st->list_mode) bottom_up_list<Off>(a, examined);
@@ -622,7 +609,6 @@ __global__ void __launch_bounds__(kBlock, 8) k_bu(BfsArgs a)
 // Parents of the vertices a top-down level discovered (no-op after bottom-up).
 __global__ void __launch_bounds__(kBlock) k_fixup(BfsArgs a)
 {
-    g5_pdl_sync();
     if (a.st->err || a.st->dir != DIR_TD || a.parent_mode == 0) return;
     uint64_t examined = 0;
     if (a.ro32) sweep<true, uint32_t>(a, examined);
@@ -677,17 +663,27 @@ __device__ void scan_and_decide(const BfsArgs &a);
 
 __global__ void __launch_bounds__(kBlock) k_count(BfsArgs a)
 {
-    g5_pdl_sync();
     const uint32_t c = blockIdx.x;
     const uint64_t w0 = (uint64_t)c * kChunkWords + (uint64_t)threadIdx.x * kWordsPerThread;
-    // both expansions leave per-word degree sums of the vertices they add
+    const bool bu = a.st->dir == DIR_BU;  // bottom-up levels leave per-word degree sums
     uint64_t cn = 0, cm = 0, cu = 0;
 #pragma unroll
     for (int k = 0; k < kWordsPerThread; ++k) {
-        const uint32_t x = (w0 + k < a.nwords) ? a.next[w0 + k] : 0u;
+        uint32_t x = (w0 + k < a.nwords) ? a.next[w0 + k] : 0u;
         if (a.st->dir == DIR_BU && w0 + k < a.nwords) cu += __popc(~(a.visited[w0 + k] | x));
         cn += __popc(x);
-        if (x) cm += a.wdeg[w0 + k];
+        if (bu) {
+            if (x) cm += a.wdeg[w0 + k];
+            continue;
+        }
+        // top-down levels: the degrees of the new vertices (the expansion's
+        // next-bit atomics stay fire-and-forget; a returning atomic per
+        // discovered edge, to add degrees there, cost 5 % of the search)
+        while (x) {
+            const int b = __ffs(x) - 1;
+            x &= x - 1;
+            cm += __ldg(a.deg + (w0 + k) * 32 + b);
+        }
     }
     cn = warp_sum_u64(cn);
     cm = warp_sum_u64(cm);
@@ -826,7 +822,6 @@ __device__ void scan_and_decide(const BfsArgs &a)
 
 __global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
 {
-    g5_pdl_sync();
     const uint32_t c = blockIdx.x;
     const int lane = g5_lane(), wid = threadIdx.x >> 5;
     const uint64_t wbeg = (uint64_t)c * kChunkWords + (uint64_t)wid * kWordsPerWarp;
@@ -1131,7 +1126,7 @@ struct g5_bfs {
     uint32_t *ro32 = nullptr;     // uint32 copy of the row offsets (nnz < 2^32)
     uint32_t *first = nullptr;    // first neighbour of each vertex (dense, coalesced)
     uint32_t *multi = nullptr;    // reached more than once in a top-down level
-    uint32_t *wdeg = nullptr;     // per-word degree sums written by the expansion
+    uint32_t *wdeg = nullptr;     // per-word degree sums written by bottom-up
     uint32_t *ulist = nullptr;    // sorted unvisited vertices (n entries)
     unsigned *done = nullptr;     // k_count's finished-block counter
     int64_t *pred = nullptr;
@@ -1168,7 +1163,6 @@ struct g5_bfs {
     int64_t *cur_pred = nullptr;    // parent array of the last search
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     Prof prof;
-    bool pdl = true;  // level kernels as programmatic dependent launches
     int64_t with_edges = 0;  // vertices of degree > 0
     bool ran = false;
     int64_t last_root = -1;
@@ -1194,19 +1188,18 @@ void enqueue_level(g5_bfs *b, const BfsArgs &a, cudaStream_t s, Prof *pf = nullp
 {
     Prof dummy;
     Prof &p = pf ? *pf : dummy;
-    // the level's kernels follow one another as programmatic dependent
-    // launches (each sets up while the one before drains)
-    const bool pdl = b->pdl;
+    // (programmatic dependent launches here measured no faster: 605 against
+    // 603 GTEPS at scale 26, 508 against 516 at scale 24)
     p.mark(KP_EXPAND, s);
-    g5::launch(pdl, k_td, g5::grid_for(8), kBlock, s, a);
-    if (a.ro32) g5::launch(pdl, k_bu<uint32_t>, g5::grid_for(8), kBlock, s, a);
-    else g5::launch(pdl, k_bu<int64_t>, g5::grid_for(8), kBlock, s, a);
+    k_td<<<g5::grid_for(8), kBlock, 0, s>>>(a);
+    if (a.ro32) k_bu<uint32_t><<<g5::grid_for(8), kBlock, 0, s>>>(a);
+    else k_bu<int64_t><<<g5::grid_for(8), kBlock, 0, s>>>(a);
     p.mark(KP_FIXUP, s);
-    if (a.parent_mode != 0) g5::launch(pdl, k_fixup, g5::grid_for(8), kBlock, s, a);
+    if (a.parent_mode != 0) k_fixup<<<g5::grid_for(8), kBlock, 0, s>>>(a);
     p.mark(KP_COUNT, s);
-    g5::launch(pdl, k_count, a.nchunks, kBlock, s, a);
+    k_count<<<a.nchunks, kBlock, 0, s>>>(a);
     p.mark(KP_WRITE, s);
-    g5::launch(pdl, k_write, a.nchunks, kBlock, s, a);
+    k_write<<<a.nchunks, kBlock, 0, s>>>(a);
     p.mark(KP_CODEC, s);
     if (a.codec) {
         g5::codec_encode_launch(b->cw, b->queue, &b->st->nf, b->codec_stream, a.codec,
@@ -1500,16 +1493,7 @@ g5_status g5_bfs_create(g5_graph *g, const g5_bfs_config *cfg, g5_bfs **out)
         for (uint32_t w : iso) isolated += __builtin_popcount(w);
         b->with_edges = g->n - isolated;
     }
-    if (b->cfg.use_graph && (st = build_graph(b, b->pred, &b->exec, &b->graph)) != G5_OK) {
-        // a driver that cannot capture programmatic dependent launches into
-        // the loop's body: the same graph with ordinary launches
-        cudaGetLastError();
-        if (b->graph) cudaGraphDestroy(b->graph);
-        b->graph = nullptr;
-        b->exec = nullptr;
-        b->pdl = false;
-        if ((st = build_graph(b, b->pred, &b->exec, &b->graph)) != G5_OK) return fail(st);
-    }
+    if (b->cfg.use_graph && (st = build_graph(b, b->pred, &b->exec, &b->graph)) != G5_OK) return fail(st);
     b->cur_pred = b->pred;
     *out = b;
     return G5_OK;
