@@ -348,8 +348,8 @@ g5_status g5_batch_serve_step(g5_batch *bt, const int32_t *adm_graph, const int3
  *     sharing one degree-ordered copy of the graph).  While fewer than four
  *     of its queries wait and none of its cohorts runs, they run alone on
  *     the one-root workspaces (a lone query finishes sooner alone); otherwise
- *     they gather, and when a batch workspace is free and 16 queries wait
- *     (or the oldest has waited 10 ms; g5_server_cohort_policy sets both),
+ *     they gather, and when a batch workspace is free and 64 queries wait
+ *     (or the oldest has waited 30 ms; g5_server_cohort_policy sets both),
  *     the queued queries, up to its root slots (at most 64), start together
  *     as one batched search, so under heavy load each adjacency read is
  *     shared by up to 64 queries.  Cohort graphs get the
@@ -371,7 +371,7 @@ g5_status g5_server_create(g5_graph *const *graphs, int ngraphs, size_t mem_budg
 g5_status g5_server_create_modes(g5_graph *const *graphs, int ngraphs, size_t mem_budget,
                                  int keep_results, const int *modes, g5_server **out);
 /* Cohort graphs: a cohort starts when min_roots (1..64) queries wait or
- * the oldest has waited max_wait_ms (defaults 16 and 10 ms). */
+ * the oldest has waited max_wait_ms (defaults 64 and 30 ms). */
 g5_status g5_server_cohort_policy(g5_server *sv, int min_roots, double max_wait_ms);
 /* Slots per graph chosen by the admission rule. */
 g5_status g5_server_slots(g5_server *sv, int *slots);
