@@ -46,6 +46,16 @@ constexpr int kWordsPerThread = kChunkWords / kBlock;
 constexpr uint32_t kTileDefault = 256;  // frontier edges per top-down warp tile
 constexpr int kBuSerialDefault = 8;     // entries a lane scans alone before the warp helps
 constexpr uint32_t kHeavy = 64;    // degree above which top-down sets the parent itself
+// Sparse levels: a top-down level whose frontier has at most kSparseCap
+// adjacency entries, or a bottom-up level sweeping an unvisited list of at
+// most kSparseCap vertices, adds at most kSparseCap vertices; it also
+// appends them to a list and sums their degrees.  If their degrees sum to at
+// most kSparseEdges and the next level is top-down, k_count returns at once
+// and block 0 of k_write turns the list into the next queue, instead of two
+// passes over the whole bitmaps.
+constexpr uint32_t kSparseCap = 4096;
+constexpr uint64_t kSparseEdges = 65536;
+constexpr int kSparseRound = 4;  // list entries per thread per round of the finish
 
 enum : int32_t { DIR_TD = 0, DIR_BU = 1 };
 
@@ -70,6 +80,10 @@ struct BfsState {
     int32_t list_mode;  // 1: this bottom-up level sweeps the unvisited list
     uint64_t codec_acc[2]; // encoded words, values through the codec
     uint64_t ulen;      // unvisited list length
+    uint64_t slen;      // vertices appended to the sparse list by this level
+    uint64_t stm;       // their adjacency entries (degree sum)
+    int32_t sparse;     // 1: this top-down level appends what it discovers
+    int32_t sdone;      // 1: the sparse path took this level (set by k_count)
 };
 
 // Where the in-loop codec's streams are copied when a caller asks for them
@@ -110,6 +124,7 @@ struct BfsArgs {
     unsigned *done;        // blocks of k_count finished (reset by the last one)
     uint32_t *ulist;       // sorted unvisited vertices for a bottom-up level
     uint64_t *chunk_u;     // per chunk: unvisited vertices after the level
+    uint32_t *slist;       // vertices a sparse top-down level discovered (unordered)
     int parent_mode;       // 0 atomicMin, 1 heavy atomicMin + fix-up, 2 first writer + fix-up
     const uint32_t *first; // first (smallest) neighbour of each vertex, 0 for isolated ones
     uint64_t tile;         // frontier edges per top-down warp tile (a power of two >= 32)
@@ -135,6 +150,23 @@ __device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v)
 #pragma unroll
     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
     return v;
+}
+
+// Whether the next top-down level, whose frontier has tm adjacency entries,
+// appends its discoveries to the sparse list (it discovers at most tm
+// vertices, so the list always holds them).  The list is unordered, so
+// searches that encode each level's sorted queue, and the fix-up parent
+// modes, keep the full passes.
+__device__ __forceinline__ int32_t sparse_next(const BfsArgs &a, uint64_t tm)
+{
+    return (a.slist && a.codec == 0 && a.parent_mode == 0 && tm <= kSparseCap) ? 1 : 0;
+}
+
+// Whether a bottom-up level that sweeps an unvisited list of ulen vertices
+// appends what it finds (at most ulen vertices).
+__device__ __forceinline__ int32_t sparse_next_list(const BfsArgs &a, uint64_t ulen)
+{
+    return (a.slist && a.codec == 0 && a.parent_mode == 0 && ulen <= kSparseCap) ? 1 : 0;
 }
 
 // ---- init -----------------------------------------------------------------
@@ -163,6 +195,10 @@ __global__ void k_init(BfsArgs a)
         st->codec_acc[0] = st->codec_acc[1] = 0;
         st->list_mode = 0;
         st->ulen = 0;
+        st->slen = 0;
+        st->stm = 0;
+        st->sparse = s_ok ? sparse_next(a, (uint64_t)s_deg) : 0;
+        st->sdone = 0;
         a.log[0].dir = DIR_TD;
         a.log[0].nf = st->nf;
         a.log[0].mf = st->mf;
@@ -204,6 +240,7 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
     const uint64_t gw = (uint64_t)blockIdx.x * kWarps + wib;
     const uint64_t nw = (uint64_t)gridDim.x * kWarps;
     const uint64_t mf = a.st->mf, nf = a.st->nf;
+    const bool sparse = a.st->sparse != 0;  // the same for the whole grid
     const uint64_t ntiles = (mf + a.tile - 1) >> a.tile_shift;
     if (ntiles > a.max_tiles) {
         if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(&a.st->err, G5_DEVERR_CAPACITY);
@@ -228,6 +265,8 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
             // i(e) <= cur + 32 when every queued vertex has an edge (cur is
             // the vertex of the previous group's last edge); lo == 32 is then
             // exact, and the next boundary confirms it
+            bool claimed = false;  // this lane set v's next bit first (sparse levels)
+            uint32_t cv = 0;
             bool in_range = true;
             if (lo == 32 && e < e1) in_range = (i + 1 > nf) ? false : (a.qoff[i + 1] > e);
             if (e < e1) {
@@ -248,7 +287,14 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
                             // value <= u (even a stale one) makes the atomic moot
                             if ((unsigned long long)a.pred[v] > u)
                                 atomicMin((unsigned long long *)(a.pred + v), u);
-                            if (!(a.next[v >> 5] & bit)) atomicOr(a.next + (v >> 5), bit);
+                            if (!(a.next[v >> 5] & bit)) {
+                                if (sparse) {
+                                    claimed = !(atomicOr(a.next + (v >> 5), bit) & bit);
+                                    cv = v;
+                                } else {
+                                    atomicOr(a.next + (v >> 5), bit);
+                                }
+                            }
                         } else if (a.parent_mode == 1) {
                             if (!(a.next[v >> 5] & bit)) atomicOr(a.next + (v >> 5), bit);
                         } else {
@@ -259,6 +305,23 @@ __device__ void expand_td(const BfsArgs &a, uint64_t &examined)
                             else if (!(a.multi[v >> 5] & bit)) atomicOr(a.multi + (v >> 5), bit);
                         }
                     }
+                }
+            }
+            if (sparse) {
+                // the warp's new vertices go to the list with one atomic, and
+                // their degree sum to the level's with another
+                const unsigned cm = __ballot_sync(0xFFFFFFFFu, claimed);
+                if (cm) {
+                    const int lead = __ffs(cm) - 1;
+                    const uint64_t dsum = warp_sum_u64(claimed ? (uint64_t)__ldg(a.deg + cv) : 0ull);
+                    unsigned long long base = 0;
+                    if (lane == lead) {
+                        base = atomicAdd((unsigned long long *)&a.st->slen, (unsigned long long)__popc(cm));
+                        atomicAdd((unsigned long long *)&a.st->stm, (unsigned long long)dsum);
+                    }
+                    base = __shfl_sync(0xFFFFFFFFu, base, lead);
+                    const uint64_t p = base + __popc(cm & g5_lanemask_lt());
+                    if (claimed && p < kSparseCap) a.slist[p] = cv;
                 }
             }
             cur = __shfl_sync(0xFFFFFFFFu, i, 31);
@@ -546,6 +609,21 @@ __device__ void bottom_up_list(const BfsArgs &a, uint64_t &examined)
         // the word's new bits and their degree sum, and that lane alone
         // updates next and wdeg (one atomic pair per word, not per vertex)
         const unsigned fm = __ballot_sync(0xFFFFFFFFu, found);
+        if (fm && a.st->sparse) {
+            // the warp's new vertices go to the sparse list with one atomic,
+            // their degree sum to the level's with another (the flag is read
+            // here, not kept in a register across the loop)
+            const int lead = __ffs(fm) - 1;
+            const uint64_t dsum = warp_sum_u64(found ? (uint64_t)(e - s) : 0ull);
+            unsigned long long base = 0;
+            if (lane == lead) {
+                base = atomicAdd((unsigned long long *)&a.st->slen, (unsigned long long)__popc(fm));
+                atomicAdd((unsigned long long *)&a.st->stm, (unsigned long long)dsum);
+            }
+            base = __shfl_sync(0xFFFFFFFFu, base, lead);
+            const uint64_t p = base + __popc(fm & g5_lanemask_lt());
+            if (found && p < kSparseCap) a.slist[p] = v;
+        }
         if (fm) {
             const uint32_t wv = mine ? (v >> 5) : 0xFFFFFFFFu;
             const uint32_t wprev = __shfl_up_sync(0xFFFFFFFFu, wv, 1);
@@ -660,9 +738,19 @@ __device__ __forceinline__ void warp_chunk_counts(const BfsArgs &a, uint64_t wbe
 // thread; faster here than the lane-parallel walk of k_write).
 
 __device__ void scan_and_decide(const BfsArgs &a);
+__device__ bool sparse_take(const BfsArgs &a);
 
-__global__ void __launch_bounds__(kBlock) k_count(BfsArgs a)
+__global__ void __launch_bounds__(kBlock, 6) k_count(BfsArgs a)
 {
+    // a level the sparse path takes needs no counts: block 0 of k_write
+    // builds its queue from the list
+    __shared__ int s_take;
+    if (threadIdx.x == 0) {
+        s_take = sparse_take(a) ? 1 : 0;
+        if (blockIdx.x == 0) a.st->sdone = s_take;
+    }
+    __syncthreads();
+    if (s_take) return;
     const uint32_t c = blockIdx.x;
     const uint64_t w0 = (uint64_t)c * kChunkWords + (uint64_t)threadIdx.x * kWordsPerThread;
     const bool bu = a.st->dir == DIR_BU;  // bottom-up levels leave per-word degree sums
@@ -802,6 +890,10 @@ __device__ void scan_and_decide(const BfsArgs &a)
         st->nvisited += tn;
         st->examined = 0;
         st->want_queue = want_q ? 1 : 0;
+        // (list_mode: the next level sweeps the unvisited list of tu vertices)
+        st->sparse = nd == DIR_TD ? sparse_next(a, tm) : (st->list_mode ? sparse_next_list(a, tu) : 0);
+        st->slen = 0;
+        st->stm = 0;
         if (tn && nd == DIR_BU) st->bu_levels += 1;
         if (want_q) a.qoff[tn] = tm;
         if (L + 1 < a.max_levels) {
@@ -820,8 +912,128 @@ __device__ void scan_and_decide(const BfsArgs &a)
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_write(BfsArgs a)
+// Whether the sparse path takes the level that just expanded.  The
+// expansion appended every vertex it added to the list and summed their
+// degrees; the path takes the level when the new vertices have at most
+// kSparseEdges adjacency entries (a larger next level wants the sorted queue
+// the full passes build) and the next level is top-down (a bottom-up one
+// needs the frontier bitmap or the unvisited list k_write builds).  Every
+// block of k_count evaluates it before any block changes the state.
+__device__ bool sparse_take(const BfsArgs &a)
 {
+    const BfsState *st = a.st;
+    if (!st->sparse || st->err || st->slen > kSparseCap || st->stm > kSparseEdges) return false;
+    const uint64_t tn = st->slen, tm = st->stm;
+    const uint64_t mu_after = st->mu >= tm ? st->mu - tm : 0;
+    // the direction rule of scan_and_decide
+    const bool next_bu = st->dir == DIR_BU ? !((double)tn < (double)a.n / a.beta && tn < st->nf)
+                                           : (double)tm > (double)mu_after / a.alpha;
+    return !next_bu;
+}
+
+// Block 0 of k_write on a level the sparse path took: the list becomes the
+// next queue (edge offsets by block scans of the degrees in list order, row
+// bases, tile starts, levels), the new vertices join the visited bitmap,
+// their next words (after a bottom-up level also their per-word degree
+// sums) are cleared, and the level state and the loop condition are set as
+// in scan_and_decide.  Entries are taken kSparseRound per thread per round,
+// all of a round's loads issued before any is used.  The queue is not
+// sorted: the top-down expansion needs only the edge offsets to follow queue
+// order, and parents come from atomicMin whatever the order.
+__device__ void sparse_finish(const BfsArgs &a)
+{
+    __shared__ uint64_t s_w[33];
+    BfsState *st = a.st;
+    const uint32_t len = (uint32_t)st->slen;
+    const int32_t L = st->level;
+    const bool bu = st->dir == DIR_BU;
+    const uint32_t tid = threadIdx.x;
+    uint64_t carry = 0;
+    for (uint32_t base = 0; base < len; base += kSparseRound * kBlock) {
+        uint32_t vv[kSparseRound], dd[kSparseRound];
+        int64_t rs[kSparseRound];
+        uint64_t mps[kSparseRound];
+#pragma unroll
+        for (int k = 0; k < kSparseRound; ++k) {
+            const uint32_t i = base + k * kBlock + tid;
+            vv[k] = i < len ? a.slist[i] : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < kSparseRound; ++k) {
+            const uint32_t i = base + k * kBlock + tid;
+            dd[k] = i < len ? __ldg(a.deg + vv[k]) : 0u;
+            rs[k] = i < len ? __ldg(a.row_off + vv[k]) : 0;
+        }
+#pragma unroll
+        for (int k = 0; k < kSparseRound; ++k) {
+            mps[k] = 0;
+            if (base + k * kBlock < len) {  // the same for every thread
+                uint64_t tot = 0;
+                mps[k] = carry + block_excl_scan_1024(dd[k], s_w, tot);
+                carry += tot;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kSparseRound; ++k) {
+            const uint32_t p = base + k * kBlock + tid;
+            if (p < len) {
+                const uint32_t v = vv[k];
+                const uint64_t mp = mps[k];
+                a.queue[p] = v;
+                a.qoff[p] = mp;
+                a.qbase[p] = rs[k] - (int64_t)mp;
+                uint64_t t = (mp + a.tile - 1) >> a.tile_shift;
+                const uint64_t tend = (mp + dd[k] + a.tile - 1) >> a.tile_shift;
+                for (; t < tend && t < a.max_tiles; ++t) a.tile_start[t] = p;
+                if (a.level) a.level[v] = L + 1;
+                atomicOr(a.visited + (v >> 5), 1u << (v & 31));
+                a.next[v >> 5] = 0;  // every next bit of this level is a list entry
+                if (bu) a.wdeg[v >> 5] = 0;
+            }
+        }
+    }
+    __syncthreads();  // every thread has read the level state
+    if (tid == 0) {
+        const uint64_t tn = len, tm = carry;
+        a.log[L].examined = st->examined;
+        const uint64_t mu_after = st->mu >= tm ? st->mu - tm : 0;
+        st->level = L + 1;
+        st->dir = DIR_TD;
+        st->nf = tn;
+        st->mf = tm;
+        st->mu = mu_after;
+        st->nvisited += tn;
+        st->examined = 0;
+        st->want_queue = 1;
+        st->list_mode = 0;
+        st->ulen = 0;
+        st->sparse = sparse_next(a, tm);
+        st->slen = 0;
+        st->stm = 0;
+        a.qoff[tn] = tm;
+        if (L + 1 < a.max_levels) {
+            a.log[L + 1].dir = DIR_TD;
+            a.log[L + 1].nf = tn;
+            a.log[L + 1].mf = tm;
+            a.log[L + 1].examined = 0;
+        }
+        bool cont = tn > 0 && st->err == 0;
+        if (cont && L + 2 >= a.max_levels) {
+            st->err |= G5_DEVERR_LEVELS;
+            cont = false;
+        }
+        if (a.use_cond) cudaGraphSetConditional(a.cond, cont ? 1u : 0u);
+    }
+}
+
+// (at most 48 registers: the sparse finish must not cost the full pass its
+// fifth block per SM)
+__global__ void __launch_bounds__(kBlock, 5) k_write(BfsArgs a)
+{
+    if (a.st->sdone) {  // the sparse path took the level
+        if (blockIdx.x == 0) sparse_finish(a);
+        return;
+    }
     const uint32_t c = blockIdx.x;
     const int lane = g5_lane(), wid = threadIdx.x >> 5;
     const uint64_t wbeg = (uint64_t)c * kChunkWords + (uint64_t)wid * kWordsPerWarp;
@@ -1137,6 +1349,7 @@ struct g5_bfs {
     int64_t *qbase = nullptr;
     uint32_t *tile_start = nullptr;
     uint64_t *chunks = nullptr;
+    uint32_t *slist = nullptr;    // sparse top-down list (kSparseCap entries)
     BfsState *st = nullptr;
     LevelRec *log = nullptr;
     int64_t *root_dev = nullptr;
@@ -1284,6 +1497,7 @@ g5_status alloc_ws(g5_bfs *b)
     G5_CUDA(cudaMalloc(&b->qbase, sizeof(int64_t) * (size_t)n));
     G5_CUDA(cudaMalloc(&b->tile_start, sizeof(uint32_t) * a.max_tiles));
     G5_CUDA(cudaMalloc(&b->chunks, sizeof(uint64_t) * 3 * a.nchunks));
+    G5_CUDA(cudaMalloc(&b->slist, sizeof(uint32_t) * kSparseCap));
     G5_CUDA(cudaMalloc(&b->st, sizeof(BfsState)));
     G5_CUDA(cudaMalloc(&b->log, sizeof(LevelRec) * (size_t)b->cfg.max_levels));
     G5_CUDA(cudaMalloc(&b->root_dev, sizeof(int64_t)));
@@ -1321,6 +1535,7 @@ g5_status alloc_ws(g5_bfs *b)
     a.chunk_n = b->chunks;
     a.chunk_m = b->chunks + a.nchunks;
     a.chunk_u = b->chunks + 2 * a.nchunks;
+    a.slist = b->slist;
     a.st = b->st;
     a.log = b->log;
     a.root_dev = b->root_dev;
@@ -1390,6 +1605,7 @@ void free_ws(g5_bfs *b)
     cudaFree(b->qbase);
     cudaFree(b->tile_start);
     cudaFree(b->chunks);
+    cudaFree(b->slist);
     cudaFree(b->st);
     cudaFree(b->log);
     cudaFree(b->root_dev);
