@@ -304,6 +304,36 @@ def test_run_many_pipelined_copies_match_oracle():
     with pytest.raises(g5.G5Error):
         b.run_many(np.array([0, n], np.int64), None)
     b.close()
+
+
+def test_parents_stay_exact_across_roots_without_edges():
+    """The parent array is not refilled per search: a root without edges
+    (the only vertex without edges a search writes) is reset by the next
+    search into the same array, in single runs and in both buffers of the
+    pipelined call, and vertices of other components get -1."""
+    rng = np.random.default_rng(11)
+    n = 2000
+    e = rng.integers(0, 1500, size=(3000, 2))  # vertices 1500.. have no edges
+    e = np.concatenate([e, [[1600, 1601], [1601, 1602]]])  # a small second component
+    ro, col = orc.build_csr(n, e)
+    deg = np.diff(ro)
+    iso = [int(v) for v in np.nonzero(deg == 0)[0][:4]]
+    big = int(np.argmax(deg))
+    roots = [iso[0], big, iso[1], iso[2], 1600, iso[3], big, 1601, iso[0]]
+    g = g5.Graph.from_csr(ro, col)
+    for use_graph in (True, False):
+        b = g5.CudaBFS(g, use_graph=use_graph)
+        for r in roots:
+            b.runBFS(r)
+            assert np.array_equal(b.getPredecessor(), orc.bfs(ro, col, r)[0]), (r, use_graph)
+        if use_graph:
+            outs = [np.empty(n, np.int64) for _ in roots]
+            for rep in range(2):
+                b.run_many(np.array(roots, np.int64), outs)
+                for r, o in zip(roots, outs):
+                    assert np.array_equal(o, orc.bfs(ro, col, r)[0]), (rep, r)
+        b.close()
+    g.close()
     g.close()
 
 
