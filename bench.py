@@ -513,7 +513,8 @@ def main():
                                     "scope": "whole search (every kernel of the level loop), algorithmic bytes"},
                          "dram_measured": dram_measured(kern["name"], g.scale, peak, value_rank,
                                                         statistics.mean(nedges) if nedges else None),
-                         "traffic_settings": capture_settings(kern["name"], g.scale, alpha, beta, sizes or {})},
+                         # the headline traffic comes from the per-kind capture
+                         "traffic_settings": capture_settings("k_bu_kinds", g.scale, alpha, beta, sizes or {})},
             "clocks": clocks,
             "validation": {"all_valid": all_valid, "all_min_parent": all_minpar},
             "plain": {"hmean_gteps": value_rank, "mean_ms": statistics.mean(dev_ms),

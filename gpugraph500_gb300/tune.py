@@ -22,7 +22,7 @@ import math
 from typing import Sequence
 
 ALPHAS = (4.0, 14.0, 25.0, 40.0, 70.0, 120.0, 400.0)
-BETAS = (64.0, 200.0, 600.0, 2000.0, 6000.0)
+BETAS = (64.0, 200.0, 600.0, 1000.0, 2000.0, 3000.0, 6000.0)
 TILES = (64, 128, 256, 512)
 SERIALS = (4, 8, 16, 32)
 # the batched search steps 64 roots at once and its bottom-up levels are
