@@ -41,8 +41,12 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
-constexpr int kChunkWords = 2048;  // bitmap words per compaction chunk
-constexpr int kWordsPerThread = kChunkWords / kBlock;
+// Bitmap words per compaction chunk (one block of k_count / k_write each):
+// per graph the smallest of 512, 1024 and 2048 that gives at most
+// kMaxChunks chunks, so small graphs still get many blocks and large ones a
+// short chunk scan (per search, against 2048 everywhere: scale 16 -18 %,
+// scale 20 -15 % with 512; scale 24 -3 % with 1024).
+constexpr int kMaxChunks = 512;
 constexpr uint32_t kTileDefault = 256;  // frontier edges per top-down warp tile
 constexpr int kBuSerialDefault = 8;     // entries a lane scans alone before the warp helps
 constexpr uint32_t kHeavy = 64;    // degree above which top-down sets the parent itself
@@ -107,6 +111,7 @@ struct BfsArgs {
     int64_t nnz;
     uint64_t nwords;
     uint32_t nchunks;
+    int chunk_words;      // bitmap words per compaction chunk: 512, 1024 or 2048
     uint32_t *visited;
     uint32_t *front;
     uint32_t *next;
@@ -704,21 +709,19 @@ __global__ void __launch_bounds__(kBlock) k_fixup(BfsArgs a)
 
 // ---- compaction: count, scan, write ----------------------------------------------
 
-// A compaction chunk is kChunkWords bitmap words; each of the 8 warps of a
+// A compaction chunk is CW bitmap words; each of the 8 warps of a
 // block owns 256 consecutive words and walks them 32 at a time: lane l loads
 // word l (coalesced), then for every non-empty word the lanes read the
 // degrees of its set vertices in one coalesced 128-byte load.
-constexpr int kWordsPerWarp = kChunkWords / kWarps;
-constexpr int kWordIters = kWordsPerWarp / 32;  // words per lane
-
-__device__ __forceinline__ void warp_chunk_counts(const BfsArgs &a, uint64_t wbeg, const uint32_t (&xs)[kWordIters],
+template <int CW>
+__device__ __forceinline__ void warp_chunk_counts(const BfsArgs &a, uint64_t wbeg, const uint32_t (&xs)[CW / kWarps / 32],
                                                   uint64_t &cn, uint64_t &cm)
 {
     const int lane = g5_lane();
     cn = 0;
     cm = 0;
 #pragma unroll
-    for (int i = 0; i < kWordIters; ++i) {
+    for (int i = 0; i < CW / kWarps / 32; ++i) {
         const uint32_t x = xs[i];
         cn += __popc(x);
         unsigned act = __ballot_sync(0xFFFFFFFFu, x != 0u);
@@ -733,15 +736,17 @@ __device__ __forceinline__ void warp_chunk_counts(const BfsArgs &a, uint64_t wbe
     cm = warp_sum_u64(cm);
 }
 
-// Counting: each thread owns kChunkWords / kBlock consecutive words and sums
+// Counting: each thread owns CW / kBlock consecutive words and sums
 // popcounts and the degrees of their set vertices (independent loads per
 // thread; faster here than the lane-parallel walk of k_write).
 
 __device__ void scan_and_decide(const BfsArgs &a);
 __device__ bool sparse_take(const BfsArgs &a);
 
+template <int CW>
 __global__ void __launch_bounds__(kBlock, 6) k_count(BfsArgs a)
 {
+    constexpr int kWordsPerThread = CW / kBlock;
     // a level the sparse path takes needs no counts: block 0 of k_write
     // builds its queue from the list
     __shared__ int s_take;
@@ -752,7 +757,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_count(BfsArgs a)
     __syncthreads();
     if (s_take) return;
     const uint32_t c = blockIdx.x;
-    const uint64_t w0 = (uint64_t)c * kChunkWords + (uint64_t)threadIdx.x * kWordsPerThread;
+    const uint64_t w0 = (uint64_t)c * CW + (uint64_t)threadIdx.x * kWordsPerThread;
     const bool bu = a.st->dir == DIR_BU;  // bottom-up levels leave per-word degree sums
     uint64_t cn = 0, cm = 0, cu = 0;
 #pragma unroll
@@ -1028,15 +1033,18 @@ __device__ void sparse_finish(const BfsArgs &a)
 
 // (at most 48 registers: the sparse finish must not cost the full pass its
 // fifth block per SM)
+template <int CW>
 __global__ void __launch_bounds__(kBlock, 5) k_write(BfsArgs a)
 {
+    constexpr int kWordsPerWarp = CW / kWarps;
+    constexpr int kWordIters = kWordsPerWarp / 32;  // words per lane
     if (a.st->sdone) {  // the sparse path took the level
         if (blockIdx.x == 0) sparse_finish(a);
         return;
     }
     const uint32_t c = blockIdx.x;
     const int lane = g5_lane(), wid = threadIdx.x >> 5;
-    const uint64_t wbeg = (uint64_t)c * kChunkWords + (uint64_t)wid * kWordsPerWarp;
+    const uint64_t wbeg = (uint64_t)c * CW + (uint64_t)wid * kWordsPerWarp;
     const int32_t L = a.st->level;  // index of the new frontier
     const bool want_q = a.st->want_queue != 0;
     const bool want_u = a.st->list_mode != 0;  // next level is bottom-up
@@ -1053,7 +1061,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_write(BfsArgs a)
     }
     // per-warp totals, then the warp's offsets inside the chunk
     uint64_t cn = 0, cm = 0, cu = 0;
-    if (want_q || a.level) warp_chunk_counts(a, wbeg, xs, cn, cm);
+    if (want_q || a.level) warp_chunk_counts<CW>(a, wbeg, xs, cn, cm);
     if (want_u) {
 #pragma unroll
         for (int i = 0; i < kWordIters; ++i) cu += __popc(~(vs[i] | xs[i]));
@@ -1410,9 +1418,17 @@ void enqueue_level(g5_bfs *b, const BfsArgs &a, cudaStream_t s, Prof *pf = nullp
     p.mark(KP_FIXUP, s);
     if (a.parent_mode != 0) k_fixup<<<g5::grid_for(8), kBlock, 0, s>>>(a);
     p.mark(KP_COUNT, s);
-    k_count<<<a.nchunks, kBlock, 0, s>>>(a);
+    switch (a.chunk_words) {
+    case 512: k_count<512><<<a.nchunks, kBlock, 0, s>>>(a); break;
+    case 1024: k_count<1024><<<a.nchunks, kBlock, 0, s>>>(a); break;
+    default: k_count<2048><<<a.nchunks, kBlock, 0, s>>>(a); break;
+    }
     p.mark(KP_WRITE, s);
-    k_write<<<a.nchunks, kBlock, 0, s>>>(a);
+    switch (a.chunk_words) {
+    case 512: k_write<512><<<a.nchunks, kBlock, 0, s>>>(a); break;
+    case 1024: k_write<1024><<<a.nchunks, kBlock, 0, s>>>(a); break;
+    default: k_write<2048><<<a.nchunks, kBlock, 0, s>>>(a); break;
+    }
     p.mark(KP_CODEC, s);
     if (a.codec) {
         g5::codec_encode_launch(b->cw, b->queue, &b->st->nf, b->codec_stream, a.codec,
@@ -1470,7 +1486,13 @@ g5_status alloc_ws(g5_bfs *b)
     a.n = n;
     a.nnz = g->nnz;
     a.nwords = (uint64_t)((n + 31) / 32);
-    a.nchunks = (uint32_t)((a.nwords + kChunkWords - 1) / kChunkWords);
+    a.chunk_words = 2048;
+    for (int cw = 512; cw < 2048; cw *= 2)
+        if ((a.nwords + cw - 1) / cw <= (uint64_t)kMaxChunks) {
+            a.chunk_words = cw;
+            break;
+        }
+    a.nchunks = (uint32_t)((a.nwords + a.chunk_words - 1) / a.chunk_words);
     a.tile = b->cfg.tile_edges;
     a.tile_shift = __builtin_ctz(b->cfg.tile_edges);
     a.bu_serial = b->cfg.bu_serial;
