@@ -1363,6 +1363,7 @@ struct g5_bfs {
     int64_t *root_dev = nullptr;
     uint32_t *codec_stream = nullptr;
     CodecCapture *ccap = nullptr;  // device descriptor (codec searches)
+    bool capture_on = false;       // the level loop launches the stream copy (k_codec_capture)
     g5::CodecWork cw;
     // host mirrors
     int64_t *h_root = nullptr;  // pinned
@@ -1433,7 +1434,8 @@ void enqueue_level(g5_bfs *b, const BfsArgs &a, cudaStream_t s, Prof *pf = nullp
     if (a.codec) {
         g5::codec_encode_launch(b->cw, b->queue, &b->st->nf, b->codec_stream, a.codec,
                                 b->cfg.codec_threshold, s);
-        k_codec_capture<<<g5::grid_for(1), kBlock, 0, s>>>(a.ccap, b->codec_stream, b->cw.scal, b->st);
+        // the stream copy is launched only while a caller has a buffer set
+        if (b->capture_on) k_codec_capture<<<g5::grid_for(1), kBlock, 0, s>>>(a.ccap, b->codec_stream, b->cw.scal, b->st);
         g5::decode_launch_acc(b->cw, b->codec_stream, b->cw.scal + g5::CS_WORDS, b->dqueue, (size_t)a.n,
                               a.codec, b->cfg.codec_threshold, &b->st->nf, b->queue, b->st->codec_acc, s);
     }
@@ -1987,6 +1989,25 @@ g5_status g5_bfs_codec_capture(g5_bfs *b, uint32_t *buf_dev, uint64_t cap_words,
     h.max_rec = buf_dev ? (uint32_t)max_levels : 0;
     G5_CUDA(cudaStreamSynchronize(b->stream));
     G5_CUDA(cudaMemcpy(b->ccap, &h, sizeof h, cudaMemcpyHostToDevice));
+    const bool on = buf_dev != nullptr;
+    if (on != b->capture_on) {
+        // the level loop's graphs launch the copy only while it is on
+        b->capture_on = on;
+        if (b->exec) {
+            cudaGraphExecDestroy(b->exec);
+            cudaGraphDestroy(b->graph);
+            b->exec = nullptr;
+            b->graph = nullptr;
+            G5_TRY(build_graph(b, b->pred, &b->exec, &b->graph));
+        }
+        if (b->exec2) {
+            cudaGraphExecDestroy(b->exec2);
+            cudaGraphDestroy(b->graph2);
+            b->exec2 = nullptr;
+            b->graph2 = nullptr;
+            G5_TRY(build_graph(b, b->pred2, &b->exec2, &b->graph2));
+        }
+    }
     return G5_OK;
 }
 
