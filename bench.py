@@ -548,6 +548,9 @@ def main():
 
 
 BU_KERNEL = "k_bu"
+# graphs of at least this many vertices sweep the unvisited list from their
+# first bottom-up level on (the library's rule; smaller ones sweep the words)
+LIST_FIRST = 1 << 21
 TD_KERNEL = "k_td"
 
 
@@ -562,7 +565,7 @@ def ncu_summary(kernel, scale):
             for ln in f:
                 k, sep, v = ln.partition(":")
                 if sep and k in ("dram_bytes_per_launch", "ncu_mean_us", "search_dram_gbs_ncu",
-                                 "search_dram_bytes_per_search", "sweep_dram_bytes_per_launch",
+                                 "search_dram_bytes_per_search", "first_dram_bytes_per_launch",
                                  "list_dram_bytes_per_launch"):
                     out[k] = float(v)
                 elif sep and k == "settings":
@@ -574,10 +577,10 @@ def ncu_summary(kernel, scale):
 
 
 def kind_traffic(kind, scale):
-    """DRAM bytes per launch of one k_bu launch kind ("bu_sweep" or
+    """DRAM bytes per launch of one k_bu launch kind ("bu_first" or
     "bu_list") from the committed summary profiles/k_bu_kinds_scale<s>.txt,
     or None."""
-    key = {"bu_sweep": "sweep_dram_bytes_per_launch", "bu_list": "list_dram_bytes_per_launch"}.get(kind)
+    key = {"bu_first": "first_dram_bytes_per_launch", "bu_list": "list_dram_bytes_per_launch"}.get(kind)
     return ncu_summary("k_bu_kinds", scale).get(key) if key else None
 
 
@@ -632,13 +635,15 @@ def kernel_roofline(g5, g, roots, alpha, beta, peak, sizes=None):
     one as the headline.  C = candidates of a bottom-up level (vertices with
     edges not yet visited), off = bytes of a row offset (4 while nnz < 2^32).
     Per launch:
-      k_bu word sweep (first bottom-up level): N/8 visited words + (off + 4) C
-        (each candidate's row start and its first neighbour from the dense
-        copy; the row end is the next start) + 4 E_bu (adjacency read until
-        the first hit) + N/8 frontier probes + N/8 next words
-      k_bu list sweep (later bottom-up levels): 4 C (the unvisited list) +
-        (2 off + 4) C (row bounds and first neighbour of each listed vertex)
-        + 4 E_bu + N/8 frontier probes
+      k_bu over the list of unvisited vertices: 4 C (the list) + (2 off + 4) C
+        (row bounds and first neighbour of each listed vertex) + 4 E_bu
+        (adjacency read until the first hit) + N/8 frontier probes
+      k_bu over the bitmap words (the library's first bottom-up level of a run
+        on graphs of fewer than 2^21 vertices): N/8 visited words + (off + 4) C
+        (row start and dense first neighbour) + 4 E_bu + N/8 frontier probes +
+        N/8 next words
+      the first bottom-up level of a run ("bu_first", the largest C) is
+      reported apart from the later ones ("bu_list")
       k_td: 20 |F| (queue entry, edge offset, row base) + 4 E_td + N/8 visited."""
     pb = g5.CudaBFS(g, alpha=alpha, beta=beta, use_graph=False, profile=True, **(sizes or {}))
     n = g.n
@@ -647,7 +652,7 @@ def kernel_roofline(g5, g, roots, alpha, beta, peak, sizes=None):
     with_edges = int(np.count_nonzero(np.diff(ro)))
     del ro
     tot = {}
-    acc = {k: [0.0, 0.0, 0] for k in ("bu_sweep", "bu_list", "td")}  # bytes, ms, launches
+    acc = {k: [0.0, 0.0, 0] for k in ("bu_first", "bu_list", "td")}  # bytes, ms, launches
     for r in roots:
         code = pb.run(int(r), None, None, stats=True)
         if code != 0:
@@ -664,12 +669,12 @@ def kernel_roofline(g5, g, roots, alpha, beta, peak, sizes=None):
             d, nf, _, read = (int(x) for x in row)
             seen += nf
             cand = max(with_edges - seen, 0)
-            if d == 1 and not prev_bu:
+            if d == 1 and not prev_bu and n < LIST_FIRST:
                 b = 3 * n / 8 + (off + 4) * cand + 4 * read
-                key = "bu_sweep"
+                key = "bu_first"
             elif d == 1:
                 b = (4 + 2 * off + 4) * cand + 4 * read + n / 8
-                key = "bu_list"
+                key = "bu_list" if prev_bu else "bu_first"
             else:
                 b = 20 * nf + 4 * read + n / 8
                 key = "td"

@@ -42,11 +42,16 @@ namespace {
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
 // Bitmap words per compaction chunk (one block of k_count / k_write each):
-// per graph the smallest of 512, 1024 and 2048 that gives at most
+// per graph the smallest of 256, 512, 1024 and 2048 that gives at most
 // kMaxChunks chunks, so small graphs still get many blocks and large ones a
 // short chunk scan (per search, against 2048 everywhere: scale 16 -18 %,
-// scale 20 -15 % with 512; scale 24 -3 % with 1024).
+// scale 20 -15 % with 512, each about 3 % more with 256; scale 24 -3 % with
+// 1024).
 constexpr int kMaxChunks = 512;
+// Graphs of at least this many vertices sweep the unvisited list from their
+// first bottom-up level on (scale 22: 1.7 % faster per search; scale 20: 3 %
+// slower).
+constexpr int64_t kListFirst = (int64_t)1 << 21;
 constexpr uint32_t kTileDefault = 256;  // frontier edges per top-down warp tile
 constexpr int kBuSerialDefault = 8;     // entries a lane scans alone before the warp helps
 constexpr uint32_t kHeavy = 64;    // degree above which top-down sets the parent itself
@@ -111,7 +116,8 @@ struct BfsArgs {
     int64_t nnz;
     uint64_t nwords;
     uint32_t nchunks;
-    int chunk_words;      // bitmap words per compaction chunk: 512, 1024 or 2048
+    int chunk_words;      // bitmap words per compaction chunk: 256, 512, 1024 or 2048
+    int list_first;       // 1: the first bottom-up level of a run sweeps the unvisited list too
     uint32_t *visited;
     uint32_t *front;
     uint32_t *next;
@@ -512,10 +518,11 @@ __device__ void sweep(const BfsArgs &a, uint64_t &examined)
     }
 }
 
-// First bottom-up level: one warp per 32-vertex word, software-pipelined so
-// that a word's visited bits are loaded two steps and its candidates' row
-// offsets one step before the word is scanned; the scan of one word then
-// overlaps the loads of the next two instead of waiting on each in turn.
+// First bottom-up level on graphs of fewer than kListFirst vertices: one warp
+// per 32-vertex word, software-pipelined so that a word's visited bits are
+// loaded two steps and its candidates' row offsets one step before the word
+// is scanned; the scan of one word then overlaps the loads of the next two
+// instead of waiting on each in turn.
 template <typename Off>
 __device__ void sweep_bu(const BfsArgs &a, uint64_t &examined)
 {
@@ -678,7 +685,8 @@ __global__ void __launch_bounds__(kBlock, 8) k_td(BfsArgs a)
 }
 
 // Bottom-up expansion of the level (no-op when the level is top-down): the
-// word sweep for the first bottom-up level, the unvisited list afterwards.
+// list of unvisited vertices, or on small graphs the bitmap words for the
+// first bottom-up level of a run.
 template <typename Off>
 __global__ void __launch_bounds__(kBlock, 8) k_bu(BfsArgs a)
 {
@@ -759,11 +767,13 @@ __global__ void __launch_bounds__(kBlock, 6) k_count(BfsArgs a)
     const uint32_t c = blockIdx.x;
     const uint64_t w0 = (uint64_t)c * CW + (uint64_t)threadIdx.x * kWordsPerThread;
     const bool bu = a.st->dir == DIR_BU;  // bottom-up levels leave per-word degree sums
+    // unvisited vertices (the list length for a following bottom-up level)
+    const bool count_u = bu || a.list_first;
     uint64_t cn = 0, cm = 0, cu = 0;
 #pragma unroll
     for (int k = 0; k < kWordsPerThread; ++k) {
         uint32_t x = (w0 + k < a.nwords) ? a.next[w0 + k] : 0u;
-        if (a.st->dir == DIR_BU && w0 + k < a.nwords) cu += __popc(~(a.visited[w0 + k] | x));
+        if (count_u && w0 + k < a.nwords) cu += __popc(~(a.visited[w0 + k] | x));
         cn += __popc(x);
         if (bu) {
             if (x) cm += a.wdeg[w0 + k];
@@ -883,9 +893,13 @@ __device__ void scan_and_decide(const BfsArgs &a)
             if ((double)tn < (double)a.n / a.beta && tn < st->nf) nd = DIR_TD;
         }
         const bool want_q = (nd == DIR_TD) || a.codec != 0;
-        // a bottom-up level right after another one sweeps the unvisited
-        // list k_write is about to write; the first one sweeps the words
-        st->list_mode = (st->dir == DIR_BU && nd == DIR_BU) ? 1 : 0;
+        // a bottom-up level sweeps the list of unvisited vertices that
+        // k_write is about to write; on graphs of fewer than kListFirst
+        // vertices the first one of a run sweeps the bitmap words instead
+        // (there the list costs more to build than it saves; on large graphs
+        // the word sweep leaves the lanes of visited vertices idle: the list
+        // is 7 % faster per search at scale 26, 4 % at 24)
+        st->list_mode = (nd == DIR_BU && (st->dir == DIR_BU || a.list_first)) ? 1 : 0;
         st->ulen = tu;
         st->level = L + 1;
         st->dir = nd;
@@ -1420,12 +1434,14 @@ void enqueue_level(g5_bfs *b, const BfsArgs &a, cudaStream_t s, Prof *pf = nullp
     if (a.parent_mode != 0) k_fixup<<<g5::grid_for(8), kBlock, 0, s>>>(a);
     p.mark(KP_COUNT, s);
     switch (a.chunk_words) {
+    case 256: k_count<256><<<a.nchunks, kBlock, 0, s>>>(a); break;
     case 512: k_count<512><<<a.nchunks, kBlock, 0, s>>>(a); break;
     case 1024: k_count<1024><<<a.nchunks, kBlock, 0, s>>>(a); break;
     default: k_count<2048><<<a.nchunks, kBlock, 0, s>>>(a); break;
     }
     p.mark(KP_WRITE, s);
     switch (a.chunk_words) {
+    case 256: k_write<256><<<a.nchunks, kBlock, 0, s>>>(a); break;
     case 512: k_write<512><<<a.nchunks, kBlock, 0, s>>>(a); break;
     case 1024: k_write<1024><<<a.nchunks, kBlock, 0, s>>>(a); break;
     default: k_write<2048><<<a.nchunks, kBlock, 0, s>>>(a); break;
@@ -1489,12 +1505,13 @@ g5_status alloc_ws(g5_bfs *b)
     a.nnz = g->nnz;
     a.nwords = (uint64_t)((n + 31) / 32);
     a.chunk_words = 2048;
-    for (int cw = 512; cw < 2048; cw *= 2)
+    for (int cw = 256; cw < 2048; cw *= 2)
         if ((a.nwords + cw - 1) / cw <= (uint64_t)kMaxChunks) {
             a.chunk_words = cw;
             break;
         }
     a.nchunks = (uint32_t)((a.nwords + a.chunk_words - 1) / a.chunk_words);
+    a.list_first = n >= kListFirst ? 1 : 0;
     a.tile = b->cfg.tile_edges;
     a.tile_shift = __builtin_ctz(b->cfg.tile_edges);
     a.bu_serial = b->cfg.bu_serial;
@@ -1649,14 +1666,14 @@ void free_ws(g5_bfs *b)
 // candidates of a bottom-up level (vertices with edges not yet visited) and
 // off the bytes of a row offset, per level: top-down 20|F| + 4 E_td + N/8
 // (queue entry, edge offset and row base per frontier vertex, adjacency,
-// visited bitmap); the first bottom-up level of a run 3N/8 + (off + 4) C +
+// visited bitmap); a bottom-up sweep of the unvisited list (2 off + 8) C +
+// 4 E_bu + N/8 (the list, row bounds and first neighbour of each listed
+// vertex, adjacency until the first hit, frontier); a sweep of the bitmap
+// words (the first bottom-up level on small graphs) 3N/8 + (off + 4) C +
 // 4 E_bu (visited, frontier and next bitmaps, each candidate's row start and
-// dense first neighbour, adjacency until the first hit); a later one
-// (2 off + 8) C + 4 E_bu + N/8 (the unvisited list, row bounds and first
-// neighbour of each listed vertex, adjacency, frontier); plus 4 + 9 bytes
-// per vertex the level adds (queue, parent, level) after top-down and 9
-// after bottom-up.
-int64_t alg_bytes(const LevelRec *log, int nlev, int64_t n, int64_t with_edges, int off)
+// dense first neighbour, adjacency); plus 4 + 9 bytes per vertex the level
+// adds (queue, parent, level) after top-down and 9 after bottom-up.
+int64_t alg_bytes(const LevelRec *log, int nlev, int64_t n, int64_t with_edges, int off, bool list_first)
 {
     double B = 0, seen = 0;
     for (int L = 0; L < nlev; ++L) {
@@ -1667,7 +1684,7 @@ int64_t alg_bytes(const LevelRec *log, int nlev, int64_t n, int64_t with_edges, 
         const double E = 4.0 * (double)log[L].examined;
         if (log[L].dir == DIR_TD)
             B += 20.0 * nf + E + (double)n / 8.0 + 13.0 * nf1;
-        else if (L == 0 || log[L - 1].dir != DIR_BU)
+        else if (!list_first && (L == 0 || log[L - 1].dir != DIR_BU))
             B += 3.0 * (double)n / 8.0 + (off + 4.0) * cand + E + 9.0 * nf1;
         else
             B += (2.0 * off + 8.0) * cand + E + (double)n / 8.0 + 9.0 * nf1;
@@ -1807,7 +1824,7 @@ g5_status g5_bfs_run(g5_bfs *b, int64_t root, int64_t *pred_out, int32_t *level_
         }
         stats->codec_words = (int64_t)hs.codec_acc[0];
         stats->codec_values = (int64_t)hs.codec_acc[1];
-        stats->alg_bytes = alg_bytes(b->h_log, nlev, b->g->n, b->with_edges, b->ro32 ? 4 : 8);
+        stats->alg_bytes = alg_bytes(b->h_log, nlev, b->g->n, b->with_edges, b->ro32 ? 4 : 8, b->args.list_first != 0);
         float ms = 0;
         cudaEventElapsedTime(&ms, b->ev0, b->ev1);
         stats->device_ms = ms;

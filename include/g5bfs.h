@@ -173,11 +173,11 @@ typedef struct g5_bfs_stats {
     int64_t codec_words;      /* sum of encoded words over levels                 */
     int64_t codec_values;     /* sum of values that went through the codec        */
     int64_t alg_bytes;        /* algorithmic HBM bytes of the search: per level,
-                                 top-down 20|F| + 4 E + N/8; first bottom-up
-                                 3N/8 + (off + 4) C + 4 E; later bottom-up
-                                 (2 off + 8) C + 4 E + N/8 (C candidates, off
-                                 row-offset bytes); + 13 or 9 bytes per vertex
-                                 added (queue, parent, level)                   */
+                                 top-down 20|F| + 4 E + N/8; bottom-up (a sweep
+                                 of the unvisited list) (2 off + 8) C + 4 E +
+                                 N/8 (C candidates, off row-offset bytes); + 13
+                                 or 9 bytes per vertex added (queue, parent,
+                                 level)                                          */
     double device_ms;         /* device time of the search (CUDA events)          */
     double kernel_ms[8];      /* profile mode: prologue, expand, fixup, count,
                                  scan, write, codec, unused (ms, summed)          */
