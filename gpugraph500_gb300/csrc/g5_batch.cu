@@ -62,6 +62,9 @@ struct GraphDesc {
     const uint32_t *perm;    // original id -> new id
     const int64_t *ostart;   // by original id: start of the vertex's row in col
     const uint32_t *odeg;    // by original id: its degree
+    const uint32_t *blist;   // original ids of the vertices with edges, ascending
+    uint64_t nblist;         // their count
+    uint64_t step0;          // first bottom-up warp step of this graph
     int64_t n;
     int64_t nnz;
     uint64_t vbase;      // first global vertex id
@@ -103,6 +106,8 @@ struct BArgs {
     uint64_t max_tiles;
     uint64_t *chunk_n, *chunk_m;
     uint8_t *chunk_live;    // per chunk: bit 0 next frontier not empty, bit 1 nothing for k_bwrite
+    const uint8_t *step_graph; // graph of each bottom-up warp step (32 list entries)
+    uint64_t nsteps;
     BState *st;
     const int64_t *roots;   // device copy of the roots (graph-major)
     const int32_t *root_off;
@@ -244,21 +249,24 @@ __global__ void __launch_bounds__(kB, 4) k_bbu(BArgs a)
     const uint64_t gw = ((uint64_t)blockIdx.x * kB + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * kB) >> 5;
     uint64_t examined = 0;
-    for (uint64_t w = gw; w < a.ntot / 32; w += nw) {
-        // vertices in original-id order: high-degree vertices, which have
-        // the lowest new ids, spread over the warps
-        const GraphDesc &d = a.gd[graph_of(a, w * 32)];
+    for (uint64_t w = gw; w < a.nsteps; w += nw) {
+        // the graph's vertices with edges in original-id order, 32 per warp
+        // step (vertices without edges are never reached, and half the
+        // vertices of a Kronecker graph have none): high-degree vertices,
+        // which have the lowest new ids, spread over the warps
+        const GraphDesc &d = a.gd[a.step_graph[w]];
         if (d.dir != BU || d.nf == 0) continue;
-        const uint64_t ol = w * 32 + lane - d.vbase;
+        const uint64_t li = (w - d.step0) * 32 + lane;
+        const uint64_t ol = li < d.nblist ? __ldg(d.blist + li) : 0u;
         const uint32_t R = (uint32_t)d.nroots;
-        // new id and row bounds, indexed by original id: three coalesced
-        // loads issued together
+        // new id and row bounds, indexed by original id: three loads issued
+        // together (nearly coalesced: the list is ascending)
         uint32_t vl = 0, dg = 0;
         int64_t s = 0;
-        if ((int64_t)ol < d.n) {
+        if (li < d.nblist) {
             vl = __ldg(d.perm + ol);
             s = __ldg(d.ostart + ol);
-            dg = __ldg(d.odeg + ol);  // 0: no edges, never reached
+            dg = __ldg(d.odeg + ol);
         }
         const int64_t e = s + dg;
         const uint64_t v = d.vbase + vl;
@@ -862,6 +870,7 @@ struct g5_batch {
     cudaStream_t stream = nullptr;
     GraphDesc *gd = nullptr;
     uint8_t *chunk_graph = nullptr;
+    uint8_t *step_graph = nullptr;  // graph of each bottom-up warp step
     uint32_t *deg = nullptr;
     uint32_t *iso = nullptr;
     uint64_t *words = nullptr;  // vis | front | next
@@ -969,6 +978,7 @@ void free_batch(g5_batch *b)
     cudaFree(b->qbase);
     cudaFree(b->tile_start);
     cudaFree(b->chunks);
+    cudaFree(b->step_graph);
     cudaFree(b->st);
     cudaFree(b->roots);
     cudaFree(b->root_off);
@@ -984,6 +994,11 @@ void free_batch(g5_batch *b)
     b->owned.clear();
     if (b->stream) cudaStreamDestroy(b->stream);
 }
+
+struct HasEdges {
+    const uint32_t *deg;
+    __device__ bool operator()(const uint32_t &v) const { return deg[v] > 0; }
+};
 
 // Degree-ordered copy of g on b's stream: new ids by descending degree (ties
 // by original id), rows in new-id order, each row's neighbours renamed but in
@@ -1027,7 +1042,23 @@ g5_status build_relabel(g5_batch *b, const g5_graph *g, GraphDesc &d)
     G5_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, t2, row2, row2, n + 1, s));
     k_rl_cols<<<blocks, 256, 0, s>>>(g->row_off, g->col, orig, perm, row2, n, col2);
     k_rl_orig<<<blocks, 256, 0, s>>>(perm, row2, n, ostart, odeg);
+    // the bottom-up sweep's vertex list: original ids with edges, ascending
+    // (ids still holds 0..n-1: the sort wrote its values elsewhere)
+    uint32_t *blist = nullptr;
+    if (!alloc((void **)&blist, sizeof(uint32_t) * n)) return G5_ERR_OOM;
+    g5::DevBuf<int64_t> nsel;
+    if (nsel.alloc(1) != G5_OK) return G5_ERR_OOM;
+    size_t t3 = 0;
+    const HasEdges pred{odeg};
+    G5_CUDA(cub::DeviceSelect::If(nullptr, t3, ids.p, blist, nsel.p, (int64_t)n, pred, s));
+    g5::DevBuf<uint8_t> tmp3;
+    if (tmp3.alloc(t3) != G5_OK) return G5_ERR_OOM;
+    G5_CUDA(cub::DeviceSelect::If(tmp3.p, t3, ids.p, blist, nsel.p, (int64_t)n, pred, s));
+    int64_t nl = 0;
+    G5_CUDA(cudaMemcpyAsync(&nl, nsel.p, sizeof nl, cudaMemcpyDeviceToHost, s));
     G5_CUDA(cudaStreamSynchronize(s));
+    d.blist = blist;
+    d.nblist = (uint64_t)nl;
     return G5_OK;
 }
 
@@ -1092,14 +1123,27 @@ g5_status batch_create_impl(g5_graph *const *graphs, int ngraphs, const g5_batch
             d.perm = o.perm;
             d.ostart = o.ostart;
             d.odeg = o.odeg;
+            d.blist = o.blist;
+            d.nblist = o.nblist;
             continue;
         }
         const g5_status rs = build_relabel(b, graphs[i], b->hgd[i]);
         if (rs != G5_OK) return fail(rs);
     }
+    // bottom-up warp steps: each graph's list in 32-entry steps, graphs one
+    // after another
+    std::vector<uint8_t> sg;
+    for (int i = 0; i < ngraphs; ++i) {
+        GraphDesc &d = b->hgd[i];
+        d.step0 = sg.size();
+        const uint64_t steps = (d.nblist + 31) / 32;
+        sg.insert(sg.end(), steps, (uint8_t)i);
+    }
+    a.nsteps = sg.size();
 #define B_ALLOC(ptr, bytes) \
     if (cudaMalloc(&(ptr), (bytes)) != cudaSuccess) return fail(G5_ERR_OOM)
     B_ALLOC(b->gd, sizeof(GraphDesc) * ngraphs);
+    B_ALLOC(b->step_graph, sg.size() + 1);
     B_ALLOC(b->chunk_graph, cg.size());
     B_ALLOC(b->deg, sizeof(uint32_t) * vb);
     B_ALLOC(b->iso, sizeof(uint32_t) * (vb / 32));
@@ -1118,7 +1162,8 @@ g5_status batch_create_impl(g5_graph *const *graphs, int ngraphs, const g5_batch
         cudaMallocHost(&b->h_root_off, sizeof(int32_t) * (ngraphs + 1)) != cudaSuccess ||
         cudaMallocHost(&b->h_st, sizeof(BState)) != cudaSuccess)
         return fail(G5_ERR_OOM);
-    if (cudaMemcpy(b->chunk_graph, cg.data(), cg.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+    if ((!sg.empty() && cudaMemcpy(b->step_graph, sg.data(), sg.size(), cudaMemcpyHostToDevice) != cudaSuccess) ||
+        cudaMemcpy(b->chunk_graph, cg.data(), cg.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b->gd, b->hgd.data(), sizeof(GraphDesc) * ngraphs, cudaMemcpyHostToDevice) != cudaSuccess)
         return fail(G5_ERR_CUDA);
     a.gd = b->gd;
@@ -1135,6 +1180,7 @@ g5_status batch_create_impl(g5_graph *const *graphs, int ngraphs, const g5_batch
     a.chunk_n = b->chunks;
     a.chunk_m = b->chunks + a.nchunks;
     a.chunk_live = reinterpret_cast<uint8_t *>(b->chunks + 2 * (uint64_t)a.nchunks);
+    a.step_graph = b->step_graph;
     a.st = b->st;
     a.roots = b->roots;
     a.root_off = b->root_off;
