@@ -511,8 +511,7 @@ def main():
                          "peak_kind": peak_kind + " (copy, burst)", "kernel": kern,
                          "search": {"achieved": achieved, "frac": achieved / peak,
                                     "scope": "whole search (every kernel of the level loop), algorithmic bytes"},
-                         "dram_measured": dram_measured(kern["name"], g.scale, peak, value_rank,
-                                                        statistics.mean(nedges) if nedges else None),
+                         "dram_measured": dram_measured(g.scale, peak),
                          # the headline traffic comes from the per-kind capture
                          "traffic_settings": capture_settings("k_bu_kinds", g.scale, alpha, beta, sizes or {})},
             "clocks": clocks,
@@ -556,17 +555,18 @@ TD_KERNEL = "k_td"
 
 def ncu_summary(kernel, scale):
     """The 'key: value' lines of the committed ncu summary
-    profiles/<kernel>_scale<scale>.txt (DRAM bytes per launch, mean launch
-    time, whole-search DRAM throughput), as floats; {} when absent."""
+    profiles/<kernel>_scale<scale>.txt (DRAM bytes per launch and mean launch
+    time per launch kind, the capture's settings), as floats; {} when
+    absent."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_scale{scale}.txt")
     out = {}
     try:
         with open(path) as f:
             for ln in f:
                 k, sep, v = ln.partition(":")
-                if sep and k in ("dram_bytes_per_launch", "ncu_mean_us", "search_dram_gbs_ncu",
-                                 "search_dram_bytes_per_search", "first_dram_bytes_per_launch",
-                                 "list_dram_bytes_per_launch"):
+                if sep and k in ("first_dram_bytes_per_launch", "list_dram_bytes_per_launch",
+                                 "first_ncu_us_scale24",
+                                 "first_dram_bytes_scale24", "list_ncu_us_scale24", "list_dram_bytes_scale24"):
                     out[k] = float(v)
                 elif sep and k == "settings":
                     # "alpha=14 beta=2000 tile_edges=128 bu_serial=8"
@@ -584,12 +584,6 @@ def kind_traffic(kind, scale):
     return ncu_summary("k_bu_kinds", scale).get(key) if key else None
 
 
-def ncu_traffic(kernel, scale):
-    """DRAM bytes per launch of `kernel` at `scale` from the committed ncu
-    summary, or None."""
-    return ncu_summary(kernel, scale).get("dram_bytes_per_launch")
-
-
 def capture_settings(kernel, scale, alpha, beta, sizes):
     """The thresholds and sizes of the committed capture, and whether they are
     this run's (the per-launch traffic depends on the launch mix they give)."""
@@ -601,31 +595,23 @@ def capture_settings(kernel, scale, alpha, beta, sizes):
     return {"capture": cap, "run": run, "match": all(cap.get(k) == v for k, v in run.items())}
 
 
-def dram_measured(kernel, scale, peak, gteps=None, edges_per_search=None):
-    """Measured DRAM throughput from the committed ncu launch list: the
-    kernel's DRAM bytes over its own ncu durations (one capture for both, so
-    cold-cache and serialised), and the same for every kernel of the level
-    loop.  With the run's TEPS and mean Graph500 edge count per search, also
-    the "measured bytes per traversed edge" view: the capture's DRAM bytes per
-    search over the edges, times the run's TEPS, against the nominal 8 TB/s
-    and the measured peak (cold-cache bytes, so an upper estimate).  Reported
-    beside the algorithmic roofline, not instead of it."""
-    s = ncu_summary(kernel, scale)
-    if "dram_bytes_per_launch" not in s or "ncu_mean_us" not in s:
+def dram_measured(scale, peak):
+    """Measured DRAM throughput of the bottom-up expansion from the committed
+    single-kernel ncu capture at scale 24, summarised in
+    profiles/k_bu_kinds_scale<s>.txt: each launch kind's DRAM bytes over its
+    own ncu durations (one capture for both, so cold-cache and serialised).
+    Reported beside the algorithmic roofline, not instead of it."""
+    s = ncu_summary("k_bu_kinds", scale)
+    out = {}
+    for kind, key in (("bu_first", "first"), ("bu_list", "list")):
+        b, us = s.get(f"{key}_dram_bytes_scale24"), s.get(f"{key}_ncu_us_scale24")
+        if b and us:
+            gbs = b / (us * 1e-6) / 1e9
+            out[kind] = {"gbs": gbs, "frac": gbs / peak, "bytes_per_launch": b, "ncu_us": us}
+    if not out:
         return None
-    gbs = s["dram_bytes_per_launch"] / (s["ncu_mean_us"] * 1e-6) / 1e9
-    out = {"kernel_gbs": gbs, "kernel_frac": gbs / peak,
-           "source": f"ncu launch list, profiles/{kernel}_scale{scale}.txt (bytes and durations of one capture)"}
-    if "search_dram_gbs_ncu" in s:
-        out["search_gbs"] = s["search_dram_gbs_ncu"]
-        out["search_frac"] = s["search_dram_gbs_ncu"] / peak
-    if "search_dram_bytes_per_search" in s and gteps and edges_per_search:
-        bpe = s["search_dram_bytes_per_search"] / edges_per_search
-        gbs = bpe * gteps
-        out["bytes_per_teps_edge"] = bpe
-        out["at_value_gbs"] = gbs
-        out["at_value_frac_of_8tbs"] = gbs / 8000.0
-        out["at_value_frac"] = gbs / peak
+    out["source"] = (f"ncu, k_bu alone at scale 24, profiles/k_bu_kinds_scale{scale}.txt "
+                     "(bytes and durations of one capture)")
     return out
 
 

@@ -17,42 +17,38 @@ def bench():
 
 
 def test_committed_summary_parses(bench):
-    s = bench.ncu_summary("k_bu", 26)
-    assert {"dram_bytes_per_launch", "ncu_mean_us", "search_dram_gbs_ncu"} <= set(s)
-    assert bench.ncu_traffic("k_bu", 26) == s["dram_bytes_per_launch"] > 0
-    m = bench.dram_measured("k_bu", 26, 6786.9)
-    gbs = s["dram_bytes_per_launch"] / (s["ncu_mean_us"] * 1e-6) / 1e9
-    assert m["kernel_gbs"] == pytest.approx(gbs)
-    assert m["kernel_frac"] == pytest.approx(gbs / 6786.9)
-    assert m["search_frac"] == pytest.approx(s["search_dram_gbs_ncu"] / 6786.9)
+    s = bench.ncu_summary("k_bu_kinds", 26)
+    assert {"first_dram_bytes_per_launch", "list_dram_bytes_per_launch",
+            "first_ncu_us_scale24", "first_dram_bytes_scale24"} <= set(s)
+    # the scale-26 traffic is the scale-24 capture times 4
+    assert s["first_dram_bytes_per_launch"] == pytest.approx(4 * s["first_dram_bytes_scale24"])
+    assert s["list_dram_bytes_per_launch"] == pytest.approx(4 * s["list_dram_bytes_scale24"])
+    assert bench.kind_traffic("bu_first", 26) == s["first_dram_bytes_per_launch"] > 0
+    assert bench.kind_traffic("td", 26) is None
+    m = bench.dram_measured(26, 6786.9)
+    gbs = s["first_dram_bytes_scale24"] / (s["first_ncu_us_scale24"] * 1e-6) / 1e9
+    assert m["bu_first"]["gbs"] == pytest.approx(gbs)
+    assert m["bu_first"]["frac"] == pytest.approx(gbs / 6786.9)
     # a measured fraction far above 1 would mean the summary is not the kernel's
-    assert 0 < m["kernel_frac"] < 1.2 and 0 < m["search_frac"] < 1.2
-
-
-def test_bytes_per_edge_view(bench):
-    s = bench.ncu_summary("k_bu", 26)
-    m = bench.dram_measured("k_bu", 26, 6786.9, 640.0, 1.07e9)
-    bpe = s["search_dram_bytes_per_search"] / 1.07e9
-    assert m["bytes_per_teps_edge"] == pytest.approx(bpe)
-    assert m["at_value_gbs"] == pytest.approx(bpe * 640.0)
-    assert m["at_value_frac_of_8tbs"] == pytest.approx(bpe * 640.0 / 8000.0)
-    assert "at_value_gbs" not in bench.dram_measured("k_bu", 26, 6786.9)
+    for kind in ("bu_first", "bu_list"):
+        assert 0 < m[kind]["frac"] < 1.2
 
 
 def test_capture_settings(bench):
-    cap = bench.ncu_summary("k_bu", 26)["settings"]
+    cap = bench.ncu_summary("k_bu_kinds", 26)["settings"]
     assert set(cap) == {"alpha", "beta", "tile_edges", "bu_serial"}
-    same = bench.capture_settings("k_bu", 26, cap["alpha"], cap["beta"],
+    same = bench.capture_settings("k_bu_kinds", 26, cap["alpha"], cap["beta"],
                                   {"tile_edges": int(cap["tile_edges"]), "bu_serial": int(cap["bu_serial"])})
     assert same["match"]
-    other = bench.capture_settings("k_bu", 26, cap["alpha"] * 2, cap["beta"], {})
+    other = bench.capture_settings("k_bu_kinds", 26, cap["alpha"] * 2, cap["beta"], {})
     assert not other["match"] and other["run"]["tile_edges"] == 256
 
 
 def test_missing_summary(bench):
-    assert bench.ncu_summary("k_bu", 99) == {}
-    assert bench.ncu_traffic("k_bu", 99) is None
-    assert bench.dram_measured("k_bu", 99, 6786.9) is None
+    assert bench.ncu_summary("k_bu_kinds", 99) == {}
+    assert bench.kind_traffic("bu_first", 99) is None
+    assert bench.dram_measured(99, 6786.9) is None
+    assert bench.capture_settings("k_bu_kinds", 99, 25, 1000, {}) is None
 
 
 def test_size_flags_parse(bench, monkeypatch):
