@@ -22,9 +22,10 @@
 //
 // GPU design, one stream per call: every miniblock is independent for
 // encoding (its deltas only need the input), so one warp packs one
-// miniblock, a block one group, and the group's place in the stream is the
-// prefix of the groups before it, found in the same pass by a decoupled
-// look-back (one launch).  Decoding needs each group's position, which the
+// miniblock; a first launch stores every miniblock's bit width and the word
+// count of each block's range of groups, a second one places each range
+// after the ranges before it and packs (two launches, no device waits).
+// Decoding needs each group's position, which the
 // stream only gives as a chain (each header says how long its group is): a
 // first pass follows the chain inside chunks of the stream from every
 // possible entry and carries the real entries across chunks by look-back;
@@ -205,21 +206,6 @@ __global__ void __launch_bounds__(kB) k_scan_down(const typename Op::T *in, type
 
 // ---- encoder ---------------------------------------------------------------------------
 
-// Lane j of a warp loads vector j of miniblock k and its predecessor vector.
-__device__ __forceinline__ void load_vectors(const uint32_t *in, uint64_t k, uint4 &cur, uint4 &prev)
-{
-    const int lane = g5_lane();
-    const uint4 *v = reinterpret_cast<const uint4 *>(in) + k * 32;
-    cur = v[lane];
-    uint4 p;
-    p.x = __shfl_up_sync(0xFFFFFFFFu, cur.x, 1);
-    p.y = __shfl_up_sync(0xFFFFFFFFu, cur.y, 1);
-    p.z = __shfl_up_sync(0xFFFFFFFFu, cur.z, 1);
-    p.w = __shfl_up_sync(0xFFFFFFFFu, cur.w, 1);
-    if (lane == 0) p = k ? v[-1] : make_uint4(0, 0, 0, 0);
-    prev = p;
-}
-
 __device__ __forceinline__ uint4 deltas(uint4 cur, uint4 prev, int mode)
 {
     if (mode == G5_CODEC_DM)
@@ -275,9 +261,9 @@ __device__ __forceinline__ void mb_locate(const uint32_t *in, const uint32_t *gp
 
 // ---- one-pass kernels: decoupled look-back -----------------------------------------------
 //
-// The single-stream encoder and decoder are one pass each over the stream's
-// tiles (a group of 16 miniblocks for packing and unpacking, a range of
-// stream vectors for locating groups).  Blocks claim tiles in launch order
+// The single-stream decoder's passes run over the stream's tiles (a group of
+// 16 miniblocks for unpacking, a range of stream vectors for locating
+// groups).  Blocks claim tiles in launch order
 // from a counter, so a tile only ever waits on tiles claimed before it, whose
 // blocks are already running.  Each tile publishes its own aggregate, then
 // its inclusive prefix once known; a tile combines the nearest inclusive
@@ -297,30 +283,17 @@ enum : uint32_t { ST_NONE = 0, ST_AGG = 1, ST_INC = 2 };
 
 // scalar slots of the one-pass kernels (the scalar block holds kScalars)
 enum {
-    CS_E_CTR = 16, CS_E_DONE = 17, CS_E_EPOCH = 18, CS_E_ERR = 19,
     CS_L_CTR = 20, CS_L_DONE = 21, CS_L_EPOCH = 22,
     CS_U_CTR = 25, CS_U_DONE = 26, CS_U_EPOCH = 27
 };
 
 __device__ __forceinline__ uint64_t vload64(const uint64_t *p) { return *reinterpret_cast<const volatile uint64_t *>(p); }
 __device__ __forceinline__ void vstore64(uint64_t *p, uint64_t v) { *reinterpret_cast<volatile uint64_t *>(p) = v; }
-__device__ __forceinline__ uint32_t vload32(const uint32_t *p) { return *reinterpret_cast<const volatile uint32_t *>(p); }
 
 __device__ __forceinline__ uint32_t status_flag(uint64_t s, uint64_t epoch)
 {
     return (s >> 2) == epoch ? (uint32_t)(s & 3u) : ST_NONE;
 }
-
-// Plain sums of 64-bit values (encoder: words per group).
-struct SumU64 {
-    typedef uint64_t T;
-    __device__ static T id() { return 0; }
-    __device__ static T op(T a, T b) { return a + b; }
-    __device__ static T shfl_down(T v, int o) { return __shfl_down_sync(0xFFFFFFFFu, v, o); }
-    __device__ static T bcast0(T v) { return __shfl_sync(0xFFFFFFFFu, v, 0); }
-    __device__ static T load(const T *p) { return vload64(p); }
-    __device__ static void store(T *p, T v) { vstore64(p, v); }
-};
 
 // Running lane sums with resets (decoder: a raw miniblock restarts the sums).
 struct ResetAddV {
@@ -451,9 +424,9 @@ __device__ __forceinline__ bool last_block(uint64_t *done)
 
 // Stream header words and the VariableByte tail of n - n1 (< 128) values,
 // written by one warp; blkend = word after the block part.  Total words ->
-// scal[CS_WORDS].  (compositecodec.h:31-51, variablebyte.h:100-161.)
+// scal[CS_WORDS] and, if given, *words_out.  (compositecodec.h:31-51, variablebyte.h:100-161.)
 __device__ void enc_tail_warp(const uint32_t *in, uint64_t n, uint64_t n1, uint64_t blkend, uint32_t *out,
-                              uint64_t *scal, uint32_t *s_val, uint32_t *s_bytes)
+                              uint64_t *scal, uint64_t *words_out, uint32_t *s_val, uint32_t *s_bytes)
 {
     const int lane = g5_lane();
     const uint32_t nt = (uint32_t)(n - n1);
@@ -479,6 +452,7 @@ __device__ void enc_tail_warp(const uint32_t *in, uint64_t n, uint64_t n1, uint6
         const uint32_t tw = (p + 3) / 4;
         s_val[0] = tw;
         scal[CS_WORDS] = blkend + tw;
+        if (words_out) *words_out = blkend + tw;
         scal[CS_BLKEND] = blkend;
     }
     __syncwarp();
@@ -486,20 +460,185 @@ __device__ void enc_tail_warp(const uint32_t *in, uint64_t n, uint64_t n1, uint6
     for (uint32_t i = lane; i < tw; i += 32) out[blkend + i] = s_bytes[i];
 }
 
-// ---- encoder: one pass ----------------------------------------------------------------
+// ---- encoder: two passes ----------------------------------------------------------------
 //
-// One tile per kTG groups of 16 miniblocks (64 miniblocks), warp w handling
-// miniblocks w, w + 16, w + 32 and w + 48 of the tile: first every warp
-// computes its miniblocks' bit widths (their loads issued together), the
-// block adds up the tile's words (4 header words per group + 4 b per
-// miniblock), the tile's position in the stream is the exclusive prefix of
-// the tiles before it (look-back), then the warps pack their miniblocks there
-// from a second read of the input (the tile's 32 KB are still in L1 / L2).
-// The block with the last group writes the stream header and the
-// VariableByte tail.  n comes from device memory, so the launch can sit in a
-// CUDA graph with a fixed grid.
-constexpr int kTG = 4;               // groups per encoder / unpacker tile
-constexpr int kTM = 16 * kTG;        // miniblocks per tile
+// A miniblock's bit width depends only on its own 128 values and the vector
+// before them, so the stream's layout is fixed once every width is known.
+// Block b of the B launched blocks takes the groups [b NG / B, (b + 1) NG / B)
+// in both passes (NG groups of 16 miniblocks):
+//   k_enc_widths  a warp per miniblock ORs the deltas and stores the width
+//                 (one byte per miniblock); the block stores its range's
+//                 word count (4 header words per group + 4 b per miniblock)
+//   k_enc_pack    the block adds up the counts of the blocks before it (its
+//                 range's place in the stream), scans its groups' sizes, and
+//                 a warp per miniblock packs the deltas at their place from a
+//                 second read of the input (mostly still in L2); the block
+//                 with the last group writes the stream header and the
+//                 VariableByte tail
+// No block waits on another: the launch boundary orders the passes.  n comes
+// from device memory, so both launches can sit in a CUDA graph with a fixed
+// grid.
+constexpr int kEB = 512;  // encoder threads per block: 16 warps
+constexpr int kEU = 4;    // miniblocks whose loads a warp has in flight together (widths)
+constexpr int kPU = 2;    // the same when packing (two blocks of 512 fit an SM at 64 registers)
+
+struct EncLen {
+    uint64_t n, n1, nmb, ng;
+    bool raw, too_long;
+};
+
+__device__ __forceinline__ EncLen enc_len(const uint64_t *n_dev, uint64_t max_n, uint64_t raw_thr)
+{
+    EncLen e;
+    const uint64_t n_in = *n_dev;
+    e.too_long = n_in > max_n;  // a device-side length past the workspace: nothing is written
+    e.n = e.too_long ? 0 : n_in;
+    e.n1 = e.n / 128 * 128;
+    e.nmb = e.n / 128;
+    e.ng = (e.nmb + 15) / 16;
+    e.raw = raw_thr && e.n <= raw_thr;
+    return e;
+}
+
+__device__ __forceinline__ void enc_range(uint64_t ng, uint32_t nb, uint64_t &g0, uint64_t &g1)
+{
+    g0 = ng * blockIdx.x / nb;
+    g1 = ng * (blockIdx.x + 1) / nb;
+}
+
+// Lane j's vector j of miniblock k; lane 0 also the vector before the
+// miniblock (zero before the first).  Loads only: prev_of() shuffles later.
+__device__ __forceinline__ void load_cur(const uint32_t *in, uint64_t k, uint4 &cur, uint4 &pl)
+{
+    const uint4 *v = reinterpret_cast<const uint4 *>(in) + k * 32;
+    cur = v[g5_lane()];
+    pl = (g5_lane() == 0 && k) ? v[-1] : make_uint4(0, 0, 0, 0);
+}
+
+__device__ __forceinline__ uint4 prev_of(const uint4 &cur, const uint4 &pl)
+{
+    uint4 p;
+    p.x = __shfl_up_sync(0xFFFFFFFFu, cur.x, 1);
+    p.y = __shfl_up_sync(0xFFFFFFFFu, cur.y, 1);
+    p.z = __shfl_up_sync(0xFFFFFFFFu, cur.z, 1);
+    p.w = __shfl_up_sync(0xFFFFFFFFu, cur.w, 1);
+    return g5_lane() == 0 ? pl : p;
+}
+
+// The widths of group g (16 bytes, byte q = miniblock 16 g + q) with the
+// bytes of miniblocks past nmb cleared (a partial last group's header
+// carries width 0 there, simdbinarypacking.h:200-214).
+__device__ __forceinline__ uint4 group_widths(const uint8_t *wb, uint64_t g, uint64_t nmb)
+{
+    uint4 w = *reinterpret_cast<const uint4 *>(wb + 16 * g);
+    const uint64_t c = nmb - 16 * g;  // miniblocks in the group
+    if (c < 16) {
+        uint32_t x[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int keep = (int)c - 4 * j;  // bytes of word j that stay
+            x[j] = keep >= 4 ? x[j] : keep <= 0 ? 0u : x[j] & ((1u << (8 * keep)) - 1u);
+        }
+        w = make_uint4(x[0], x[1], x[2], x[3]);
+    }
+    return w;
+}
+
+// Sum of the first i widths of a group (bytes 0 .. i-1 of w).
+__device__ __forceinline__ uint32_t widths_before(const uint4 &w, uint32_t i)
+{
+    const uint32_t x[4] = {w.x, w.y, w.z, w.w};
+    uint32_t s = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int keep = (int)i - 4 * j;
+        const uint32_t m = keep >= 4 ? 0xFFFFFFFFu : keep <= 0 ? 0u : (1u << (8 * keep)) - 1u;
+        s = __dp4a(x[j] & m, 0x01010101u, s);
+    }
+    return s;
+}
+
+__global__ void __launch_bounds__(kEB, 2) k_enc_widths(const uint32_t *__restrict__ in, const uint64_t *n_dev,
+                                                    uint64_t max_n, uint64_t raw_thr, uint8_t *__restrict__ wb,
+                                                    uint64_t *__restrict__ btot, uint32_t nb, int mode)
+{
+    __shared__ uint32_t s_sum;
+    g5_pdl_sync();
+    const EncLen e = enc_len(n_dev, max_n, raw_thr);
+    if (e.raw || e.too_long) return;
+    const int lane = g5_lane(), wid = threadIdx.x >> 5;
+    uint64_t g0, g1;
+    enc_range(e.ng, nb, g0, g1);
+    const uint64_t k1 = min(16 * g1, e.nmb);
+    if (threadIdx.x == 0) s_sum = 0;
+    __syncthreads();
+    uint32_t sum = 0;  // warp-uniform
+    for (uint64_t kb = 16 * g0 + wid; kb < k1; kb += 16 * kEU) {
+        uint4 cur[kEU], pl[kEU];
+#pragma unroll
+        for (int i = 0; i < kEU; ++i) {
+            cur[i] = pl[i] = make_uint4(0, 0, 0, 0);
+            if (kb + 16 * i < k1) load_cur(in, kb + 16 * i, cur[i], pl[i]);
+        }
+#pragma unroll
+        for (int i = 0; i < kEU; ++i) {
+            const uint64_t k = kb + 16 * i;
+            if (k >= k1) break;
+            const uint4 d = deltas(cur[i], prev_of(cur[i], pl[i]), mode);
+            const uint32_t b = bits_of(__reduce_or_sync(0xFFFFFFFFu, d.x | d.y | d.z | d.w));
+            if (lane == 0) wb[k] = (uint8_t)b;
+            sum += b;
+        }
+    }
+    if (lane == 0 && sum) atomicAdd(&s_sum, sum);
+    __syncthreads();
+    if (threadIdx.x == 0) btot[blockIdx.x] = 4 * (g1 - g0) + 4 * (uint64_t)s_sum;
+}
+
+// Sum over the block (kEB threads) of a 64-bit value, returned to all.
+__device__ __forceinline__ uint64_t block_sum_u64(uint64_t x, uint64_t *s_red)
+{
+    const int lane = g5_lane(), wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
+    if (lane == 0) s_red[wid] = x;
+    __syncthreads();
+    uint64_t t = 0;
+#pragma unroll
+    for (int i = 0; i < kEB / 32; ++i) t += s_red[i];
+    __syncthreads();
+    return t;
+}
+
+// Exclusive scan over the block (kEB threads) of a 32-bit value; total -> tot.
+__device__ __forceinline__ uint32_t block_excl_u32(uint32_t x, uint32_t *s_w, uint32_t &tot)
+{
+    const int lane = g5_lane(), wid = threadIdx.x >> 5;
+    uint32_t inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) s_w[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        const uint32_t v = lane < kEB / 32 ? s_w[lane] : 0u;
+        uint32_t vi = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, vi, o);
+            if (lane >= o) vi += y;
+        }
+        if (lane < kEB / 32) s_w[lane] = vi - v;
+        if (lane == kEB / 32 - 1) s_w[kEB / 32] = vi;
+    }
+    __syncthreads();
+    const uint32_t r = s_w[wid] + inc - x;
+    tot = s_w[kEB / 32];
+    __syncthreads();
+    return r;
+}
 
 // Packs a miniblock's deltas (lane j holds vector j) with width b (1..31)
 // into shared memory at s + po: value j of lane l occupies bits j b .. of
@@ -523,140 +662,92 @@ __device__ __forceinline__ void pack_mb_smem(const uint4 &d, uint32_t b, uint32_
     }
 }
 
-__global__ void __launch_bounds__(kOB) k_enc1(const uint32_t *__restrict__ in, const uint64_t *n_dev,
-                                              uint64_t max_n, uint64_t raw_thr, uint32_t *__restrict__ out,
-                                              uint64_t *scal, uint64_t *tst, uint64_t *tagg, uint64_t *tinc, int mode)
+__global__ void __launch_bounds__(kEB, 2) k_enc_pack(const uint32_t *__restrict__ in, const uint64_t *n_dev,
+                                                  uint64_t max_n, uint64_t raw_thr, uint32_t *__restrict__ out,
+                                                  uint64_t *scal, const uint8_t *__restrict__ wb,
+                                                  const uint64_t *__restrict__ btot, uint32_t nb,
+                                                  uint64_t *words_out, int mode)
 {
-    __shared__ __align__(16) uint32_t s_out[kTG * (4 + 16 * 128)];  // the tile's words, packed before its place is known
-    __shared__ uint32_t s_b[kTM];
-    __shared__ uint32_t s_off[kTM];  // payload word offset of each miniblock in the tile
-    __shared__ uint32_t s_goff[kTG]; // header word offset of each group in the tile
-    __shared__ uint32_t s_tw;        // words of the tile
-    __shared__ uint64_t s_t, s_excl;
+    __shared__ __align__(16) uint32_t s_stage[kEB / 32][128];  // one miniblock's payload per warp
+    __shared__ uint32_t s_goff[kEB];  // words from the chunk's first header to each group's header
+    __shared__ uint64_t s_red[kEB / 32];
+    __shared__ uint32_t s_w[kEB / 32 + 1];
     __shared__ uint32_t s_val[128];
     __shared__ uint32_t s_bytes[(128 * 5 + 3) / 4 + 1];
+    g5_pdl_sync();
+    const EncLen e = enc_len(n_dev, max_n, raw_thr);
     const int lane = g5_lane(), wid = threadIdx.x >> 5;
-    const uint64_t n_in = *n_dev;
-    const bool too_long = n_in > max_n;  // a device-side length past the workspace: nothing is written
-    const uint64_t n = too_long ? 0 : n_in;
-    const uint64_t epoch = scal[CS_E_EPOCH];
-    const uint64_t n1 = n / 128 * 128, nmb = n / 128, ngroups = (nmb + 15) / 16;
-    const uint64_t ntiles = too_long ? 0 : (ngroups + kTG - 1) / kTG;
-    const bool raw = raw_thr && n <= raw_thr;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        scal[CS_N] = n;
-        scal[CS_N1] = n1;
-        scal[CS_NMB] = nmb;
-        scal[CS_RAW] = raw ? 1 : 0;
+        scal[CS_N] = e.n;
+        scal[CS_N1] = e.n1;
+        scal[CS_NMB] = e.nmb;
+        scal[CS_RAW] = e.raw ? 1 : 0;
+        scal[CS_ERR] = e.too_long ? G5_DEVERR_CAPACITY : 0;
     }
-    if (raw) {
-        for (uint64_t i = (uint64_t)blockIdx.x * kOB + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kOB)
+    if (e.too_long) return;
+    if (e.raw) {
+        for (uint64_t i = (uint64_t)blockIdx.x * kEB + threadIdx.x; i < e.n; i += (uint64_t)gridDim.x * kEB)
             out[i] = in[i];
-        if (blockIdx.x == 0 && threadIdx.x == 0) scal[CS_WORDS] = n;
-    } else {
-        for (;;) {
-            const uint64_t t = claim_tile(&scal[CS_E_CTR], &s_t);
-            if (t >= ntiles) break;
-            const uint64_t k0 = (uint64_t)kTM * t;
-            // widths: all of the warp's loads first
-            uint4 cur[kTG], prev[kTG];
-#pragma unroll
-            for (int i = 0; i < kTG; ++i) {
-                const uint64_t k = k0 + 16 * i + wid;
-                if (k < nmb) load_vectors(in, k, cur[i], prev[i]);
-            }
-#pragma unroll
-            for (int i = 0; i < kTG; ++i) {
-                const uint64_t k = k0 + 16 * i + wid;
-                uint32_t b = 0;
-                if (k < nmb) {
-                    const uint4 d = deltas(cur[i], prev[i], mode);
-                    uint32_t acc = d.x | d.y | d.z | d.w;
-#pragma unroll
-                    for (int o = 16; o; o >>= 1) acc |= __shfl_xor_sync(0xFFFFFFFFu, acc, o);
-                    b = bits_of(acc);
-                }
-                if (lane == 0) s_b[16 * i + wid] = b;
-            }
-            __syncthreads();
-            if (wid == 0) {
-                // words of miniblock i, plus its group's 4 header words at the
-                // group's first miniblock (no header past the last group);
-                // exclusive scan over the 64, two per lane
-                uint32_t e[2], x = 0;
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int i = 2 * lane + h;
-                    const bool head = (i & 15) == 0 && (uint64_t)kTG * t + i / 16 < ngroups;
-                    e[h] = 4 * s_b[i] + (head ? 4u : 0u);
-                    x += e[h];
-                }
-                uint32_t inc = x;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-                    if (lane >= o) inc += y;
-                }
-                uint32_t pos = inc - x;
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int i = 2 * lane + h;
-                    if ((i & 15) == 0) {
-                        s_goff[i / 16] = pos;
-                        s_off[i] = pos + 4;
-                    } else {
-                        s_off[i] = pos;
-                    }
-                    pos += e[h];
-                }
-                if (lane == 31) s_tw = inc;
-            }
-            __syncthreads();
-            // warp 0 finds the tile's place (look-back) first, so that later
-            // tiles see its aggregate early; the other warps pack meanwhile
-            // into shared memory, the tile's words relative to its start
-            if (wid == 0) {
-                const uint64_t ex = lookback<SumU64>(tst, tagg, tinc, t, epoch, (uint64_t)s_tw, &scal[CS_E_ERR]);
-                if (lane == 0) s_excl = ex;
-                if (lane < 4 * kTG && (uint64_t)kTG * t + lane / 4 < ngroups) {
-                    const int g = lane / 4, q = lane & 3;
-                    const uint32_t *bw = s_b + 16 * g + 4 * q;
-                    s_out[s_goff[g] + q] = (bw[0] << 24) | (bw[1] << 16) | (bw[2] << 8) | bw[3];
-                }
-            }
-#pragma unroll 1
-            for (int i = 0; i < kTG; ++i) {
-                const uint64_t k = k0 + 16 * i + wid;
-                if (k >= nmb) break;
-                const uint32_t b = s_b[16 * i + wid];
-                const uint32_t po = s_off[16 * i + wid];
-                uint4 c, pv;
-                load_vectors(in, k, c, pv);
-                if (b == 32) reinterpret_cast<uint4 *>(s_out + po)[lane] = c;
-                else if (b) pack_mb_smem(deltas(c, pv, mode), b, s_out, po);
-            }
-            __syncthreads();
-            const uint64_t base = 4 + s_excl;  // word of the tile's first header (a multiple of 4)
-            {
-                uint4 *dst = reinterpret_cast<uint4 *>(out + base);
-                const uint4 *src = reinterpret_cast<const uint4 *>(s_out);
-                for (uint32_t i = threadIdx.x; i < s_tw / 4; i += kOB) dst[i] = src[i];
-            }
-            if (t == ntiles - 1 && wid == 1) enc_tail_warp(in, n, n1, base + s_tw, out, scal, s_val, s_bytes);
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            scal[CS_WORDS] = e.n;
+            if (words_out) *words_out = e.n;
         }
-        if (too_long && blockIdx.x == 0 && threadIdx.x == 0)
-            atomicOr((unsigned long long *)&scal[CS_E_ERR], (unsigned long long)G5_DEVERR_CAPACITY);
-        else if (ntiles == 0 && blockIdx.x == 0 && wid == 0)
-            enc_tail_warp(in, n, n1, 4, out, scal, s_val, s_bytes);
+        return;
     }
-    if (last_block(&scal[CS_E_DONE])) {
-        scal[CS_ERR] = scal[CS_E_ERR];
-        scal[CS_E_ERR] = 0;
-        scal[CS_E_CTR] = 0;
-        scal[CS_E_DONE] = 0;
-        scal[CS_E_EPOCH] = epoch + 1;
-        __threadfence();
+    if (e.ng == 0) {
+        if (blockIdx.x == 0 && wid == 0) enc_tail_warp(in, e.n, e.n1, 4, out, scal, words_out, s_val, s_bytes);
+        return;
     }
+    uint64_t g0, g1;
+    enc_range(e.ng, nb, g0, g1);
+    if (g0 == g1) return;
+    uint64_t x = 0;
+    for (uint32_t i = threadIdx.x; i < blockIdx.x; i += kEB) x += btot[i];
+    uint64_t cbase = 4 + block_sum_u64(x, s_red);  // word of the chunk's first group header
+    uint32_t *stage = s_stage[wid];
+    for (uint64_t c0 = g0; c0 < g1; c0 += kEB) {
+        const uint64_t g = c0 + threadIdx.x;
+        const uint32_t gw = g < g1 ? 4 + 4 * widths_before(group_widths(wb, g, e.nmb), 16) : 0u;
+        uint32_t ctot;
+        s_goff[threadIdx.x] = block_excl_u32(gw, s_w, ctot);
+        __syncthreads();
+        const uint64_t k1 = min(16 * min(c0 + kEB, g1), e.nmb);
+        for (uint64_t kb = 16 * c0 + wid; kb < k1; kb += 16 * kPU) {
+            uint4 cur[kPU], pl[kPU], gwd[kPU];
+#pragma unroll
+            for (int i = 0; i < kPU; ++i) {
+                cur[i] = pl[i] = gwd[i] = make_uint4(0, 0, 0, 0);
+                const uint64_t k = kb + 16 * i;
+                if (k < k1) {
+                    load_cur(in, k, cur[i], pl[i]);
+                    gwd[i] = group_widths(wb, k / 16, e.nmb);
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < kPU; ++i) {
+                const uint64_t k = kb + 16 * i;
+                if (k >= k1) break;
+                const uint32_t q = (uint32_t)(k % 16);
+                const uint64_t gpos = cbase + s_goff[k / 16 - c0];
+                if (q == 0 && lane < 4)  // the group's header: its 16 widths, big-endian bytes
+                    out[gpos + lane] = __byte_perm(comp(gwd[i], lane), 0, 0x0123);
+                const uint32_t b = (comp(gwd[i], q / 4) >> (8 * (q % 4))) & 0xFFu;
+                const uint64_t pos = gpos + 4 + 4 * (uint64_t)widths_before(gwd[i], q);
+                uint4 *dst = reinterpret_cast<uint4 *>(out + pos);
+                if (b == 32) {
+                    dst[lane] = cur[i];
+                } else if (b) {
+                    pack_mb_smem(deltas(cur[i], prev_of(cur[i], pl[i]), mode), b, stage, 0);
+                    __syncwarp();
+                    if (lane < (int)b) dst[lane] = reinterpret_cast<const uint4 *>(stage)[lane];
+                    __syncwarp();
+                }
+            }
+        }
+        cbase += ctot;
+        __syncthreads();
+    }
+    if (g1 == e.ng && wid == 0) enc_tail_warp(in, e.n, e.n1, cbase, out, scal, words_out, s_val, s_bytes);
 }
 
 // ---- decoder: locate groups ----------------------------------------------------------
@@ -739,6 +830,7 @@ __global__ void __launch_bounds__(kOB) k_loc_tables(const uint32_t *__restrict__
 {
     __shared__ uint16_t s_j[kLocMax];
     __shared__ uint64_t s_t;
+    g5_pdl_sync();
     const DecHead h = dec_head(in, words_dev, cap, raw_thr, n_expect, max_vec, max_mb);
     const uint32_t S = loc_chunk(h.nv);
     const uint64_t nchunks = (h.raw || h.bad || h.ng == 0) ? 0 : (h.nv - 1 + S - 1) / S;
@@ -799,6 +891,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_loc_walk(const uint32_t *__res
                                                            const uint32_t *ltab, uint64_t *lent)
 {
     extern __shared__ uint32_t s_tab[];
+    g5_pdl_sync();
     const DecHead h = dec_head(in, words_dev, cap, raw_thr, n_expect, max_vec, max_mb);
     const uint32_t S = loc_chunk(h.nv);
     const uint64_t nchunks = (h.raw || h.bad || h.ng == 0) ? 0 : (h.nv - 1 + S - 1) / S;
@@ -864,6 +957,7 @@ __global__ void __launch_bounds__(kOB) k_loc_pos(const uint32_t *__restrict__ in
                                                  const uint16_t *ljump, const uint64_t *lent, uint32_t *gpos)
 {
     __shared__ uint16_t s_j[kLocMax];
+    g5_pdl_sync();
     if (scal[CS_RAW] || scal[CS_ERR]) return;
     const uint64_t ng = scal[CS_NG], nmb = scal[CS_NMB];
     const uint64_t nv = scal[CS_WORDS] / 4;
@@ -922,6 +1016,8 @@ __global__ void __launch_bounds__(kOB) k_loc_pos(const uint32_t *__restrict__ in
 // whatever the block part holds.  With `expect` every value is compared with
 // the expected one (the level loop's round-trip check); `acc` accumulates
 // words and values.
+constexpr int kTG = 4;          // groups per unpacker tile
+constexpr int kTM = 16 * kTG;   // miniblocks per tile
 
 // Stream position (16-byte vectors) and width of miniblock i of the group
 // whose header is at vector p.
@@ -996,7 +1092,8 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
                                                     const uint32_t *__restrict__ gpos, uint32_t *__restrict__ out,
                                                     uint64_t cap, const uint64_t *n_expect,
                                                     const uint32_t *__restrict__ expect, uint64_t *acc,
-                                                    uint64_t *ust, VecFlag *uagg, VecFlag *uinc, int mode)
+                                                    uint64_t *ust, VecFlag *uagg, VecFlag *uinc, uint64_t *n_out,
+                                                    int mode)
 {
     __shared__ VecFlag s_vf[kTM];
     __shared__ VecFlag s_base[kTM];     // each miniblock's prefix from the tile's start
@@ -1006,10 +1103,14 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
     __shared__ uint64_t s_t;
     __shared__ uint32_t s_b[kTailMaxBytes / 4];
     const int lane = g5_lane(), wid = threadIdx.x >> 5;
+    g5_pdl_sync();
     const uint64_t epoch = scal[CS_U_EPOCH];
     const uint64_t err0 = scal[CS_ERR];
     const uint64_t words = scal[CS_WORDS];
     bool bad = false;
+    // the value count: final here for a raw stream or one the locator
+    // rejected, else the tail's writer below sets it
+    if (n_out && blockIdx.x == 0 && threadIdx.x == 0 && (scal[CS_RAW] || err0)) *n_out = scal[CS_N];
     if (scal[CS_RAW]) {
         const uint64_t n = scal[CS_N];
         if (!err0)
@@ -1033,7 +1134,10 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
             const uint64_t blkend = scal[CS_BLKEND];
             const uint64_t tw = words > blkend ? words - blkend : 0;
             if (tw * 4 > kTailMaxBytes) {
-                if (lane == 0) atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_CORRUPT);
+                if (lane == 0) {
+                    atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)G5_DEVERR_CORRUPT);
+                    if (n_out) *n_out = 0;
+                }
             } else {
                 for (uint64_t i = lane; i < tw; i += 32) s_b[i] = in[blkend + i];
                 __syncwarp();
@@ -1065,6 +1169,7 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
                         }
                     }
                     scal[CS_N] = o;
+                    if (n_out) *n_out = o;
                     if (n_expect && o != *n_expect) e |= G5_DEVERR_MISMATCH;
                     if (e) atomicOr((unsigned long long *)&scal[CS_ERR], (unsigned long long)e);
                     if (acc) {
@@ -1622,9 +1727,9 @@ g5_status codec_work_alloc(CodecWork &w, size_t max_n)
     const size_t T = codec_tiles(max_n), C = codec_chunks(max_n);
     G5_CUDA(cudaMalloc(&w.scal, sizeof(uint64_t) * kScalars));
     G5_CUDA(cudaMalloc(&w.gpos, sizeof(uint32_t) * T));
-    G5_CUDA(cudaMalloc(&w.est, sizeof(uint64_t) * 3 * T));
-    w.eagg = w.est + T;
-    w.einc = w.est + 2 * T;
+    w.enc_blocks = w.grid;
+    G5_CUDA(cudaMalloc(&w.ewb, 16 * T));
+    G5_CUDA(cudaMalloc(&w.etot, sizeof(uint64_t) * w.enc_blocks));
     G5_CUDA(cudaMalloc(&w.ltab, sizeof(uint32_t) * kEntries * C));
     G5_CUDA(cudaMalloc(&w.lent, sizeof(uint64_t) * C));
     G5_CUDA(cudaMalloc(&w.ljump, sizeof(uint16_t) * (w.max_vec + 2)));
@@ -1636,10 +1741,9 @@ g5_status codec_work_alloc(CodecWork &w, size_t max_n)
     w.uinc = w.uagg + T;
     // epochs start at 1, so zeroed status words read as "not published"
     G5_CUDA(cudaMemset(w.scal, 0, sizeof(uint64_t) * kScalars));
-    G5_CUDA(cudaMemset(w.est, 0, sizeof(uint64_t) * 3 * T));
     G5_CUDA(cudaMemset(w.ust, 0, sizeof(uint64_t) * T));
     const uint64_t one = 1;
-    for (int e : {CS_E_EPOCH, CS_L_EPOCH, CS_U_EPOCH})
+    for (int e : {CS_L_EPOCH, CS_U_EPOCH})
         G5_CUDA(cudaMemcpy(w.scal + e, &one, sizeof one, cudaMemcpyHostToDevice));
     return G5_OK;
 }
@@ -1648,7 +1752,8 @@ void codec_work_free(CodecWork &w)
 {
     cudaFree(w.scal);
     cudaFree(w.gpos);
-    cudaFree(w.est);
+    cudaFree(w.ewb);
+    cudaFree(w.etot);
     cudaFree(w.ltab);
     cudaFree(w.lent);
     cudaFree(w.ljump);
@@ -1658,29 +1763,36 @@ void codec_work_free(CodecWork &w)
 }
 
 void codec_encode_launch(CodecWork &w, const uint32_t *in, const uint64_t *n_dev, uint32_t *out, int mode,
-                         uint64_t raw_threshold, cudaStream_t s)
+                         uint64_t raw_threshold, cudaStream_t s, uint64_t *words_out)
 {
-    k_enc1<<<w.grid, kOB, 0, s>>>(in, n_dev, w.max_n, raw_threshold, out, w.scal, w.est, w.eagg, w.einc, mode);
+    // programmatic dependent launches: each kernel's first instruction waits
+    // for the kernel before it, so only the launch latency is overlapped
+    const uint32_t nb = (uint32_t)std::min(w.grid, w.enc_blocks);
+    launch(true, k_enc_widths, nb, kEB, s, in, n_dev, (uint64_t)w.max_n, raw_threshold, w.ewb, w.etot, nb, mode);
+    launch(true, k_enc_pack, nb, kEB, s, in, n_dev, (uint64_t)w.max_n, raw_threshold, out, w.scal,
+           (const uint8_t *)w.ewb, (const uint64_t *)w.etot, nb, words_out, mode);
 }
 
 void codec_decode_launch(CodecWork &w, const uint32_t *in, const uint64_t *words_dev, uint32_t *out, size_t cap,
                          int mode, uint64_t raw_threshold, const uint64_t *n_expect_dev, const uint32_t *expect,
-                         cudaStream_t s)
+                         cudaStream_t s, uint64_t *n_out)
 {
-    decode_launch_acc(w, in, words_dev, out, cap, mode, raw_threshold, n_expect_dev, expect, nullptr, s);
+    decode_launch_acc(w, in, words_dev, out, cap, mode, raw_threshold, n_expect_dev, expect, nullptr, s, n_out);
 }
 
 void decode_launch_acc(CodecWork &w, const uint32_t *in, const uint64_t *words_dev, uint32_t *out, size_t cap,
                        int mode, uint64_t raw_threshold, const uint64_t *n_expect_dev, const uint32_t *expect,
-                       uint64_t *acc, cudaStream_t s)
+                       uint64_t *acc, cudaStream_t s, uint64_t *n_out)
 {
-    k_loc_tables<<<w.grid, kOB, 0, s>>>(in, words_dev, cap, raw_threshold, n_expect_dev, w.scal, w.max_vec,
-                                        w.max_mb, w.ltab, w.ljump);
-    k_loc_walk<<<1, kWalkThreads, sizeof(uint32_t) * kEntries * kLocFit, s>>>(
-        in, words_dev, cap, raw_threshold, n_expect_dev, w.scal, w.max_vec, w.max_mb, w.ltab, w.lent);
-    k_loc_pos<<<w.grid, kOB, 0, s>>>(in, w.scal, w.ljump, w.lent, w.gpos);
-    k_dec_unpack<<<w.grid, kOB, 0, s>>>(in, w.scal, w.gpos, out, cap, n_expect_dev, expect, acc, w.ust, w.uagg,
-                                        w.uinc, mode);
+    // programmatic dependent launches: each kernel's first instruction waits
+    // for the kernel before it, so only the launch latency is overlapped
+    const uint64_t mv = w.max_vec, mm = w.max_mb, c = cap, rt = raw_threshold;
+    launch(true, k_loc_tables, w.grid, kOB, s, in, words_dev, c, rt, n_expect_dev, w.scal, mv, mm, w.ltab, w.ljump);
+    launch_dyn(true, k_loc_walk, 1, kWalkThreads, sizeof(uint32_t) * kEntries * kLocFit, s, in, words_dev, c, rt,
+               n_expect_dev, w.scal, mv, mm, (const uint32_t *)w.ltab, w.lent);
+    launch(true, k_loc_pos, w.grid, kOB, s, in, w.scal, (const uint16_t *)w.ljump, (const uint64_t *)w.lent, w.gpos);
+    launch(true, k_dec_unpack, w.grid, kOB, s, in, w.scal, (const uint32_t *)w.gpos, out, c, n_expect_dev, expect,
+           acc, w.ust, w.uagg, w.uinc, n_out, mode);
 }
 
 }  // namespace g5
@@ -1807,9 +1919,8 @@ g5_status g5_codec_encode_async(g5_codec *c, const uint32_t *in_dev, const uint6
     if (mode != G5_CODEC_D4 && mode != G5_CODEC_DM) return G5_ERR_INVALID_ARG;
     if (((uintptr_t)in_dev | (uintptr_t)out_dev) & 15) return G5_ERR_INVALID_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    g5::codec_encode_launch(c->w, in_dev, n_dev, out_dev, mode, 0, s);
+    g5::codec_encode_launch(c->w, in_dev, n_dev, out_dev, mode, 0, s, out_words_dev);
     G5_CUDA(cudaGetLastError());
-    G5_CUDA(cudaMemcpyAsync(out_words_dev, c->w.scal + g5::CS_WORDS, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
     return G5_OK;
 }
 
@@ -1820,9 +1931,8 @@ g5_status g5_codec_decode_async(g5_codec *c, const uint32_t *in_dev, const uint6
     if (mode != G5_CODEC_D4 && mode != G5_CODEC_DM) return G5_ERR_INVALID_ARG;
     if (((uintptr_t)in_dev | (uintptr_t)out_dev) & 15) return G5_ERR_INVALID_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    g5::codec_decode_launch(c->w, in_dev, words_dev, out_dev, out_cap, mode, 0, nullptr, nullptr, s);
+    g5::codec_decode_launch(c->w, in_dev, words_dev, out_dev, out_cap, mode, 0, nullptr, nullptr, s, out_n_dev);
     G5_CUDA(cudaGetLastError());
-    G5_CUDA(cudaMemcpyAsync(out_n_dev, c->w.scal + g5::CS_N, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
     return G5_OK;
 }
 
@@ -2009,13 +2119,12 @@ g5_status g5_codec_decode_batch(g5_codec *c, const uint32_t *in_dev, const uint6
 // that may not block on (or fragment) device memory between requests, or a
 // host process whose device memory is owned by another allocator (a
 // framework's caching pool) with no headroom for cudaMalloc.  The encoder's
-// scratch (its scalars and tile counter, the length, and the look-back words
-// of every group) lives in the file-scope array below instead of a g5_codec
-// workspace: 12,608 bytes (about 12 KiB, kNoAllocBytes) that every GPU which
-// loads the library holds until the process exits.  Nothing in it needs
-// clearing between calls: the look-back words carry the call's epoch, and
-// the last block of each call resets the tile counter and advances the
-// epoch (the array starts zeroed).  The array's device address is looked up
+// scratch (its scalars, the length, the bit width of every miniblock and the
+// word count of every encoder block) lives in the file-scope array below
+// instead of a g5_codec workspace: 12,608 bytes (about 12 KiB,
+// kNoAllocBytes) that every GPU which loads the library holds until the
+// process exits.  Nothing in it needs clearing between calls: each call
+// writes every width and count it reads.  The array's device address is looked up
 // once per device and cached for the life of the process, so the entry point
 // must not be used again on a device after cudaDeviceReset in the same
 // process (the reset frees the module that holds the array).
@@ -2024,9 +2133,10 @@ namespace {
 
 constexpr size_t kNoAllocMaxValues = (size_t)1 << 20;             // values per call
 constexpr size_t kNoAllocMb = kNoAllocMaxValues / 128 + 1;          // miniblocks
-constexpr size_t kNoAllocTiles = kNoAllocMb / 16 + 2;               // look-back groups
+constexpr size_t kNoAllocWb = (kNoAllocMb / 16 + 1) * 16;          // miniblock widths, whole groups
+constexpr size_t kNoAllocBlocks = 516;                              // encoder blocks at most
 constexpr size_t kNoAllocScal = sizeof(uint64_t) * g5::kScalars;    // scalars
-constexpr size_t kNoAllocBytes = kNoAllocScal + 16 + 3 * sizeof(uint64_t) * kNoAllocTiles;
+constexpr size_t kNoAllocBytes = kNoAllocScal + 16 + kNoAllocWb + sizeof(uint64_t) * kNoAllocBlocks;
 static_assert(kNoAllocBytes == 12608, "the documented size of the scratch array");
 
 // In host code this name is only a host-side stand-in for the device array;
@@ -2070,11 +2180,10 @@ extern "C" g5_status g5_codec_encode_noalloc(const uint32_t *in_dev, size_t n, u
     w.grid = g5::codec_grid();
     w.scal = reinterpret_cast<uint64_t *>(b);
     uint64_t *n_dev = reinterpret_cast<uint64_t *>(b + kNoAllocScal);
-    w.est = reinterpret_cast<uint64_t *>(b + kNoAllocScal + 16);
-    w.eagg = w.est + kNoAllocTiles;
-    w.einc = w.est + 2 * kNoAllocTiles;
-    static_assert(kNoAllocScal + 16 + 3 * sizeof(uint64_t) * kNoAllocTiles <= kNoAllocBytes,
-                  "scratch layout exceeds the static array");
+    w.ewb = b + kNoAllocScal + 16;
+    w.etot = reinterpret_cast<uint64_t *>(b + kNoAllocScal + 16 + kNoAllocWb);
+    w.enc_blocks = (int)kNoAllocBlocks;
+    static_assert((kNoAllocScal + 16 + kNoAllocWb) % 16 == 0, "the widths are read as 16-byte vectors");
     cudaStream_t s = (cudaStream_t)stream;
     uint64_t hn = n;
     G5_CUDA(cudaMemcpyAsync(n_dev, &hn, sizeof hn, cudaMemcpyHostToDevice, s));
@@ -2083,7 +2192,7 @@ extern "C" g5_status g5_codec_encode_noalloc(const uint32_t *in_dev, size_t n, u
     uint64_t sc[3] = {0, 0, 0};  // CS_N, CS_WORDS, CS_ERR
     G5_CUDA(cudaMemcpyAsync(sc, w.scal, sizeof sc, cudaMemcpyDeviceToHost, s));
     G5_CUDA(cudaStreamSynchronize(s));
-    if (sc[g5::CS_ERR]) return G5_ERR_TIMEOUT;
+    if (sc[g5::CS_ERR]) return G5_ERR_CAPACITY;
     *out_words = (size_t)sc[g5::CS_WORDS];
     return G5_OK;
 }

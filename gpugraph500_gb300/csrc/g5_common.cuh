@@ -85,6 +85,24 @@ cudaError_t launch(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, cuda
     return cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
+// As launch(), with smem bytes of dynamic shared memory.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_dyn(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 }  // namespace g5
 
 // Device-side error flags (bit set in a status word).

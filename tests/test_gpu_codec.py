@@ -63,6 +63,26 @@ def test_large_queues_match_oracle(codec, mode, omode):
         assert np.array_equal(back, x)
 
 
+def test_encoder_ranges_longer_than_one_chunk():
+    """Over 318 M values every encoder block's range holds more than 512
+    groups, so the packing pass places its groups in several chunks."""
+    n = 330_000_123
+    rng = np.random.default_rng(5)
+    x = np.cumsum(rng.integers(1, 16, size=n, dtype=np.uint8), dtype=np.uint32)
+    c = g5.Codec(n)
+    try:
+        din = torch.from_numpy(x.view(np.int32)).cuda()
+        dout = torch.empty(g5.Codec.bound(n) + 8, dtype=torch.int32, device="cuda")
+        w = c.encode(din, n, dout, g5.CODEC_D4)
+        assert np.array_equal(host_u32(dout, w), orc.encode(x, orc.D4))
+        del din
+        back = torch.empty(n + 132, dtype=torch.int32, device="cuda")
+        assert c.decode(dout, w, back, n + 128, g5.CODEC_D4) == n
+        assert torch.equal(back[:n].cpu(), torch.from_numpy(x.view(np.int32)))
+    finally:
+        c.close()
+
+
 def test_level_queues(codec, golden_dir):
     fx = np.load(os.path.join(golden_dir, "levels_s12.npz"))
     qo, so = fx["q_off"], fx["s_off"]
