@@ -844,15 +844,16 @@ __global__ void __launch_bounds__(kOB) k_loc_tables(const uint32_t *__restrict__
             uint32_t r = kDead;
             if (a + p < h.nv) {
                 const uint4 hv = v[a + p];
-                uint32_t sum = 0;
-                bool ok = true;
+                // the 16 widths (bytes) added four at a time; a byte above
+                // 32 rules the vector out as a header
+                const uint32_t x[4] = {hv.x, hv.y, hv.z, hv.w};
+                uint32_t sum = 0, over = 0;
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const uint32_t b = width_of(hv, i);
-                    ok &= b <= 32;
-                    sum += b;
+                for (int j = 0; j < 4; ++j) {
+                    sum = __dp4a(x[j], 0x01010101u, sum);
+                    over |= __vcmpgtu4(x[j], 0x20202020u);
                 }
-                if (ok && a + p + 1 + sum <= h.nv) r = p + 1 + sum;  // <= S + 512 < kDead
+                if (!over && a + p + 1 + sum <= h.nv) r = p + 1 + sum;  // <= S + 512 < kDead
                 ljump[a + p] = (uint16_t)r;
             }
             s_j[p] = (uint16_t)r;
@@ -1024,9 +1025,17 @@ constexpr int kTM = 16 * kTG;   // miniblocks per tile
 __device__ __forceinline__ void mb_at(const uint32_t *in, uint32_t p, int i, uint64_t &off, uint32_t &b)
 {
     const uint4 hv = reinterpret_cast<const uint4 *>(in)[p];
-    uint64_t o = (uint64_t)p + 1;
-    for (int q = 0; q < i; ++q) o += width_of(hv, q);
-    off = o;
+    // the widths before i: the leading (big-endian) bytes of the header
+    // words, each word's bytes added by one dp4a
+    const uint32_t x[4] = {hv.x, hv.y, hv.z, hv.w};
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int keep = i - 4 * j;
+        const uint32_t m = keep >= 4 ? 0xFFFFFFFFu : keep <= 0 ? 0u : ~(0xFFFFFFFFu >> (8 * keep));
+        sum = __dp4a(x[j] & m, 0x01010101u, sum);
+    }
+    off = (uint64_t)p + 1 + sum;
     b = width_of(hv, i);
 }
 
