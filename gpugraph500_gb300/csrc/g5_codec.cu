@@ -481,6 +481,7 @@ __device__ void enc_tail_warp(const uint32_t *in, uint64_t n, uint64_t n1, uint6
 constexpr int kEB = 512;  // encoder threads per block: 16 warps
 constexpr int kEU = 4;    // miniblocks whose loads a warp has in flight together (widths)
 constexpr int kPU = 2;    // the same when packing (two blocks of 512 fit an SM at 64 registers)
+constexpr int kPC = 256;  // groups per packing chunk (each miniblock's place held in shared memory)
 
 struct EncLen {
     uint64_t n, n1, nmb, ng;
@@ -641,19 +642,19 @@ __device__ __forceinline__ uint32_t block_excl_u32(uint32_t x, uint32_t *s_w, ui
 }
 
 // Packs a miniblock's deltas (lane j holds vector j) with width b (1..31)
-// into shared memory at s + po: value j of lane l occupies bits j b .. of
-// lane l's bit stream, whose word w is s[po + 4 w + l]
+// into shared memory at s: value j of lane l occupies bits j b .. of lane
+// l's bit stream, whose word w is s[4 w + l]
 // (ipackwithoutmask<b>, simdintegratedbitpacking.cpp:875).  Each lane ORs
 // its four values into place (a value that straddles two words into both)
 // after the words are cleared: no division, no loop over values.
-__device__ __forceinline__ void pack_mb_smem(const uint4 &d, uint32_t b, uint32_t *s, uint32_t po)
+__device__ __forceinline__ void pack_mb_smem(const uint4 &d, uint32_t b, uint32_t *s)
 {
     const int lane = g5_lane();
-    for (uint32_t idx = lane; idx < 4 * b; idx += 32) s[po + idx] = 0;
+    if (lane < (int)b) reinterpret_cast<uint4 *>(s)[lane] = make_uint4(0, 0, 0, 0);  // 4 b words
     __syncwarp();
     const uint32_t bit = (uint32_t)lane * b, w = bit >> 5, sh = bit & 31;
     const bool spill = sh + b > 32;
-    uint32_t *p = s + po + 4 * w;
+    uint32_t *p = s + 4 * w;
     const uint32_t v[4] = {d.x, d.y, d.z, d.w};
 #pragma unroll
     for (int l = 0; l < 4; ++l) {
@@ -669,7 +670,8 @@ __global__ void __launch_bounds__(kEB, 2) k_enc_pack(const uint32_t *__restrict_
                                                   uint64_t *words_out, int mode)
 {
     __shared__ __align__(16) uint32_t s_stage[kEB / 32][128];  // one miniblock's payload per warp
-    __shared__ uint32_t s_goff[kEB];  // words from the chunk's first header to each group's header
+    __shared__ __align__(16) uint32_t s_moff[kPC * 16];  // words from the chunk's first header to each miniblock
+    __shared__ __align__(16) uint8_t s_mb[kPC * 16];     // each miniblock's width
     __shared__ uint64_t s_red[kEB / 32];
     __shared__ uint32_t s_w[kEB / 32 + 1];
     __shared__ uint32_t s_val[128];
@@ -705,39 +707,58 @@ __global__ void __launch_bounds__(kEB, 2) k_enc_pack(const uint32_t *__restrict_
     for (uint32_t i = threadIdx.x; i < blockIdx.x; i += kEB) x += btot[i];
     uint64_t cbase = 4 + block_sum_u64(x, s_red);  // word of the chunk's first group header
     uint32_t *stage = s_stage[wid];
-    for (uint64_t c0 = g0; c0 < g1; c0 += kEB) {
+    for (uint64_t c0 = g0; c0 < g1; c0 += kPC) {
+        // thread t < kPC takes group c0 + t: its size into the chunk's scan,
+        // then its header, and its miniblocks' places and widths into
+        // shared memory
         const uint64_t g = c0 + threadIdx.x;
-        const uint32_t gw = g < g1 ? 4 + 4 * widths_before(group_widths(wb, g, e.nmb), 16) : 0u;
+        const bool mine = threadIdx.x < kPC && g < g1;
+        uint4 wv = make_uint4(0, 0, 0, 0);
+        if (mine) wv = group_widths(wb, g, e.nmb);
         uint32_t ctot;
-        s_goff[threadIdx.x] = block_excl_u32(gw, s_w, ctot);
+        const uint32_t goff = block_excl_u32(mine ? 4 + 4 * widths_before(wv, 16) : 0u, s_w, ctot);
+        if (mine) {
+            // the 16 widths, big-endian bytes in each word (simdbinarypacking.h:200-214)
+            reinterpret_cast<uint4 *>(out + cbase + goff)[0] =
+                make_uint4(__byte_perm(wv.x, 0, 0x0123), __byte_perm(wv.y, 0, 0x0123),
+                           __byte_perm(wv.z, 0, 0x0123), __byte_perm(wv.w, 0, 0x0123));
+            reinterpret_cast<uint4 *>(s_mb)[threadIdx.x] = wv;
+            uint32_t o = goff + 4;
+            const uint32_t x[4] = {wv.x, wv.y, wv.z, wv.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                uint4 r;
+                r.x = o;
+                o += 4 * (x[j] & 0xFFu);
+                r.y = o;
+                o += 4 * ((x[j] >> 8) & 0xFFu);
+                r.z = o;
+                o += 4 * ((x[j] >> 16) & 0xFFu);
+                r.w = o;
+                o += 4 * (x[j] >> 24);
+                reinterpret_cast<uint4 *>(s_moff)[4 * threadIdx.x + j] = r;
+            }
+        }
         __syncthreads();
-        const uint64_t k1 = min(16 * min(c0 + kEB, g1), e.nmb);
-        for (uint64_t kb = 16 * c0 + wid; kb < k1; kb += 16 * kPU) {
-            uint4 cur[kPU], pl[kPU], gwd[kPU];
+        const uint64_t kc = 16 * c0;  // the chunk's first miniblock
+        const uint32_t mk = (uint32_t)(min(16 * min(c0 + kPC, g1), e.nmb) - kc);  // its miniblocks
+        for (uint32_t mb = wid; mb < mk; mb += 16 * kPU) {
+            uint4 cur[kPU], pl[kPU];
 #pragma unroll
             for (int i = 0; i < kPU; ++i) {
-                cur[i] = pl[i] = gwd[i] = make_uint4(0, 0, 0, 0);
-                const uint64_t k = kb + 16 * i;
-                if (k < k1) {
-                    load_cur(in, k, cur[i], pl[i]);
-                    gwd[i] = group_widths(wb, k / 16, e.nmb);
-                }
+                cur[i] = pl[i] = make_uint4(0, 0, 0, 0);
+                if (mb + 16 * i < mk) load_cur(in, kc + mb + 16 * i, cur[i], pl[i]);
             }
 #pragma unroll
             for (int i = 0; i < kPU; ++i) {
-                const uint64_t k = kb + 16 * i;
-                if (k >= k1) break;
-                const uint32_t q = (uint32_t)(k % 16);
-                const uint64_t gpos = cbase + s_goff[k / 16 - c0];
-                if (q == 0 && lane < 4)  // the group's header: its 16 widths, big-endian bytes
-                    out[gpos + lane] = __byte_perm(comp(gwd[i], lane), 0, 0x0123);
-                const uint32_t b = (comp(gwd[i], q / 4) >> (8 * (q % 4))) & 0xFFu;
-                const uint64_t pos = gpos + 4 + 4 * (uint64_t)widths_before(gwd[i], q);
-                uint4 *dst = reinterpret_cast<uint4 *>(out + pos);
+                const uint32_t m = mb + 16 * i;
+                if (m >= mk) break;
+                const uint32_t b = s_mb[m];
+                uint4 *dst = reinterpret_cast<uint4 *>(out + cbase + s_moff[m]);
                 if (b == 32) {
                     dst[lane] = cur[i];
                 } else if (b) {
-                    pack_mb_smem(deltas(cur[i], prev_of(cur[i], pl[i]), mode), b, stage, 0);
+                    pack_mb_smem(deltas(cur[i], prev_of(cur[i], pl[i]), mode), b, stage);
                     __syncwarp();
                     if (lane < (int)b) dst[lane] = reinterpret_cast<const uint4 *>(stage)[lane];
                     __syncwarp();
