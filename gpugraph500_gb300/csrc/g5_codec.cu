@@ -1916,8 +1916,7 @@ g5_status g5_codec_encode(g5_codec *c, const uint32_t *in_dev, size_t n, uint32_
     G5_CUDA(cudaGetLastError());
     G5_CUDA(cudaMemcpyAsync(c->h_scal, c->w.scal, sizeof(uint64_t) * 8, cudaMemcpyDeviceToHost, s));
     G5_CUDA(cudaStreamSynchronize(s));
-    if (c->h_scal[g5::CS_ERR] & G5_DEVERR_WAIT) return G5_ERR_TIMEOUT;
-    if (c->h_scal[g5::CS_ERR]) return G5_ERR_CAPACITY;
+    if (c->h_scal[g5::CS_ERR]) return G5_ERR_CAPACITY;  // the encoder has no device waits
     *out_words = (size_t)c->h_scal[g5::CS_WORDS];
     return G5_OK;
 }
