@@ -283,7 +283,7 @@ enum : uint32_t { ST_NONE = 0, ST_AGG = 1, ST_INC = 2 };
 
 // scalar slots of the one-pass kernels (the scalar block holds kScalars)
 enum {
-    CS_L_CTR = 20, CS_L_DONE = 21, CS_L_EPOCH = 22,
+    CS_L_CTR = 20, CS_L_DONE = 21,
     CS_U_CTR = 25, CS_U_DONE = 26, CS_U_EPOCH = 27
 };
 
@@ -833,6 +833,7 @@ __device__ __forceinline__ uint32_t width_of(uint4 h, int i)
 }
 
 constexpr int kLocMin = 2048, kLocMax = 16384;  // chunk sizes in vectors
+constexpr int kLocBatch = 4;                    // candidate vectors a thread loads together
 constexpr int kLocFit = 96;                     // chunks whose tables the walk holds in shared memory
 constexpr int kWalkThreads = 1024;
 
@@ -855,29 +856,39 @@ __global__ void __launch_bounds__(kOB) k_loc_tables(const uint32_t *__restrict__
     const DecHead h = dec_head(in, words_dev, cap, raw_thr, n_expect, max_vec, max_mb);
     const uint32_t S = loc_chunk(h.nv);
     const uint64_t nchunks = (h.raw || h.bad || h.ng == 0) ? 0 : (h.nv - 1 + S - 1) / S;
-    const uint64_t epoch = scal[CS_L_EPOCH];
     for (;;) {
         const uint64_t c = claim_tile(&scal[CS_L_CTR], &s_t);
         if (c >= nchunks) break;
         const uint64_t a = 1 + c * S;  // first vector of the chunk
         const uint4 *v = reinterpret_cast<const uint4 *>(in);
-        for (uint32_t p = threadIdx.x; p < S; p += kOB) {
-            uint32_t r = kDead;
-            if (a + p < h.nv) {
-                const uint4 hv = v[a + p];
-                // the 16 widths (bytes) added four at a time; a byte above
-                // 32 rules the vector out as a header
-                const uint32_t x[4] = {hv.x, hv.y, hv.z, hv.w};
-                uint32_t sum = 0, over = 0;
+        // kLocBatch of the thread's candidate vectors loaded together, then
+        // their jumps (S is a multiple of kOB * kLocBatch)
+        for (uint32_t p0 = threadIdx.x; p0 < S; p0 += kOB * kLocBatch) {
+            uint4 hv[kLocBatch];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    sum = __dp4a(x[j], 0x01010101u, sum);
-                    over |= __vcmpgtu4(x[j], 0x20202020u);
-                }
-                if (!over && a + p + 1 + sum <= h.nv) r = p + 1 + sum;  // <= S + 512 < kDead
-                ljump[a + p] = (uint16_t)r;
+            for (int i = 0; i < kLocBatch; ++i) {
+                const uint32_t p = p0 + i * kOB;
+                hv[i] = a + p < h.nv ? v[a + p] : make_uint4(0, 0, 0, 0);
             }
-            s_j[p] = (uint16_t)r;
+#pragma unroll
+            for (int i = 0; i < kLocBatch; ++i) {
+                const uint32_t p = p0 + i * kOB;
+                uint32_t r = kDead;
+                if (a + p < h.nv) {
+                    // the 16 widths (bytes) added four at a time; a byte
+                    // above 32 rules the vector out as a header
+                    const uint32_t x[4] = {hv[i].x, hv[i].y, hv[i].z, hv[i].w};
+                    uint32_t sum = 0, over = 0;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        sum = __dp4a(x[j], 0x01010101u, sum);
+                        over |= __vcmpgtu4(x[j], 0x20202020u);
+                    }
+                    if (!over && a + p + 1 + sum <= h.nv) r = p + 1 + sum;  // <= S + 512 < kDead
+                    ljump[a + p] = (uint16_t)r;
+                }
+                s_j[p] = (uint16_t)r;
+            }
         }
         __syncthreads();
         // transfer table: entry e -> (exit offset in the next chunk, groups started)
@@ -899,7 +910,6 @@ __global__ void __launch_bounds__(kOB) k_loc_tables(const uint32_t *__restrict__
     if (last_block(&scal[CS_L_DONE])) {
         scal[CS_L_CTR] = 0;
         scal[CS_L_DONE] = 0;
-        scal[CS_L_EPOCH] = epoch + 1;
         __threadfence();
     }
 }
@@ -993,7 +1003,19 @@ __global__ void __launch_bounds__(kOB) k_loc_pos(const uint32_t *__restrict__ in
         const uint64_t gnext = c + 1 < nchunks ? (lent[c + 1] >> 32) : ng;
         if (g0 >= gnext) continue;  // uniform over the block
         __syncthreads();            // the previous chunk's jumps are no longer read
-        for (uint32_t p = threadIdx.x; p < S && a + p < nv; p += kOB) s_j[p] = ljump[a + p];
+        for (uint32_t p0 = threadIdx.x; p0 < S; p0 += kOB * kLocBatch) {
+            uint16_t jv[kLocBatch];
+#pragma unroll
+            for (int i = 0; i < kLocBatch; ++i) {
+                const uint32_t p = p0 + i * kOB;
+                jv[i] = a + p < nv ? ljump[a + p] : (uint16_t)0;
+            }
+#pragma unroll
+            for (int i = 0; i < kLocBatch; ++i) {
+                const uint32_t p = p0 + i * kOB;
+                if (a + p < nv) s_j[p] = jv[i];
+            }
+        }
         __syncthreads();
         if (threadIdx.x != 0) continue;
         uint64_t p = en & 0xFFFFFFFFull;
@@ -1773,7 +1795,7 @@ g5_status codec_work_alloc(CodecWork &w, size_t max_n)
     G5_CUDA(cudaMemset(w.scal, 0, sizeof(uint64_t) * kScalars));
     G5_CUDA(cudaMemset(w.ust, 0, sizeof(uint64_t) * T));
     const uint64_t one = 1;
-    for (int e : {CS_L_EPOCH, CS_U_EPOCH})
+    for (int e : {CS_U_EPOCH})
         G5_CUDA(cudaMemcpy(w.scal + e, &one, sizeof one, cudaMemcpyHostToDevice));
     return G5_OK;
 }
