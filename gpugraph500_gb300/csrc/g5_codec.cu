@@ -834,6 +834,8 @@ __device__ __forceinline__ uint32_t width_of(uint4 h, int i)
 
 constexpr int kLocMin = 2048, kLocMax = 16384;  // chunk sizes in vectors
 constexpr int kLocBatch = 4;                    // candidate vectors a thread loads together
+// a chunk's candidates are read in whole rounds of kOB * kLocBatch, none past its end
+static_assert(kLocMin % (kOB * kLocBatch) == 0, "chunk sizes must be whole load rounds");
 constexpr int kLocFit = 96;                     // chunks whose tables the walk holds in shared memory
 constexpr int kWalkThreads = 1024;
 
