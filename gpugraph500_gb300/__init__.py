@@ -59,7 +59,7 @@ class BfsStats(C.Structure):
                 ("codec_words", C.c_int64), ("codec_values", C.c_int64), ("alg_bytes", C.c_int64),
                 ("device_ms", C.c_double), ("kernel_ms", C.c_double * 8)]
 
-    KERNELS = ("prologue", "expand", "fixup", "count", "scan", "write", "codec")
+    KERNELS = ("prologue", "expand", "fixup", "count", "scan", "write", "codec", "host")
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "kernel_ms"}

@@ -1323,7 +1323,9 @@ __global__ void k_val_edges(const int64_t *__restrict__ row_off, const uint32_t 
 }
 
 // Kernel kinds timed in profile mode.
-enum { KP_PRO = 0, KP_EXPAND, KP_FIXUP, KP_COUNT, KP_SCAN, KP_WRITE, KP_CODEC, KP_N };
+// profile-mode buckets; KP_HOST is the host loop's gap after a level (its
+// state read-back and synchronise) up to the next level's first launch
+enum { KP_PRO = 0, KP_EXPAND, KP_FIXUP, KP_COUNT, KP_SCAN, KP_WRITE, KP_CODEC, KP_HOST, KP_N };
 
 struct Prof {
     bool on = false;
@@ -1455,6 +1457,7 @@ void enqueue_level(g5_bfs *b, const BfsArgs &a, cudaStream_t s, Prof *pf = nullp
         g5::decode_launch_acc(b->cw, b->codec_stream, b->cw.scal + g5::CS_WORDS, b->dqueue, (size_t)a.n,
                               a.codec, b->cfg.codec_threshold, &b->st->nf, b->queue, b->st->codec_acc, s);
     }
+    p.mark(KP_HOST, s);
 }
 
 // The search as one CUDA graph writing its parents to `pred`: the prologue,

@@ -180,7 +180,8 @@ typedef struct g5_bfs_stats {
                                  level)                                          */
     double device_ms;         /* device time of the search (CUDA events)          */
     double kernel_ms[8];      /* profile mode: prologue, expand, fixup, count,
-                                 scan, write, codec, unused (ms, summed)          */
+                                 scan, write, codec, and the host loop's gap
+                                 after each level (ms, summed)                    */
 } g5_bfs_stats;
 
 /* One BFS from root: GlobalBFS::runBFS (cpu_2d/globalbfs.hh:548-1263) at 1x1
