@@ -424,39 +424,51 @@ __device__ __forceinline__ bool last_block(uint64_t *done)
 
 // Stream header words and the VariableByte tail of n - n1 (< 128) values,
 // written by one warp; blkend = word after the block part.  Total words ->
-// scal[CS_WORDS] and, if given, *words_out.  (compositecodec.h:31-51, variablebyte.h:100-161.)
+// scal[CS_WORDS] and, if given, *words_out.  (compositecodec.h:31-51,
+// variablebyte.h:100-161: each value's delta from the one before, 0 before
+// the first, in 7-bit groups from the low end, the high bit on the last
+// byte, zero-padded to a word.)  One lane per value: its byte count, their
+// exclusive prefix over the warp (its place), then its bytes.
 __device__ void enc_tail_warp(const uint32_t *in, uint64_t n, uint64_t n1, uint64_t blkend, uint32_t *out,
-                              uint64_t *scal, uint64_t *words_out, uint32_t *s_val, uint32_t *s_bytes)
+                              uint64_t *scal, uint64_t *words_out, uint32_t *s_bytes)
 {
     const int lane = g5_lane();
     const uint32_t nt = (uint32_t)(n - n1);
-    for (uint32_t i = lane; i < nt; i += 32) s_val[i] = in[n1 + i];
     for (uint32_t i = lane; i < (128 * 5 + 3) / 4 + 1; i += 32) s_bytes[i] = 0;
     __syncwarp();
+    uint8_t *bb = reinterpret_cast<uint8_t *>(s_bytes);
+    uint32_t p = 0, last = 0;  // bytes so far and the value before this round (warp-uniform)
+    for (uint32_t i0 = 0; i0 < nt; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const bool have = i < nt;
+        const uint32_t x = have ? in[n1 + i] : 0u;
+        uint32_t px = __shfl_up_sync(0xFFFFFFFFu, x, 1);
+        if (lane == 0) px = last;
+        const uint32_t d = x - px;
+        const uint32_t len = have ? 1u + (d >= (1u << 7)) + (d >= (1u << 14)) + (d >= (1u << 21)) + (d >= (1u << 28)) : 0u;
+        uint32_t inc = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        const uint32_t at = p + inc - len;
+        for (uint32_t k = 0; k < len; ++k)
+            bb[at + k] = (uint8_t)(((d >> (7 * k)) & 127u) | (k + 1 == len ? 128u : 0u));
+        p += __shfl_sync(0xFFFFFFFFu, inc, 31);
+        last = __shfl_sync(0xFFFFFFFFu, x, 31);
+    }
+    __syncwarp();
+    const uint32_t tw = (p + 3) / 4;
     if (lane == 0) {
         out[0] = (uint32_t)n1;
         out[1] = kCookie;
         out[2] = kCookie;
         out[3] = kCookie;
-        uint8_t *bb = reinterpret_cast<uint8_t *>(s_bytes);
-        uint32_t p = 0, prev = 0;
-        for (uint32_t i = 0; i < nt; ++i) {
-            uint32_t v = s_val[i] - prev;
-            prev = s_val[i];
-            while (v >= 128u) {
-                bb[p++] = (uint8_t)(v & 127u);
-                v >>= 7;
-            }
-            bb[p++] = (uint8_t)(v | 128u);
-        }
-        const uint32_t tw = (p + 3) / 4;
-        s_val[0] = tw;
         scal[CS_WORDS] = blkend + tw;
         if (words_out) *words_out = blkend + tw;
         scal[CS_BLKEND] = blkend;
     }
-    __syncwarp();
-    const uint32_t tw = s_val[0];
     for (uint32_t i = lane; i < tw; i += 32) out[blkend + i] = s_bytes[i];
 }
 
@@ -674,7 +686,6 @@ __global__ void __launch_bounds__(kEB, 2) k_enc_pack(const uint32_t *__restrict_
     __shared__ __align__(16) uint8_t s_mb[kPC * 16];     // each miniblock's width
     __shared__ uint64_t s_red[kEB / 32];
     __shared__ uint32_t s_w[kEB / 32 + 1];
-    __shared__ uint32_t s_val[128];
     __shared__ uint32_t s_bytes[(128 * 5 + 3) / 4 + 1];
     g5_pdl_sync();
     const EncLen e = enc_len(n_dev, max_n, raw_thr);
@@ -697,7 +708,7 @@ __global__ void __launch_bounds__(kEB, 2) k_enc_pack(const uint32_t *__restrict_
         return;
     }
     if (e.ng == 0) {
-        if (blockIdx.x == 0 && wid == 0) enc_tail_warp(in, e.n, e.n1, 4, out, scal, words_out, s_val, s_bytes);
+        if (blockIdx.x == 0 && wid == 0) enc_tail_warp(in, e.n, e.n1, 4, out, scal, words_out, s_bytes);
         return;
     }
     uint64_t g0, g1;
@@ -768,7 +779,7 @@ __global__ void __launch_bounds__(kEB, 2) k_enc_pack(const uint32_t *__restrict_
         cbase += ctot;
         __syncthreads();
     }
-    if (g1 == e.ng && wid == 0) enc_tail_warp(in, e.n, e.n1, cbase, out, scal, words_out, s_val, s_bytes);
+    if (g1 == e.ng && wid == 0) enc_tail_warp(in, e.n, e.n1, cbase, out, scal, words_out, s_bytes);
 }
 
 // ---- decoder: locate groups ----------------------------------------------------------
@@ -1142,6 +1153,66 @@ __device__ __forceinline__ uint4 mb_values(const uint4 &d, uint32_t b, const uin
     return make_uint4(cx + base.x, cy + base.y, cz + base.z, cw + base.w);
 }
 
+// VariableByte tail decoded by one warp (variablebyte.h:217-): nbytes bytes
+// in bb (shared memory), values from out[o] on, each the running sum of the
+// decoded deltas from 0; o (warp-uniform) ends past the last value.  A byte
+// with the high bit ends a value; a sixth byte of one value (a fifth byte
+// without the high bit) or an output index at cap makes the stream corrupt
+// and ends the decode there, as the sequential decoder does.  32 bytes per
+// round: a ballot marks the values' last bytes, the lane holding one
+// gathers its value's bytes from the previous last byte on, and a warp scan
+// of the values gives the running sums.
+__device__ void dec_tail_warp(const uint8_t *bb, uint32_t nbytes, uint64_t cap, uint32_t *out,
+                              const uint32_t *expect, uint64_t &o, uint64_t &e)
+{
+    const int lane = g5_lane();
+    const unsigned lt = g5_lanemask_lt();
+    uint32_t run = 0;    // the last value so far
+    int last_end = -1;   // byte index of the last value's last byte
+    for (uint32_t b0 = 0; b0 < nbytes; b0 += 32) {
+        const uint32_t pb = b0 + lane;
+        const bool in_range = pb < nbytes;
+        const bool term = in_range && (bb[pb] & 128u);
+        const unsigned tm = __ballot_sync(0xFFFFFFFFu, term);
+        const unsigned below = tm & lt;
+        const int prev_end = below ? (int)(b0 + 31 - __clz(below)) : last_end;
+        // the fifth byte of a value without the high bit
+        const unsigned em = __ballot_sync(0xFFFFFFFFu, in_range && !term && (int)pb - prev_end >= 5);
+        unsigned ok = em ? tm & ((1u << (__ffs(em) - 1)) - 1u) : tm;  // values ending before it
+        // output capacity, checked value by value
+        const uint64_t room = cap > o ? cap - o : 0;
+        if ((uint64_t)__popc(ok) > room) {
+            unsigned keep = ok;
+            for (uint64_t k = 0; k < room; ++k) keep &= keep - 1;  // drop the first `room` values
+            ok &= ~keep;
+            e |= G5_DEVERR_CORRUPT;
+        }
+        if (em) e |= G5_DEVERR_CORRUPT;
+        const bool mine = (ok >> lane) & 1u;
+        uint32_t v = 0;
+        if (mine)
+            for (int k = prev_end + 1, sh = 0; k <= (int)pb; ++k, sh += 7) v |= (uint32_t)(bb[k] & 127u) << sh;
+        uint32_t inc = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, d);
+            if (lane >= d) inc += y;
+        }
+        if (mine) {
+            const uint64_t idx = o + __popc(ok & lt);
+            const uint32_t val = run + inc;
+            out[idx] = val;
+            if (expect && expect[idx] != val) e |= G5_DEVERR_MISMATCH;
+        }
+        o += __popc(ok);
+        run += __shfl_sync(0xFFFFFFFFu, inc, 31);
+        if (tm) last_end = (int)(b0 + 31 - __clz(tm));
+        if (e & G5_DEVERR_CORRUPT) break;
+    }
+    // the lanes' mismatch flags into one
+    e |= __reduce_or_sync(0xFFFFFFFFu, (unsigned)(e & G5_DEVERR_MISMATCH)) ? G5_DEVERR_MISMATCH : 0;
+}
+
 __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__ in, uint64_t *scal,
                                                     const uint32_t *__restrict__ gpos, uint32_t *__restrict__ out,
                                                     uint64_t cap, const uint64_t *n_expect,
@@ -1195,33 +1266,9 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
             } else {
                 for (uint64_t i = lane; i < tw; i += 32) s_b[i] = in[blkend + i];
                 __syncwarp();
+                uint64_t o = n1, e = 0;
+                dec_tail_warp(reinterpret_cast<const uint8_t *>(s_b), (uint32_t)(tw * 4), cap, out, expect, o, e);
                 if (lane == 0) {
-                    const uint8_t *bb = reinterpret_cast<const uint8_t *>(s_b);
-                    uint64_t o = n1, e = 0;
-                    uint32_t prev = 0, v = 0;
-                    int shift = 0;
-                    for (uint64_t p = 0; p < tw * 4; ++p) {
-                        const uint32_t c = bb[p];
-                        v |= (c & 127u) << shift;
-                        if (c & 128u) {
-                            if (o >= cap) {
-                                e |= G5_DEVERR_CORRUPT;
-                                break;
-                            }
-                            prev += v;
-                            out[o] = prev;
-                            if (expect && expect[o] != prev) e |= G5_DEVERR_MISMATCH;
-                            ++o;
-                            v = 0;
-                            shift = 0;
-                        } else {
-                            shift += 7;
-                            if (shift > 28) {
-                                e |= G5_DEVERR_CORRUPT;
-                                break;
-                            }
-                        }
-                    }
                     scal[CS_N] = o;
                     if (n_out) *n_out = o;
                     if (n_expect && o != *n_expect) e |= G5_DEVERR_MISMATCH;
