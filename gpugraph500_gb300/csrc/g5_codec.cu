@@ -1095,35 +1095,22 @@ __device__ __forceinline__ void mb_at(const uint32_t *in, uint32_t p, int i, uin
     b = width_of(hv, i);
 }
 
-__device__ __forceinline__ VecFlag mb_aggregate(const uint4 &d, uint32_t b, int mode)
+// A miniblock's deltas (lane j: vector j) turned into its running sums from
+// the miniblock's start, in place, and the miniblock's aggregate in lane 31
+// (its lane sums, or for a raw b = 32 miniblock its last vector with a reset
+// flag).  d4 sums each lane component over the vectors; dm sums component 3
+// (every component of a vector is relative to component 3 of the vector
+// before), so components 0-2 keep their deltas.  One scan serves both the
+// aggregate and, after the prefix of what comes before is known, the values.
+__device__ __forceinline__ VecFlag mb_scan(uint4 &d, uint32_t b, int mode)
 {
+    const int lane = g5_lane();
     VecFlag r;
     if (b == 32) {
-        r.v.x = __shfl_sync(0xFFFFFFFFu, d.x, 31);
-        r.v.y = __shfl_sync(0xFFFFFFFFu, d.y, 31);
-        r.v.z = __shfl_sync(0xFFFFFFFFu, d.z, 31);
-        r.v.w = __shfl_sync(0xFFFFFFFFu, d.w, 31);
+        r.v = d;
         r.f = 1;
         return r;
     }
-    uint32_t sx = d.x, sy = d.y, sz = d.z, sw = d.w;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        sx += __shfl_xor_sync(0xFFFFFFFFu, sx, o);
-        sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
-        sz += __shfl_xor_sync(0xFFFFFFFFu, sz, o);
-        sw += __shfl_xor_sync(0xFFFFFFFFu, sw, o);
-    }
-    r.v = mode == G5_CODEC_DM ? make_uint4(sw, sw, sw, sw) : make_uint4(sx, sy, sz, sw);
-    r.f = 0;
-    return r;
-}
-
-// Absolute values of a miniblock from its deltas (or raw vector) and base.
-__device__ __forceinline__ uint4 mb_values(const uint4 &d, uint32_t b, const uint4 &base, int mode)
-{
-    const int lane = g5_lane();
-    if (b == 32) return d;
     if (mode == G5_CODEC_DM) {
         uint32_t c = d.w;
 #pragma unroll
@@ -1131,26 +1118,42 @@ __device__ __forceinline__ uint4 mb_values(const uint4 &d, uint32_t b, const uin
             const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, c, o);
             if (lane >= o) c += y;
         }
-        c += base.w;
+        d.w = c;
+        r.v = make_uint4(c, c, c, c);
+    } else {
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t yx = __shfl_up_sync(0xFFFFFFFFu, d.x, o);
+            const uint32_t yy = __shfl_up_sync(0xFFFFFFFFu, d.y, o);
+            const uint32_t yz = __shfl_up_sync(0xFFFFFFFFu, d.z, o);
+            const uint32_t yw = __shfl_up_sync(0xFFFFFFFFu, d.w, o);
+            if (lane >= o) {
+                d.x += yx;
+                d.y += yy;
+                d.z += yz;
+                d.w += yw;
+            }
+        }
+        r.v = d;
+    }
+    r.f = 0;
+    return r;
+}
+
+// Absolute values of a miniblock from its running sums (mb_scan) and the
+// sums of everything before it in the tile (base); a raw miniblock is its
+// own values.
+__device__ __forceinline__ uint4 mb_values(const uint4 &s, uint32_t b, const uint4 &base, int mode)
+{
+    const int lane = g5_lane();
+    if (b == 32) return s;
+    if (mode == G5_CODEC_DM) {
+        const uint32_t c = s.w + base.w;
         uint32_t pc = __shfl_up_sync(0xFFFFFFFFu, c, 1);
         if (lane == 0) pc = base.w;
-        return make_uint4(d.x + pc, d.y + pc, d.z + pc, c);
+        return make_uint4(s.x + pc, s.y + pc, s.z + pc, c);
     }
-    uint32_t cx = d.x, cy = d.y, cz = d.z, cw = d.w;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t yx = __shfl_up_sync(0xFFFFFFFFu, cx, o);
-        const uint32_t yy = __shfl_up_sync(0xFFFFFFFFu, cy, o);
-        const uint32_t yz = __shfl_up_sync(0xFFFFFFFFu, cz, o);
-        const uint32_t yw = __shfl_up_sync(0xFFFFFFFFu, cw, o);
-        if (lane >= o) {
-            cx += yx;
-            cy += yy;
-            cz += yz;
-            cw += yw;
-        }
-    }
-    return make_uint4(cx + base.x, cy + base.y, cz + base.z, cw + base.w);
+    return make_uint4(s.x + base.x, s.y + base.y, s.z + base.z, s.w + base.w);
 }
 
 // VariableByte tail decoded by one warp (variablebyte.h:217-): nbytes bytes
@@ -1301,8 +1304,9 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
 #pragma unroll
             for (int i = 0; i < kTG; ++i) {
                 const uint64_t k = k0 + 16 * i + wid;
-                const VecFlag m = k < nmb ? mb_aggregate(d[i], b[i], mode) : ResetAdd::id();
-                if (lane == 0) s_vf[16 * i + wid] = m;
+                // running sums in place; lane 31 holds the aggregate
+                const VecFlag m = k < nmb ? mb_scan(d[i], b[i], mode) : ResetAdd::id();
+                if (lane == 31) s_vf[16 * i + wid] = m;
             }
             __syncthreads();
             if (wid == 0) {
