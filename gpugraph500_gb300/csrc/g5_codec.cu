@@ -1063,18 +1063,24 @@ __global__ void __launch_bounds__(kOB) k_loc_pos(const uint32_t *__restrict__ in
 
 // ---- decoder: unpack (one pass) --------------------------------------------------------
 //
-// One tile per kTG groups, warp w unpacking miniblocks w, w + 16, w + 32 and
-// w + 48 of the tile at the positions the locator found: first every warp
-// unpacks its miniblocks and forms their aggregates (the lane sums, or for a
-// raw b = 32 miniblock its last vector with a reset flag), the tile's
-// aggregate goes through the look-back, then each warp unpacks its
-// miniblocks again (from L1 / L2) and adds the prefix of everything before
-// them.  Block 0 first decodes the VariableByte tail, which starts from 0
-// whatever the block part holds.  With `expect` every value is compared with
-// the expected one (the level loop's round-trip check); `acc` accumulates
-// words and values.
-constexpr int kTG = 4;          // groups per unpacker tile
-constexpr int kTM = 16 * kTG;   // miniblocks per tile
+// Tiles of 4 or 8 groups (8 when tiles of 4 would need more than one wave
+// of the grid: fewer tiles make a shorter look-back chain), warp w taking
+// miniblocks w, w + 16, w + 32, ... of the tile, four at a time, at the
+// positions the locator found: one lane scan per miniblock gives its values
+// from the miniblock's start (staged in shared memory) and, in lane 31, its
+// aggregate (the lane sums, or for a raw b = 32 miniblock its last vector
+// with a reset flag); warp 0 scans the tile's aggregates, finds the tile's
+// prefix by look-back and each miniblock's base, which is added as the
+// values are written.  Block 0 first decodes the VariableByte tail, which
+// starts from 0 whatever the block part holds.  With `expect` every value
+// is compared with the expected one (the level loop's round-trip check);
+// `acc` accumulates words and values.
+constexpr int kTG = 8;          // groups per unpacker tile, at most (4 or 8, see k_dec_unpack)
+constexpr int kTM = 16 * kTG;   // miniblocks per tile, at most (each warp takes four at a time)
+// dynamic shared memory of the unpacker: each miniblock's values relative
+// to its start (kTM x 32 vectors), aggregates, in-tile prefixes, bases, raw flags
+constexpr size_t kUValBytes = sizeof(uint4) * kTM * 32;
+constexpr size_t kUSmem = kUValBytes + 2 * sizeof(VecFlag) * kTM + sizeof(uint4) * kTM + kTM;
 
 // Stream position (16-byte vectors) and width of miniblock i of the group
 // whose header is at vector p.
@@ -1101,7 +1107,7 @@ __device__ __forceinline__ void mb_at(const uint32_t *in, uint32_t p, int i, uin
 // flag).  d4 sums each lane component over the vectors; dm sums component 3
 // (every component of a vector is relative to component 3 of the vector
 // before), so components 0-2 keep their deltas.  One scan serves both the
-// aggregate and, after the prefix of what comes before is known, the values.
+// aggregate and the values from the miniblock's start.
 __device__ __forceinline__ VecFlag mb_scan(uint4 &d, uint32_t b, int mode)
 {
     const int lane = g5_lane();
@@ -1138,22 +1144,6 @@ __device__ __forceinline__ VecFlag mb_scan(uint4 &d, uint32_t b, int mode)
     }
     r.f = 0;
     return r;
-}
-
-// Absolute values of a miniblock from its running sums (mb_scan) and the
-// sums of everything before it in the tile (base); a raw miniblock is its
-// own values.
-__device__ __forceinline__ uint4 mb_values(const uint4 &s, uint32_t b, const uint4 &base, int mode)
-{
-    const int lane = g5_lane();
-    if (b == 32) return s;
-    if (mode == G5_CODEC_DM) {
-        const uint32_t c = s.w + base.w;
-        uint32_t pc = __shfl_up_sync(0xFFFFFFFFu, c, 1);
-        if (lane == 0) pc = base.w;
-        return make_uint4(s.x + pc, s.y + pc, s.z + pc, c);
-    }
-    return make_uint4(s.x + base.x, s.y + base.y, s.z + base.z, s.w + base.w);
 }
 
 // VariableByte tail decoded by one warp (variablebyte.h:217-): nbytes bytes
@@ -1223,11 +1213,13 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
                                                     uint64_t *ust, VecFlag *uagg, VecFlag *uinc, uint64_t *n_out,
                                                     int mode)
 {
-    __shared__ VecFlag s_vf[kTM];
-    __shared__ VecFlag s_base[kTM];     // each miniblock's prefix from the tile's start
-    __shared__ VecFlag s_ex;            // the tile's exclusive prefix (look-back)
-    __shared__ uint8_t s_abs[kTM];      // 1: the miniblock's values need no tile prefix
-    __shared__ __align__(16) uint32_t s_val[kTM * 128];  // the tile's values before the tile prefix
+    extern __shared__ __align__(16) unsigned char s_dyn_u[];
+    uint4 *s_val = reinterpret_cast<uint4 *>(s_dyn_u);                        // values from each miniblock's start
+    VecFlag *s_vf = reinterpret_cast<VecFlag *>(s_dyn_u + kUValBytes);        // miniblock aggregates
+    VecFlag *s_base = s_vf + kTM;                                              // prefixes from the tile's start
+    uint4 *s_full = reinterpret_cast<uint4 *>(s_base + kTM);                   // each miniblock's base
+    uint8_t *s_raw = reinterpret_cast<uint8_t *>(s_full + kTM);                // 1: a raw miniblock
+    __shared__ VecFlag s_ex;            // the tile's aggregate, then its exclusive prefix (look-back)
     __shared__ uint64_t s_t;
     __shared__ uint32_t s_b[kTailMaxBytes / 4];
     const int lane = g5_lane(), wid = threadIdx.x >> 5;
@@ -1256,7 +1248,12 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
         }
     } else if (!err0) {
         const uint64_t nmb = scal[CS_NMB], ng = scal[CS_NG], n1 = scal[CS_N1];
-        const uint64_t ntiles = (ng + kTG - 1) / kTG;
+        // tiles of 8 groups when tiles of 4 would not all fit in one wave of
+        // the grid (fewer tiles, so a shorter look-back chain), else of 4 (more
+        // blocks at work on mid-size streams); every block decides alike
+        const int R = (ng + 3) / 4 > (uint64_t)gridDim.x ? 2 : 1;  // rounds of four miniblocks per warp
+        const uint64_t tm = 64ull * R;                              // miniblocks per tile
+        const uint64_t ntiles = (nmb + tm - 1) / tm;
         if (blockIdx.x == 0 && wid == 0) {
             // VariableByte tail (variablebyte.h:217-): words after the block part
             const uint64_t blkend = scal[CS_BLKEND];
@@ -1286,34 +1283,53 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
         for (;;) {
             const uint64_t t = claim_tile(&scal[CS_U_CTR], &s_t);
             if (t >= ntiles) break;
-            const uint64_t k0 = (uint64_t)kTM * t;
-            // aggregates: the warp's positions and loads first
-            uint4 d[kTG];
-            uint32_t b[kTG];
+            const uint64_t k0 = tm * t;
+            // each warp's miniblocks wid, wid + 16, ..., four at a time: the
+            // positions and loads first, then one lane scan per miniblock,
+            // whose running sums are the values from the miniblock's start
+            // (for dm, components 0-2 take the running component 3 of the
+            // vector before) and whose lane 31 holds the aggregate
+#pragma unroll 1
+            for (int r = 0; r < R; ++r) {
+                uint4 d[4];
+                uint32_t b[4];
 #pragma unroll
-            for (int i = 0; i < kTG; ++i) {
-                const uint64_t k = k0 + 16 * i + wid;
-                d[i] = make_uint4(0, 0, 0, 0);
-                b[i] = 0;
-                if (k < nmb) {
-                    uint64_t off;
-                    mb_at(in, gpos[k / 16], wid, off, b[i]);
-                    d[i] = unpack_vec(in, off, b[i]);
+                for (int i = 0; i < 4; ++i) {
+                    const uint64_t k = k0 + wid + 16 * (4 * r + i);
+                    d[i] = make_uint4(0, 0, 0, 0);
+                    b[i] = 0;
+                    if (k < nmb) {
+                        uint64_t off;
+                        mb_at(in, gpos[k / 16], wid, off, b[i]);
+                        d[i] = unpack_vec(in, off, b[i]);
+                    }
                 }
-            }
 #pragma unroll
-            for (int i = 0; i < kTG; ++i) {
-                const uint64_t k = k0 + 16 * i + wid;
-                // running sums in place; lane 31 holds the aggregate
-                const VecFlag m = k < nmb ? mb_scan(d[i], b[i], mode) : ResetAdd::id();
-                if (lane == 31) s_vf[16 * i + wid] = m;
+                for (int i = 0; i < 4; ++i) {
+                    const int m = wid + 16 * (4 * r + i);
+                    if (k0 + m < nmb) {
+                        const VecFlag agg = mb_scan(d[i], b[i], mode);
+                        uint4 rel = d[i];
+                        if (b[i] != 32 && mode == G5_CODEC_DM) {
+                            uint32_t cp = __shfl_up_sync(0xFFFFFFFFu, d[i].w, 1);
+                            if (lane == 0) cp = 0;
+                            rel = make_uint4(d[i].x + cp, d[i].y + cp, d[i].z + cp, d[i].w);
+                        }
+                        s_val[m * 32 + lane] = rel;
+                        if (lane == 31) s_vf[m] = agg;
+                        if (lane == 0) s_raw[m] = b[i] == 32 ? 1 : 0;
+                    } else if (lane == 31) {
+                        s_vf[m] = ResetAdd::id();
+                    }
+                }
             }
             __syncthreads();
             if (wid == 0) {
-                // prefixes from the tile's start, two miniblocks per lane (a
-                // reset inside the tile makes the rest absolute)
-                const VecFlag v0 = s_vf[2 * lane], v1 = s_vf[2 * lane + 1];
-                const VecFlag c = ResetAdd::op(v0, v1);
+                // prefixes from the tile's start, 2 R miniblocks per lane in
+                // order (a reset inside the tile makes the rest absolute)
+                const int kPer = 2 * R;
+                VecFlag c = s_vf[kPer * lane];
+                for (int j = 1; j < kPer; ++j) c = ResetAdd::op(c, s_vf[kPer * lane + j]);
                 VecFlag inc = c;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
@@ -1322,46 +1338,38 @@ __global__ void __launch_bounds__(kOB) k_dec_unpack(const uint32_t *__restrict__
                 }
                 VecFlag ex = ResetAdd::shfl_up(inc, 1);
                 if (lane == 0) ex = ResetAdd::id();
-                s_base[2 * lane] = ex;
-                s_abs[2 * lane] = (uint8_t)(ex.f | v0.f);
-                const VecFlag e1 = ResetAdd::op(ex, v0);
-                s_base[2 * lane + 1] = e1;
-                s_abs[2 * lane + 1] = (uint8_t)(e1.f | v1.f);
+                for (int j = 0; j < kPer; ++j) {
+                    s_base[kPer * lane + j] = ex;
+                    ex = ResetAdd::op(ex, s_vf[kPer * lane + j]);
+                }
                 if (lane == 31) s_ex = inc;  // the tile's aggregate, until the look-back replaces it
             }
             __syncthreads();
-            // warp 0 finds the tile's prefix (look-back) while the warps turn
-            // their deltas into values relative to the tile's start
+            // warp 0 finds the tile's prefix (look-back), then every
+            // miniblock's base: the tile's prefix combined with the
+            // miniblock's prefix inside the tile
             if (wid == 0) {
-                const VecFlag ex = lookback<ResetAddV>(ust, uagg, uinc, t, epoch, s_ex, &scal[CS_ERR]);
-                __syncwarp();
-                if (lane == 0) s_ex = ex;
-            }
-#pragma unroll
-            for (int i = 0; i < kTG; ++i) {
-                const uint64_t k = k0 + 16 * i + wid;
-                if (k < nmb)
-                    reinterpret_cast<uint4 *>(s_val)[(16 * i + wid) * 32 + lane] =
-                        mb_values(d[i], b[i], s_base[16 * i + wid].v, mode);
+                const VecFlag pre = lookback<ResetAddV>(ust, uagg, uinc, t, epoch, s_ex, &scal[CS_ERR]);
+                for (int m = lane; m < (int)tm; m += 32) s_full[m] = ResetAdd::op(pre, s_base[m]).v;
             }
             __syncthreads();
             {
-                const VecFlag ex = s_ex;
-                const uint64_t kn = min((uint64_t)kTM, nmb - k0);  // miniblocks in this tile
+                const uint64_t kn = min(tm, nmb - k0);  // miniblocks in this tile
                 for (uint32_t q = threadIdx.x; q < kn * 32; q += kOB) {
                     const uint32_t m = q >> 5;  // miniblock of this 16-byte vector
-                    uint4 x = reinterpret_cast<const uint4 *>(s_val)[q];
-                    if (!s_abs[m]) {
+                    uint4 x = s_val[q];
+                    if (!s_raw[m]) {
+                        const uint4 bm = s_full[m];
                         if (mode == G5_CODEC_DM) {
-                            x.x += ex.v.w;
-                            x.y += ex.v.w;
-                            x.z += ex.v.w;
-                            x.w += ex.v.w;
+                            x.x += bm.w;
+                            x.y += bm.w;
+                            x.z += bm.w;
+                            x.w += bm.w;
                         } else {
-                            x.x += ex.v.x;
-                            x.y += ex.v.y;
-                            x.z += ex.v.z;
-                            x.w += ex.v.w;
+                            x.x += bm.x;
+                            x.y += bm.y;
+                            x.z += bm.z;
+                            x.w += bm.w;
                         }
                     }
                     reinterpret_cast<uint4 *>(out)[k0 * 32 + q] = x;
@@ -1841,6 +1849,7 @@ g5_status codec_work_alloc(CodecWork &w, size_t max_n)
     // the walk's table cache needs more than 48 KB of shared memory (set per device)
     G5_CUDA(cudaFuncSetAttribute(k_loc_walk, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(uint32_t) * kEntries * kLocFit)));
+    G5_CUDA(cudaFuncSetAttribute(k_dec_unpack, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUSmem));
     G5_CUDA(cudaMalloc(&w.ust, sizeof(uint64_t) * T));
     G5_CUDA(cudaMalloc(&w.uagg, sizeof(VecFlag) * 2 * T));
     w.uinc = w.uagg + T;
@@ -1896,8 +1905,8 @@ void decode_launch_acc(CodecWork &w, const uint32_t *in, const uint64_t *words_d
     launch_dyn(true, k_loc_walk, 1, kWalkThreads, sizeof(uint32_t) * kEntries * kLocFit, s, in, words_dev, c, rt,
                n_expect_dev, w.scal, mv, mm, (const uint32_t *)w.ltab, w.lent);
     launch(true, k_loc_pos, w.grid, kOB, s, in, w.scal, (const uint16_t *)w.ljump, (const uint64_t *)w.lent, w.gpos);
-    launch(true, k_dec_unpack, w.grid, kOB, s, in, w.scal, (const uint32_t *)w.gpos, out, c, n_expect_dev, expect,
-           acc, w.ust, w.uagg, w.uinc, n_out, mode);
+    launch_dyn(true, k_dec_unpack, w.grid, kOB, kUSmem, s, in, w.scal, (const uint32_t *)w.gpos, out, c,
+               n_expect_dev, expect, acc, w.ust, w.uagg, w.uinc, n_out, mode);
 }
 
 }  // namespace g5
