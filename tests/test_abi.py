@@ -94,3 +94,18 @@ def test_codec_batch_bound(libg5):
     want = sum((libg5.g5_codec_bound(n) + 3) // 4 * 4 for n in sizes)
     assert g5.Codec.batch_bound(in_off) == want
     assert g5.Codec.batch_bound(np.zeros(1, np.uint64)) == 0
+
+
+def test_stats_struct_mirrors_header():
+    """g5_bfs_stats: the Python mirror has the header's fields in order, and
+    one profile bucket name per kernel_ms slot (the eighth is the host loop's
+    gap after each level)."""
+    import gpugraph500_gb300 as g5
+    src = open(os.path.join(ROOT, "include", "g5bfs.h")).read()
+    body = re.search(r"typedef struct g5_bfs_stats\s*\{(.*?)\}\s*g5_bfs_stats;", src, flags=re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = re.findall(r"\b(\w+)(?:\[(\d+)\])?\s*;", body)
+    assert [f for f, _ in fields] == [f for f, _ in g5.BfsStats._fields_]
+    slots = dict(fields)["kernel_ms"]
+    assert int(slots) == len(g5.BfsStats.KERNELS) == 8
+    assert g5.BfsStats.KERNELS[-1] == "host"
