@@ -96,16 +96,26 @@ def test_codec_batch_bound(libg5):
     assert g5.Codec.batch_bound(np.zeros(1, np.uint64)) == 0
 
 
-def test_stats_struct_mirrors_header():
-    """g5_bfs_stats: the Python mirror has the header's fields in order, and
-    one profile bucket name per kernel_ms slot (the eighth is the host loop's
-    gap after each level)."""
+def _header_fields(src, name):
+    body = re.search(r"typedef struct " + name + r"\s*\{(.*?)\}\s*" + name + ";", src, flags=re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    return re.findall(r"\b(\w+)(?:\[(\d+)\])?\s*;", body)
+
+
+@pytest.mark.parametrize("cname,pyname", [("g5_bfs_config", "BfsConfig"), ("g5_bfs_stats", "BfsStats")])
+def test_structs_mirror_header(cname, pyname):
+    """The Python ctypes mirrors have the header's fields in the header's order
+    (a mismatch would shift every later field across the C ABI)."""
     import gpugraph500_gb300 as g5
     src = open(os.path.join(ROOT, "include", "g5bfs.h")).read()
-    body = re.search(r"typedef struct g5_bfs_stats\s*\{(.*?)\}\s*g5_bfs_stats;", src, flags=re.S).group(1)
-    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
-    fields = re.findall(r"\b(\w+)(?:\[(\d+)\])?\s*;", body)
-    assert [f for f, _ in fields] == [f for f, _ in g5.BfsStats._fields_]
-    slots = dict(fields)["kernel_ms"]
+    assert [f for f, _ in _header_fields(src, cname)] == [f for f, _ in getattr(g5, pyname)._fields_]
+
+
+def test_stats_profile_buckets():
+    """One profile bucket name per kernel_ms slot; the eighth is the host
+    loop's gap after each level."""
+    import gpugraph500_gb300 as g5
+    src = open(os.path.join(ROOT, "include", "g5bfs.h")).read()
+    slots = dict(_header_fields(src, "g5_bfs_stats"))["kernel_ms"]
     assert int(slots) == len(g5.BfsStats.KERNELS) == 8
     assert g5.BfsStats.KERNELS[-1] == "host"
